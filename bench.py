@@ -1,0 +1,329 @@
+"""Benchmark of the Mallard residual-and-update path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--n 1024]
+
+Workload (the 2D four-quadrant Riemann configuration): cartesian_tri mesh of
+n x n quads split into 2 n^2 triangles (n = 1024 -> 2,097,152 cells) on the
+unit square, relabelled by a seeded random cell permutation (seed 20261203)
+and reverse-Cuthill-McKee ordered inside the library; TENO p = 3 (legendre),
+HLLC, SSPRK3 with CFL 0.5, extrapolation (transmissive) boundaries, gamma
+1.4, quadrant states split at x = y = 0.8.  Synthetic, seeded data; FP64.
+The TENO weighting is the corrected variant (same work per cell as the
+reference's weighting, which turns this state non-finite within one step).
+
+One step = spectral radius + dt + three stages of (reconstruction, face flux,
+residual gather + update), all on the GPU, replayed as a CUDA graph.  Inputs
+(tables ~14 GB) are far larger than L2, so no explicit flush is done.
+
+Metric: Mcell-updates/s = cells x steps / seconds / 1e6 (one cell-update =
+one cell advanced one full SSPRK3 step).
+
+--impl reference times the CPU oracle (the restatement of the reference's
+algorithm, all host threads) on a 256 x 256 sample of the same workload.
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "tests"))
+
+METRIC = "Mcell-updates/s on 1 GB300: FP64 plain vs FP32+learned TENO at matched L1 error"
+UNIT = "Mcell-updates/s"
+SEED = 20261203
+CFL = 0.5
+CPU_SAMPLE_N = 256
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=1024, help="quads per side (cells = 2 n^2)")
+    ap.add_argument("--variant", default="corrected", choices=["reference", "corrected"])
+    ap.add_argument("--cpu-sample-n", type=int, default=CPU_SAMPLE_N)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
+
+
+def case_mesh(n):
+    import mallard_gb300 as mg
+    m = mg.Mesh.generate("cartesian_tri", n, n, 1.0, 1.0)
+    m.permute_cells(SEED)
+    return m
+
+
+def workload_config(args, n):
+    return {"workload": f"four-quadrant Riemann, cartesian_tri {n}x{n} quads -> {2 * n * n} triangles, "
+                        f"seeded permutation + RCM, TENO p3 legendre + HLLC, SSPRK3 CFL {CFL}, transmissive BCs",
+            "cells": 2 * n * n, "teno_variant": args.variant, "seed": SEED, "precision": "fp64",
+            "l2": "inputs larger than L2 (TENO tables ~7 KB/cell); no flush", "parallelism": "replicas"}
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+                power.append(float(parts[3]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm), "power_w_max": max(power) if power else None}
+
+
+# ---------------------------------------------------------------------------
+# CPU oracle leg
+# ---------------------------------------------------------------------------
+
+def cpu_oracle_rate(n, steps, warmup, variant):
+    """Cell-updates/s of the oracle on an n x n sample, all host threads."""
+    import numpy as np  # noqa: F401
+    from cases import four_quadrant
+    from oracle import Oracle, OracleCase, OracleMesh
+    m = case_mesh(n)
+    o = Oracle()
+    threads = max(1, os.cpu_count() or 1)
+    o.set_threads(threads)
+    oc = OracleCase(OracleMesh.from_arrays(m), recon="TENO", basis="legendre", poly_order=3, riemann="HLLC")
+    oc.set_teno_variant(0 if variant == "reference" else 1)
+    for z in range(1, 5):
+        oc.add_boundary(z, "extrapolation")
+    U, W = four_quadrant(m)
+    oc.set_state(U, W)
+    if warmup:
+        oc.run(CFL, warmup)
+    t0 = time.perf_counter()
+    oc.run(CFL, steps)
+    dt = time.perf_counter() - t0
+    return m.n_cells * steps / dt / 1e6, threads, dt, m.n_cells
+
+
+def run_reference(args):
+    rank, _, world = dist_env()
+    if rank != 0:
+        return
+    rate, threads, secs, cells = cpu_oracle_rate(args.cpu_sample_n, args.steps, args.warmup, args.variant)
+    sample = (f"cartesian_tri {args.cpu_sample_n}x{args.cpu_sample_n} ({cells} cells) of the same workload, "
+              f"{args.steps} timed steps after {args.warmup} warm-up, {threads} OpenMP threads")
+    line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": workload_config(args, args.n),
+            "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU leg
+# ---------------------------------------------------------------------------
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    import mallard_gb300 as mg
+    from cases import four_quadrant
+
+    rank, local, world = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(x):
+        if not dist:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    t_setup = time.perf_counter()
+    m = case_mesh(args.n)
+    solver = mg.Solver(m, face_reconstruction="TENO", basis_type="legendre", basis_order=3, riemann_solver="HLLC",
+                       boundaries=[{"name": z, "type": "extrapolation"} for z in ("right", "top", "left", "bottom")],
+                       teno_variant=args.variant, reorder=True, device=local)
+    setup_s = time.perf_counter() - t_setup
+    stream = torch.cuda.Stream()
+    solver.set_stream(stream.cuda_stream)
+    U0, W0 = four_quadrant(m)
+    cells = m.n_cells
+
+    # ---- timed region: K steps of the device-resident loop (CUDA graph)
+    solver.set_state(U0, W0)
+    solver.launch(CFL, args.warmup)
+    solver.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    barrier()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    solver.launch(CFL, args.steps)
+    ev1.record(stream)
+    ev1.synchronize()
+    barrier()
+    ms = ev0.elapsed_time(ev1)
+    clk = clocks.stop()
+    flags = solver.status()
+    Uend, _ = solver.get_state()
+    finite = bool(np.isfinite(Uend).all()) and flags == 0
+    ms_max = max_over_ranks(ms)
+    value = cells * args.steps * world / (ms_max * 1e-3) / 1e6
+
+    # ---- per-kernel times (same steps from the same state, events around each launch)
+    solver.set_state(U0, W0)
+    solver.launch(CFL, args.warmup)
+    solver.kernel_timing(True)
+    solver.launch(CFL, args.steps)
+    kt = solver.kernel_times()
+    solver.kernel_timing(False)
+
+    # ---- end to end through the public API with host buffers
+    Uh = torch.empty((cells, 4), dtype=torch.float64, pin_memory=True).numpy()
+    Wh = torch.empty((cells, 5), dtype=torch.float64, pin_memory=True).numpy()
+    Uh[:] = U0
+    Wh[:] = W0
+    barrier()
+    e0 = time.perf_counter()
+    for _ in range(args.steps):
+        solver.set_state(Uh, Wh)
+        solver.launch(CFL, 1)
+        solver.synchronize()
+        solver.get_state(Uh, Wh)
+    e_secs = max_over_ranks(time.perf_counter() - e0)
+    e2e_value = cells * args.steps * world / e_secs / 1e6
+    h2d = cells * (4 + 5) * 8
+    d2h = cells * (4 + 5) * 8
+
+    # ---- roofline of the dominant kernel (reconstruction)
+    recon_bytes, stage_bytes = solver.traffic_model()
+    peaks = {}
+    pk = ROOT / "MEASURED_PEAKS.json"
+    if pk.exists():
+        peaks = json.loads(pk.read_text())
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    recon_ms, recon_n = kt["recon"]
+    recon_avg_s = recon_ms / max(recon_n, 1) * 1e-3
+    achieved = recon_bytes / recon_avg_s / 1e9
+    traffic = None
+    tf = ROOT / "profiles" / "teno_recon_traffic.json"
+    if tf.exists():
+        t = json.loads(tf.read_text())
+        traffic = t.get("dram_bytes_per_cell", 0) * cells or None
+    kshare = {k: {"ms_per_launch": v[0] / max(v[1], 1), "launches": v[1], "share": v[0] / max(sum(x[0] for x in kt.values()), 1e-30)}
+              for k, v in kt.items()}
+    # FP64 arithmetic roof of the reconstruction (FP64 is the binding unit on GB300)
+    K, M, nq = 10, 20, 2
+    flops_cell = 4 * (4 * (2 * (M - 1) + 2 * (K - 1) * (M - 1) + 2 * (K - 1) ** 2 + 2 * (K - 1) + 14)
+                      + 3 * nq * (K - 1) * 3)
+    fp64_peak = mg.fp64_peak_gflops(local)
+    fp64_achieved = flops_cell * cells / recon_avg_s / 1e9
+    gpu_launches = args.steps * 11
+
+    cpu = None
+    if rank == 0 and world >= 1 and not args.no_cpu_baseline:
+        rate, threads, secs, ccells = cpu_oracle_rate(args.cpu_sample_n, 2, 1, args.variant)
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"cartesian_tri {args.cpu_sample_n}x{args.cpu_sample_n} ({ccells} cells) of the same "
+                         f"workload, 2 steps after 1 warm-up, {threads} OpenMP threads, {secs:.1f} s"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": workload_config(args, args.n),
+                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                "gpu_launches": gpu_launches,
+                "clocks": clk,
+                "roofline": {"bound": "hbm", "kernel": "teno_kernel<10,20,2>", "achieved": achieved,
+                             "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                             "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if pk.exists() else "fallback",
+                             "traffic": traffic, "algorithmic_bytes_per_launch": recon_bytes},
+                "fp64_roof": {"achieved_gflops": fp64_achieved, "peak_gflops": fp64_peak,
+                              "frac": fp64_achieved / fp64_peak, "flops_per_cell": flops_cell,
+                              "peak_source": "measured FMA-chain probe on this GPU"},
+                "kernels": kshare, "stage_bytes": stage_bytes, "finite": finite, "status_flags": flags,
+                "setup_s": setup_s, "cpu_baseline": cpu}
+        print(json.dumps(line), flush=True)
+    solver.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,228 @@
+/*
+ * mallard_gb300.h -- C ABI of the GB300 residual-and-update path for the
+ * Mallard finite-volume solver (TENO reconstruction -> face flux ->
+ * residual assembly -> SSPRK3 stage update, with primitive recovery and the
+ * CFL reduction), for one GPU.
+ *
+ * Plain C: pointers, sizes and status codes; no C++ or framework types.
+ * Every call returns MGPU_OK (0) or an error code; mgpu_last_error() gives
+ * the message of the last failure on the calling thread.  Host arrays are
+ * borrowed for the duration of a call; device memory is owned by the context.
+ *
+ * Array conventions follow the reference's host views (row-major):
+ *   U (conservatives)  [n_cells][4]            rho, rho*u, rho*v, rho*E
+ *   primitives         [n_cells][5]            u, v, p, T, h
+ *   face values        [n_faces][n_q][2][4]    side 0 = cells_of_face(f,0)
+ *   rhs                [n_cells][4]
+ * Cell and face numbering at this boundary is always the caller's (the
+ * reference Mesh's); the library reorders internally.
+ *
+ * Reference interfaces each entry point replaces (paths inside the
+ * MatthewBonanni/Mallard tree):
+ *   mgpu_create/mgpu_add_boundary/mgpu_finalize
+ *        -> Solver::init_numerics + init_boundaries (src/solver/solver.cpp:110-237),
+ *           TENO::init (src/numerics/face_reconstruction.cpp:109-152)
+ *   mgpu_calc_face_values
+ *        -> FaceReconstruction::calc_face_values (src/numerics/face_reconstruction.h:82-83)
+ *   mgpu_calc_rhs
+ *        -> Solver::calc_rhs (src/solver/solver_rhs.cpp:44-55), which runs
+ *           InteriorFluxFunctor (src/numerics/flux_functor.h:124-178) and
+ *           Boundary::apply (src/boundary/boundary.h:115-116)
+ *   mgpu_take_step
+ *        -> SSPRK3::take_step (src/numerics/time_integrator.cpp:135-163)
+ *           + Solver::update_primitives (src/solver/solver.cpp:568-578)
+ *   mgpu_calc_dt
+ *        -> Solver::calc_dt / calc_spectral_radius (src/solver/solver.cpp:580-742)
+ *   mgpu_run
+ *        -> the time-step loop of Solver::run (src/solver/solver.cpp:352-373)
+ *   mgpu_riemann_flux_batch
+ *        -> RiemannSolver::calc_flux (src/numerics/riemann_solver.h:85-90)
+ *   mgpu_primitives_batch
+ *        -> Physics::compute_primitives_from_conservatives (src/physics/physics.h:274-278)
+ *   mgpu_mesh_*
+ *        -> Mesh::init_cart / init_cart_tri / init_wedge and the derived
+ *           geometry (src/mesh/mesh.cpp:167-261, 305-848)
+ */
+#ifndef MALLARD_GB300_H
+#define MALLARD_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define MGPU_OK 0
+#define MGPU_ERR_ARG 1         /* invalid argument or configuration          */
+#define MGPU_ERR_CUDA 2        /* a CUDA runtime call failed                 */
+#define MGPU_ERR_NAN 3         /* a non-finite state or time step was seen   */
+#define MGPU_ERR_TIMEOUT 4     /* a bounded device wait gave up              */
+#define MGPU_ERR_STATE 5       /* call out of order (e.g. before finalize)   */
+#define MGPU_ERR_UNSUPPORTED 6 /* configuration not built for the GPU path   */
+#define MGPU_ERR_HOST 7        /* host-side failure (allocation, table build) */
+
+/* ---- enumerations (values match the reference's string keys) ----------- */
+enum { MGPU_MESH_CARTESIAN = 0, MGPU_MESH_CARTESIAN_TRI = 1, MGPU_MESH_WEDGE = 2 };
+enum { MGPU_RECON_FO = 0, MGPU_RECON_TENO = 1 };
+enum { MGPU_BASIS_MONOMIAL = 0, MGPU_BASIS_LEGENDRE = 1 };
+enum { MGPU_RIEMANN_RUSANOV = 0, MGPU_RIEMANN_HLL = 1, MGPU_RIEMANN_HLLC = 2 };
+enum { MGPU_INTEGRATOR_SSPRK3 = 0 };
+enum {
+    MGPU_BC_SYMMETRY = 0,
+    MGPU_BC_EXTRAPOLATION = 1,
+    MGPU_BC_WALL_ADIABATIC = 2,
+    MGPU_BC_UPT = 3,
+    MGPU_BC_P_OUT = 4
+};
+/* TENO weighting: 0 = the reference's arithmetic, quirks included;
+ * 1 = corrected cut-off weights, zero-mean evaluation basis and a
+ * positivity fallback in the face flux (same work per cell). */
+enum { MGPU_TENO_REFERENCE = 0, MGPU_TENO_CORRECTED = 1 };
+/* Arithmetic of the GPU path. */
+enum { MGPU_PREC_FP64 = 0 };
+
+/* ---- mesh view: exactly the reference Mesh's public arrays (mesh.h:228-253)
+ * plus its face zones (zone 0 is "interior", mesh.h:98-104). ------------- */
+typedef struct mgpu_mesh {
+    uint32_t n_nodes, n_cells, n_faces;
+    const double* node_coords;             /* [n_nodes][2]                   */
+    const double* cell_coords;             /* [n_cells][2] vertex centroid   */
+    const double* cell_volume;             /* [n_cells]                      */
+    const double* face_area;               /* [n_faces]                      */
+    const double* face_normals;            /* [n_faces][2] area-weighted      */
+    const uint32_t* offsets_nodes_of_cell; /* [n_cells+1]                    */
+    const uint32_t* nodes_of_cell;
+    const uint32_t* offsets_faces_of_cell; /* [n_cells+1]                    */
+    const uint32_t* faces_of_cell;
+    const uint32_t* offsets_nodes_of_face; /* [n_faces+1]                    */
+    const uint32_t* nodes_of_face;
+    const int32_t* cells_of_face;          /* [n_faces][2], -1 = boundary    */
+    uint32_t n_zones;                      /* face zones, zone 0 = interior  */
+    const uint32_t* zone_offsets;          /* [n_zones+1]                    */
+    const uint32_t* zone_faces;
+} mgpu_mesh;
+
+typedef struct mgpu_mesh_buf mgpu_mesh_buf; /* an owning host mesh */
+
+/* Generate one of the reference's meshes (same numbering and geometry). */
+int mgpu_mesh_generate(int mesh_type, uint32_t nx, uint32_t ny, double Lx, double Ly, mgpu_mesh_buf** out);
+/* Build a mesh from connectivity (the reference's unimplemented FILE type):
+ * geometry is derived with the reference's formulas. */
+int mgpu_mesh_from_connectivity(uint32_t n_nodes, const double* node_coords, uint32_t n_cells,
+                                const uint32_t* offsets_nodes_of_cell, const uint32_t* nodes_of_cell,
+                                const uint32_t* offsets_faces_of_cell, const uint32_t* faces_of_cell,
+                                uint32_t n_faces, const uint32_t* offsets_nodes_of_face,
+                                const uint32_t* nodes_of_face, const int32_t* cells_of_face, uint32_t n_zones,
+                                const uint32_t* zone_offsets, const uint32_t* zone_faces, mgpu_mesh_buf** out);
+/* Relabel cells with a seeded random permutation (mt19937_64, Fisher-Yates).
+ * new_of_old (optional, [n_cells]) receives the permutation. */
+int mgpu_mesh_permute_cells(mgpu_mesh_buf* m, uint64_t seed, uint32_t* new_of_old);
+int mgpu_mesh_view(const mgpu_mesh_buf* m, mgpu_mesh* view);
+void mgpu_mesh_free(mgpu_mesh_buf* m);
+
+/* ---- TENO tables (host) ----------------------------------------------- */
+/* The tables TENO::init builds (face_reconstruction.cpp:109-788), in the
+ * reference's layout (face_reconstruction.h:195-260), built on the host
+ * without a GPU.  mgpu_finalize builds the same tables itself (in its tiled
+ * device layout); this entry point exposes them for inspection. */
+typedef struct mgpu_teno_tables mgpu_teno_tables;
+enum {
+    MGPU_TENO_OFFSETS_STENCIL_GROUPS = 0, /* uint32 [n_cells+1]             */
+    MGPU_TENO_OFFSETS_STENCILS = 1,       /* uint32 [n_stencils+1]          */
+    MGPU_TENO_STENCILS = 2,               /* uint32                         */
+    MGPU_TENO_OFFSETS_MATRICES = 3,       /* uint32 [n_stencils+1]          */
+    MGPU_TENO_MATRICES = 4,               /* double, K x M_s row-major each */
+    MGPU_TENO_TRANSFORMED_AREAS = 5,      /* double                         */
+    MGPU_TENO_INTEGRAL_PSI_TARGET = 6,    /* double [K]                     */
+    MGPU_TENO_OSCILLATION_INDICATOR = 7,  /* double [K][K]                  */
+    MGPU_TENO_POLY_INDICES = 8            /* int32 [K][2]                   */
+};
+int mgpu_teno_tables_build(const mgpu_mesh* mesh, int basis, int poly_order, double stencil_factor, int q_cell,
+                           int q_face, mgpu_teno_tables** out);
+uint64_t mgpu_teno_tables_len(const mgpu_teno_tables* t, int field);
+int mgpu_teno_tables_copy(const mgpu_teno_tables* t, int field, void* dst);
+void mgpu_teno_tables_free(mgpu_teno_tables* t);
+
+/* ---- solver context ---------------------------------------------------- */
+typedef struct mgpu_config {
+    int recon;                      /* MGPU_RECON_*                          */
+    int basis;                      /* MGPU_BASIS_*                          */
+    int poly_order;                 /* TENO basis order (1..3 on the GPU)    */
+    double max_stencil_size_factor; /* reference default 2.0                 */
+    int quadrature_order_cell;      /* 0 = reference default p+1             */
+    int quadrature_order_face;      /* 0 = reference default (p+1)/2         */
+    int riemann_solver;             /* MGPU_RIEMANN_*                        */
+    int time_integrator;            /* MGPU_INTEGRATOR_SSPRK3                */
+    double gamma, p_ref, T_ref, rho_ref, p_min, p_max; /* physics (physics.cpp:27-53) */
+    int teno_variant;               /* MGPU_TENO_*                           */
+    int precision;                  /* MGPU_PREC_*                           */
+    int reorder;                    /* 1 = reverse Cuthill-McKee cell order  */
+    int device;                     /* CUDA device ordinal                   */
+} mgpu_config;
+
+typedef struct mgpu_ctx mgpu_ctx;
+
+/* Fill cfg with the reference's defaults (TENO p=3 legendre, HLLC, SSPRK3,
+ * gamma 1.4, reference state of physics_test.cpp, p clip +-1e20). */
+void mgpu_config_defaults(mgpu_config* cfg);
+int mgpu_create(const mgpu_mesh* mesh, const mgpu_config* cfg, mgpu_ctx** out);
+/* Boundaries are applied in the order added, like the TOML [[boundaries]]
+ * list.  data: upt = (u, v, p, T); p_out = (p); others none. */
+int mgpu_add_boundary(mgpu_ctx* ctx, uint32_t zone, int bc_type, const double* data, int n_data);
+/* Build the TENO tables (host), reorder, upload; required before compute. */
+int mgpu_finalize(mgpu_ctx* ctx);
+int mgpu_destroy(mgpu_ctx* ctx);
+/* Launch on a caller stream (cudaStream_t passed as void*); NULL = own stream. */
+int mgpu_set_stream(mgpu_ctx* ctx, void* stream);
+int mgpu_synchronize(mgpu_ctx* ctx);
+
+int mgpu_set_state(mgpu_ctx* ctx, const double* U, const double* primitives);
+int mgpu_get_state(mgpu_ctx* ctx, double* U, double* primitives);
+
+/* Parity hooks (host buffers in, host buffers out). */
+int mgpu_calc_face_values(mgpu_ctx* ctx, const double* U, double* face_values, uint8_t* teno_masks);
+int mgpu_calc_rhs(mgpu_ctx* ctx, const double* U, double* rhs);
+
+/* Time stepping on the resident state. */
+int mgpu_calc_dt(mgpu_ctx* ctx, double cfl, double* dt, double* cfl_local);
+int mgpu_take_step(mgpu_ctx* ctx, double dt);
+/* n_steps x (spectral radius -> dt = cfl / max -> SSPRK3 step) without host
+ * round trips; t_out (optional) receives the simulated time advanced. */
+int mgpu_run(mgpu_ctx* ctx, double cfl, uint32_t n_steps, double* t_out);
+/* Device error flags: bit 0 non-finite state, bit 1 non-positive dt. */
+int mgpu_status(mgpu_ctx* ctx, uint32_t* flags);
+
+/* Diagnostics for measurement.  Kernel timing brackets every launch of the
+ * reconstruction, flux, update and CFL kernels with CUDA events on the
+ * launching stream; mgpu_kernel_times returns, per kernel class
+ * (0 recon, 1 flux, 2 update, 3 cfl), the summed milliseconds and launch
+ * counts since the last reset. */
+int mgpu_enable_kernel_timing(mgpu_ctx* ctx, int enable);
+int mgpu_kernel_times(mgpu_ctx* ctx, double* ms, uint32_t* launches);
+/* Algorithmic (compulsory) bytes one reconstruction launch and one full
+ * stage move, from the actual table sizes. */
+int mgpu_traffic_model(mgpu_ctx* ctx, double* recon_bytes, double* stage_bytes);
+uint32_t mgpu_n_cells(const mgpu_ctx* ctx);
+
+/* ---- unit-level GPU entry points (known-answer tests) ------------------ */
+/* n independent Riemann problems; arrays: n_unit [n][2], u_l/u_r [n][2],
+ * scalars [n]; flux [n][4].  Host buffers. */
+int mgpu_riemann_flux_batch(int solver, uint32_t n, const double* n_unit, const double* rho_l, const double* u_l,
+                            const double* p_l, const double* gamma_l, const double* h_l, const double* rho_r,
+                            const double* u_r, const double* p_r, const double* gamma_r, const double* h_r,
+                            double* flux);
+/* Euler primitive recovery for n states on the GPU. */
+int mgpu_primitives_batch(double gamma, double p_ref, double T_ref, double rho_ref, double p_min, double p_max,
+                          uint32_t n, const double* U, double* primitives);
+/* FP64 FMA throughput probe: returns measured GFLOP/s (2 flops per FMA). */
+int mgpu_probe_fp64_gflops(int device, double* gflops);
+
+const char* mgpu_last_error(void);
+int mgpu_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MALLARD_GB300_H */

@@ -1,0 +1,111 @@
+// device.h -- parameter blocks shared by the host context and the kernels.
+//
+// Device layout (cells and faces in the library's internal order):
+//   U, Utmp, W        double [n_cells][4]          conserved state, AoS (32 B/cell)
+//   prim              double [n_cells][5]
+//   TENO tables, tiled by 8 cells so that one warp (8 cells x 4 variables)
+//   reads 64 contiguous bytes per table entry:
+//     nb    uint32 [tiles][4 stencils][M-1][8]     neighbour cells (target dropped)
+//     ar    double [tiles][4][M-1][8]              transformed areas
+//     P     double [tiles][4][M-1][K-1][8]         pseudo-inverse, dof 0 and column 0
+//                                                  dropped (exact zeros in the reference)
+//     phi   double [tiles][3 faces][n_q][K-1][8]   basis shape value at each face point
+//     cface uint32 [tiles][3][8]                   face slot * 2 + side
+//   fv    double [n_faces][n_q][2][4]             reconstructed face states
+//   G     double [n_flux_faces][4]                face-area x numerical flux
+#pragma once
+
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "../../include/mallard_gb300.h"
+
+namespace mgpu {
+
+constexpr int TILE = 8;
+constexpr int MAX_BC = 16;
+constexpr int KR_MAX = 9;  // K-1 for p = 3
+
+struct GasParams {
+    double gamma, R, cv, p_min, p_max;
+};
+
+struct BcEntry {
+    int type;
+    double data[6];
+};
+
+struct BcTable {
+    int n;
+    BcEntry bc[MAX_BC];
+};
+
+struct TenoArgs {
+    int n_cells;
+    const uint32_t* nb;
+    const double* ar;
+    const double* P;
+    const double* phi;
+    const uint32_t* cface;
+    const uint8_t* smask;
+    double oi[KR_MAX * KR_MAX];  // oscillation indicator without dof 0, row-major (K-1)^2
+};
+
+struct FluxArgs {
+    int n_faces;            // faces that carry a flux
+    const int2* lr;         // internal cell ids; y = -1 on boundary faces
+    const double2* nrm;     // unit normal (reference unit<2> arithmetic, precomputed)
+    const double* area;
+    const int8_t* bc;       // -1 interior, else BcTable index
+    const double* fv;
+    double* G;
+    const double* U;        // stage input, for the positivity fallback
+    double qw[4];           // face quadrature weights
+};
+
+struct UpdateArgs {
+    int n_cells;
+    const int4* gat;        // per cell up to 4 (face*2 + negate) in the reference's summation order, -1 = none
+    const double* G;
+    const double* vol;
+    const double* dt;       // device scalar
+    double* U;              // stage-1 base; final state after stage 3
+    double* Ut;             // stage state
+    double* W;              // running sum U + dt/6 k1 + dt/6 k2
+    double* prim;
+    double* rhs;            // residual output (stage 0 only)
+    unsigned* flags;
+};
+
+struct SpecArgs {
+    int n_cells;
+    const int4* cfaces;     // faces of the cell in the reference's order, -1 = none
+    const int2* lr;
+    const double2* nrm;
+    const double* dxn;      // |s . n| with the reference's boundary rule, precomputed
+    const double* U;
+    const double* prim;
+    double* rho_cell;
+    unsigned long long* rmax_bits;
+    double gamma;
+};
+
+// Launchers (kernels.cu).  All return cudaGetLastError() of the launch.
+cudaError_t launch_teno(const TenoArgs& a, int K, int M, int nq, int variant, const double* U, double* fv,
+                        uint8_t* masks, cudaStream_t s);
+cudaError_t launch_first_order(int n_faces, const int2* lr, const double* U, double* fv, cudaStream_t s);
+cudaError_t launch_flux(const FluxArgs& a, const GasParams& g, const BcTable& bct, int rsolver, int nq,
+                        bool positivity, cudaStream_t s);
+cudaError_t launch_update(const UpdateArgs& a, const GasParams& g, int stage, cudaStream_t s);
+cudaError_t launch_spectral(const SpecArgs& a, cudaStream_t s);
+cudaError_t launch_dt(const unsigned long long* rmax_bits, double cfl, double* dt, double* t, unsigned* flags,
+                      cudaStream_t s);
+cudaError_t launch_set_scalar(double* dst, double value, cudaStream_t s);
+cudaError_t launch_permute_rows(int n, int width, const uint32_t* idx, const double* src, double* dst, bool scatter,
+                                cudaStream_t s);
+cudaError_t launch_riemann_batch(int rsolver, uint32_t n, const double* buf_in, double* flux, cudaStream_t s);
+cudaError_t launch_primitives_batch(const GasParams& g, uint32_t n, const double* U, double* W, cudaStream_t s);
+cudaError_t run_fp64_probe(int device, double* gflops);
+
+}  // namespace mgpu

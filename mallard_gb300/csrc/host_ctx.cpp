@@ -1,0 +1,1029 @@
+// host_ctx.cpp -- the solver context behind the C ABI: device layout,
+// reordering, launch sequencing and the parity hooks.
+//
+// Boundary semantics follow the reference's classes:
+//   mgpu_finalize        ~ TENO::init + Solver::allocate_memory
+//   mgpu_calc_face_values~ FaceReconstruction::calc_face_values
+//   mgpu_calc_rhs        ~ Solver::calc_rhs (solver_rhs.cpp:44-115)
+//   mgpu_take_step       ~ SSPRK3::take_step + update_primitives
+//   mgpu_calc_dt         ~ Solver::calc_dt (solver.cpp:580-590)
+// Errors never cross the ABI as exceptions: every entry point returns a
+// status and records a message for mgpu_last_error().
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <numeric>
+#include <queue>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "device.h"
+#include "host.h"
+
+namespace mgpu {
+
+namespace {
+thread_local std::string g_error;
+
+struct CudaFail : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+struct ArgFail : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+struct Unsupported : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+
+void ck(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) throw CudaFail(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+template <class T>
+struct DevArray {
+    T* p = nullptr;
+    size_t n = 0;
+    DevArray() = default;
+    DevArray(const DevArray&) = delete;
+    DevArray& operator=(const DevArray&) = delete;
+    ~DevArray() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    void alloc(size_t count) {
+        release();
+        if (count == 0) count = 1;
+        ck(cudaMalloc(&p, count * sizeof(T)), "cudaMalloc");
+        n = count;
+        ck(cudaMemset(p, 0, count * sizeof(T)), "cudaMemset");
+    }
+    void upload(const std::vector<T>& v) {
+        alloc(v.size());
+        if (!v.empty()) ck(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), "cudaMemcpy H2D");
+    }
+    size_t bytes() const { return n * sizeof(T); }
+};
+
+// reverse Cuthill-McKee over the face-neighbour graph; returns old_of_new
+std::vector<uint32_t> rcm_order(uint32_t n, const std::vector<std::vector<uint32_t>>& adj) {
+    std::vector<uint32_t> order;
+    order.reserve(n);
+    std::vector<char> seen(n, 0);
+    std::vector<uint32_t> by_degree(n);
+    std::iota(by_degree.begin(), by_degree.end(), 0u);
+    std::stable_sort(by_degree.begin(), by_degree.end(),
+                     [&](uint32_t a, uint32_t b) { return adj[a].size() < adj[b].size(); });
+    std::vector<uint32_t> nb;
+    for (uint32_t start : by_degree) {
+        if (seen[start]) continue;
+        size_t head = order.size();
+        order.push_back(start);
+        seen[start] = 1;
+        while (head < order.size()) {
+            const uint32_t c = order[head++];
+            nb.clear();
+            for (uint32_t x : adj[c])
+                if (!seen[x]) nb.push_back(x);
+            std::sort(nb.begin(), nb.end(), [&](uint32_t a, uint32_t b) {
+                return adj[a].size() != adj[b].size() ? adj[a].size() < adj[b].size() : a < b;
+            });
+            for (uint32_t x : nb) {
+                seen[x] = 1;
+                order.push_back(x);
+            }
+        }
+    }
+    std::reverse(order.begin(), order.end());
+    return order;
+}
+
+struct BcHost {
+    uint32_t zone;
+    int type;
+    double data[6];
+};
+
+}  // namespace
+
+void set_error(const std::string& msg) { g_error = msg; }
+
+}  // namespace mgpu
+
+using namespace mgpu;
+
+struct mgpu_ctx {
+    mgpu_config cfg{};
+    HostMesh mesh;
+    std::vector<BcHost> bcs;
+    bool finalized = false;
+    GasParams gas{};
+    BcTable bct{};
+    int nq = 1, K = 0, M = 0;
+    double qw[4] = {0, 0, 0, 0};
+
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+
+    // numbering: internal <-> caller
+    uint32_t N = 0;
+    std::vector<uint32_t> cell_new, cell_old;
+    uint32_t F_flux = 0, F_real = 0;
+    std::vector<int32_t> face_new;
+    std::vector<uint32_t> face_old;
+
+    // device state and work arrays
+    DevArray<double> U, Ut, W, prim, vol, fv, G, rho_cell, rhs, scal;  // scal: dt, t
+    DevArray<unsigned> flags;
+    DevArray<unsigned long long> rmax;
+    DevArray<int2> lr;
+    DevArray<double2> nrm;
+    DevArray<double> area, dxn;
+    DevArray<int8_t> bcidx;
+    DevArray<int4> gat, cfaces;
+    DevArray<uint32_t> nb, cface;
+    DevArray<double> ar, P, phi;
+    DevArray<uint8_t> smask, masks;
+    DevArray<double> staging;      // caller-order rows for state transfers
+    DevArray<uint32_t> perm_old;   // internal cell -> caller cell
+    TenoArgs teno{};
+
+    // CUDA graph of one CFL step, keyed by cfl
+    cudaGraphExec_t step_exec = nullptr;
+    double step_cfl = -1.0;
+
+    // per-launch timing
+    bool timing = false;
+    struct Mark {
+        int cls;
+        cudaEvent_t a, b;
+    };
+    std::vector<Mark> marks;
+    size_t marks_used = 0;
+    double recon_bytes = 0, stage_bytes = 0;
+
+    ~mgpu_ctx() {
+        if (step_exec) cudaGraphExecDestroy(step_exec);
+        for (auto& m : marks) {
+            cudaEventDestroy(m.a);
+            cudaEventDestroy(m.b);
+        }
+        if (own_stream && stream) cudaStreamDestroy(stream);
+    }
+
+    double* dt_ptr() { return scal.p; }
+    double* t_ptr() { return scal.p + 1; }
+
+    // ---- launch helpers ---------------------------------------------------
+    template <class F>
+    void timed(int cls, F&& launch) {
+        if (!timing) {
+            ck(launch(), "kernel launch");
+            return;
+        }
+        if (marks_used == marks.size()) {
+            Mark m{cls, nullptr, nullptr};
+            ck(cudaEventCreate(&m.a), "cudaEventCreate");
+            ck(cudaEventCreate(&m.b), "cudaEventCreate");
+            marks.push_back(m);
+        }
+        Mark& m = marks[marks_used++];
+        m.cls = cls;
+        ck(cudaEventRecord(m.a, stream), "cudaEventRecord");
+        ck(launch(), "kernel launch");
+        ck(cudaEventRecord(m.b, stream), "cudaEventRecord");
+    }
+
+    void reconstruct(const double* Uin, uint8_t* mask_out) {
+        if (cfg.recon == MGPU_RECON_TENO) {
+            timed(0, [&] { return launch_teno(teno, K, M, nq, cfg.teno_variant, Uin, fv.p, mask_out, stream); });
+        } else {
+            timed(0, [&] { return launch_first_order((int)F_flux, lr.p, Uin, fv.p, stream); });
+        }
+    }
+
+    void flux(const double* Uin) {
+        FluxArgs a{};
+        a.n_faces = (int)F_flux;
+        a.lr = lr.p;
+        a.nrm = nrm.p;
+        a.area = area.p;
+        a.bc = bcidx.p;
+        a.fv = fv.p;
+        a.G = G.p;
+        a.U = Uin;
+        for (int i = 0; i < 4; i++) a.qw[i] = qw[i];
+        const bool pos = cfg.recon == MGPU_RECON_TENO && cfg.teno_variant == MGPU_TENO_CORRECTED;
+        timed(1, [&] { return launch_flux(a, gas, bct, cfg.riemann_solver, nq, pos, stream); });
+    }
+
+    UpdateArgs update_args() {
+        UpdateArgs a{};
+        a.n_cells = (int)N;
+        a.gat = gat.p;
+        a.G = G.p;
+        a.vol = vol.p;
+        a.dt = dt_ptr();
+        a.U = U.p;
+        a.Ut = Ut.p;
+        a.W = W.p;
+        a.prim = prim.p;
+        a.rhs = rhs.p;
+        a.flags = flags.p;
+        return a;
+    }
+
+    void stage(int k) {
+        const double* in = (k == 1) ? U.p : Ut.p;
+        reconstruct(in, nullptr);
+        flux(in);
+        UpdateArgs a = update_args();
+        timed(2, [&] { return launch_update(a, gas, k, stream); });
+    }
+
+    void spectral_and_dt(double cfl, bool accumulate_t) {
+        ck(cudaMemsetAsync(rmax.p, 0, sizeof(unsigned long long), stream), "cudaMemsetAsync");
+        SpecArgs s{};
+        s.n_cells = (int)N;
+        s.cfaces = cfaces.p;
+        s.lr = lr.p;
+        s.nrm = nrm.p;
+        s.dxn = dxn.p;
+        s.U = U.p;
+        s.prim = prim.p;
+        s.rho_cell = rho_cell.p;
+        s.rmax_bits = rmax.p;
+        s.gamma = gas.gamma;
+        timed(3, [&] { return launch_spectral(s, stream); });
+        ck(launch_dt(rmax.p, cfl, dt_ptr(), accumulate_t ? t_ptr() : nullptr, flags.p, stream), "dt launch");
+    }
+
+    void cfl_step(double cfl) {
+        spectral_and_dt(cfl, true);
+        stage(1);
+        stage(2);
+        stage(3);
+    }
+
+    // ---- host <-> device in caller numbering ------------------------------
+    // One copy engine transfer of the caller's buffer (pinned or pageable)
+    // into a staging array, then a permutation kernel on the device.
+    void upload_cells(double* dst, const double* src, int width) {
+        const size_t bytes = (size_t)N * width * sizeof(double);
+        ck(cudaMemcpyAsync(staging.p, src, bytes, cudaMemcpyHostToDevice, stream), "H2D");
+        ck(launch_permute_rows((int)N, width, perm_old.p, staging.p, dst, false, stream), "permute");
+        ck(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+    }
+    void download_cells(const double* src, double* dst, int width) {
+        const size_t bytes = (size_t)N * width * sizeof(double);
+        ck(launch_permute_rows((int)N, width, perm_old.p, src, staging.p, true, stream), "permute");
+        ck(cudaMemcpyAsync(dst, staging.p, bytes, cudaMemcpyDeviceToHost, stream), "D2H");
+        ck(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+    }
+
+    void build();
+};
+
+// ---------------------------------------------------------------------------
+// mgpu_finalize: numbering, geometry precomputation, TENO tables, upload
+// ---------------------------------------------------------------------------
+void mgpu_ctx::build() {
+    const mgpu_mesh mv = mesh.view();
+    N = mv.n_cells;
+    if (N == 0) throw ArgFail("mesh has no cells");
+    if (mv.n_zones < 1) throw ArgFail("mesh has no interior zone");
+
+    // --- real faces: the union of all zones; flux faces: interior + applied BCs
+    std::vector<int> zone_bc(mv.n_zones, -2);  // -2 unused zone, -1 interior, else bc index
+    zone_bc[0] = -1;
+    for (size_t i = 0; i < bcs.size(); ++i) {
+        if (zone_bc[bcs[i].zone] != -2) throw ArgFail("a face zone carries more than one boundary condition");
+        zone_bc[bcs[i].zone] = (int)i;
+    }
+    std::vector<int> face_bc(mv.n_faces, -3);  // -3 not real
+    for (uint32_t z = 0; z < mv.n_zones; ++z)
+        for (uint32_t k = mv.zone_offsets[z]; k < mv.zone_offsets[z + 1]; ++k) {
+            const uint32_t f = mv.zone_faces[k];
+            if (face_bc[f] != -3) throw ArgFail("a face belongs to more than one zone");
+            face_bc[f] = zone_bc[z];
+        }
+    for (uint32_t c = 0; c < N; ++c) {
+        const uint32_t nf = mv.offsets_faces_of_cell[c + 1] - mv.offsets_faces_of_cell[c];
+        if (nf < 3 || nf > 4) throw Unsupported("cells must have 3 or 4 faces");
+        for (uint32_t k = mv.offsets_faces_of_cell[c]; k < mv.offsets_faces_of_cell[c + 1]; ++k)
+            if (face_bc[mv.faces_of_cell[k]] == -3) throw ArgFail("a face of a cell belongs to no zone");
+    }
+
+    // --- cell order
+    cell_old.resize(N);
+    if (cfg.reorder) {
+        std::vector<std::vector<uint32_t>> adj(N);
+        for (uint32_t f = 0; f < mv.n_faces; ++f) {
+            if (face_bc[f] == -3) continue;
+            const int32_t a = mv.cells_of_face[2 * (size_t)f], b = mv.cells_of_face[2 * (size_t)f + 1];
+            if (b >= 0) {
+                adj[a].push_back((uint32_t)b);
+                adj[b].push_back((uint32_t)a);
+            }
+        }
+        cell_old = rcm_order(N, adj);
+    } else {
+        std::iota(cell_old.begin(), cell_old.end(), 0u);
+    }
+    cell_new.assign(N, 0);
+    for (uint32_t c = 0; c < N; ++c) cell_new[cell_old[c]] = c;
+
+    // --- face order: flux faces by internal left cell, then the rest
+    std::vector<uint32_t> flux_faces, other_faces;
+    for (uint32_t f = 0; f < mv.n_faces; ++f) {
+        if (face_bc[f] == -3) continue;
+        (face_bc[f] == -2 ? other_faces : flux_faces).push_back(f);
+    }
+    auto key = [&](uint32_t f) {
+        const int32_t a = mv.cells_of_face[2 * (size_t)f], b = mv.cells_of_face[2 * (size_t)f + 1];
+        return std::make_pair(cell_new[a], b >= 0 ? cell_new[b] : 0xffffffffu);
+    };
+    std::stable_sort(flux_faces.begin(), flux_faces.end(), [&](uint32_t x, uint32_t y) { return key(x) < key(y); });
+    F_flux = (uint32_t)flux_faces.size();
+    F_real = F_flux + (uint32_t)other_faces.size();
+    face_old = flux_faces;
+    face_old.insert(face_old.end(), other_faces.begin(), other_faces.end());
+    face_new.assign(mv.n_faces, -1);
+    for (uint32_t i = 0; i < F_real; ++i) face_new[face_old[i]] = (int32_t)i;
+
+    // --- per-face geometry (reference unit<2>, spectral-radius distance)
+    std::vector<int2> h_lr(F_real);
+    std::vector<double2> h_nrm(F_real);
+    std::vector<double> h_area(F_real), h_dxn(F_real);
+    std::vector<int8_t> h_bc(F_real, -1);
+    for (uint32_t i = 0; i < F_real; ++i) {
+        const uint32_t f = face_old[i];
+        const int32_t a = mv.cells_of_face[2 * (size_t)f], b = mv.cells_of_face[2 * (size_t)f + 1];
+        h_lr[i] = make_int2((int)cell_new[a], b >= 0 ? (int)cell_new[b] : -1);
+        const double* nv = mv.face_normals + 2 * (size_t)f;
+        const double inv = 1 / std::sqrt(nv[0] * nv[0] + nv[1] * nv[1]);
+        const double n0 = nv[0] * inv, n1 = nv[1] * inv;
+        h_nrm[i] = make_double2(n0, n1);
+        h_area[i] = mv.face_area[f];
+        double s0, s1;
+        if (b == -1) {
+            s0 = 2.0 * std::pow(mv.cell_volume[a], 1.0 / 2);
+            s1 = 2.0 * std::pow(mv.cell_volume[a], 1.0 / 2);
+        } else {
+            s0 = mv.cell_coords[2 * (size_t)b] - mv.cell_coords[2 * (size_t)a];
+            s1 = mv.cell_coords[2 * (size_t)b + 1] - mv.cell_coords[2 * (size_t)a + 1];
+        }
+        h_dxn[i] = std::fabs(s0 * n0 + s1 * n1);
+        if (i < F_flux && face_bc[f] >= 0) h_bc[i] = (int8_t)face_bc[f];
+    }
+
+    // --- per-cell gather list in the reference's summation order
+    std::vector<int4> h_gat(N, make_int4(-1, -1, -1, -1)), h_cf(N, make_int4(-1, -1, -1, -1));
+    std::vector<int> fill(N, 0);
+    auto push = [&](uint32_t cold, int val) {
+        const uint32_t c = cell_new[cold];
+        if (fill[c] >= 4) throw Unsupported("a cell receives more than 4 face fluxes");
+        int* e = &h_gat[c].x;
+        e[fill[c]++] = val;
+    };
+    for (uint32_t k = mv.zone_offsets[0]; k < mv.zone_offsets[1]; ++k) {
+        const uint32_t f = mv.zone_faces[k];
+        const int fn = face_new[f];
+        const int32_t a = mv.cells_of_face[2 * (size_t)f], b = mv.cells_of_face[2 * (size_t)f + 1];
+        push((uint32_t)a, fn * 2 + 1);
+        if (b >= 0) push((uint32_t)b, fn * 2);
+    }
+    for (const BcHost& bc : bcs)
+        for (uint32_t k = mv.zone_offsets[bc.zone]; k < mv.zone_offsets[bc.zone + 1]; ++k) {
+            const uint32_t f = mv.zone_faces[k];
+            push((uint32_t)mv.cells_of_face[2 * (size_t)f], face_new[f] * 2 + 1);
+        }
+    for (uint32_t cold = 0; cold < N; ++cold) {
+        int* e = &h_cf[cell_new[cold]].x;
+        int j = 0;
+        for (uint32_t k = mv.offsets_faces_of_cell[cold]; k < mv.offsets_faces_of_cell[cold + 1]; ++k)
+            e[j++] = face_new[mv.faces_of_cell[k]];
+    }
+    std::vector<double> h_vol(N);
+    for (uint32_t c = 0; c < N; ++c) h_vol[c] = mv.cell_volume[cell_old[c]];
+
+    // --- quadrature
+    QuadRule qf;
+    if (cfg.recon == MGPU_RECON_FO) {
+        gauss_legendre_rule(1, qf);
+    } else {
+        const int order = cfg.quadrature_order_face > 0 ? cfg.quadrature_order_face : (cfg.poly_order + 1) / 2;
+        if (!gauss_legendre_rule(order, qf)) throw ArgFail("Gauss-Legendre quadrature rule not implemented.");
+    }
+    nq = qf.n();
+    if (nq > 2) throw Unsupported("the GPU path supports 1 or 2 face quadrature points");
+    for (int q = 0; q < nq; ++q) qw[q] = qf.wts[q];
+
+    // --- TENO tables straight into the tiled layout
+    const size_t tiles = (N + TILE - 1) / TILE;
+    if (cfg.recon == MGPU_RECON_TENO) {
+        TenoTables t;
+        build_teno_stencils(mv, cfg.basis, cfg.poly_order, cfg.max_stencil_size_factor, cfg.quadrature_order_cell,
+                            cfg.quadrature_order_face, t);
+        K = t.K;
+        M = t.M;
+        if (!((K == 10 && M == 20 && nq == 2) || (K == 6 && M == 12 && nq == 1) || (K == 3 && M == 6 && nq == 1)))
+            throw Unsupported("GPU TENO kernels exist for p = 1..3 with stencil factor 2 and default face quadrature");
+        const int KR = K - 1, MR = M - 1, S = 4, NF = 3;
+        std::vector<uint32_t> h_nb(tiles * S * MR * TILE, 0), h_cface(tiles * NF * TILE, 0);
+        std::vector<double> h_ar(tiles * S * MR * TILE, 0.0), h_P(tiles * S * MR * KR * TILE, 0.0),
+            h_phi(tiles * NF * nq * KR * TILE, 0.0);
+        std::vector<uint8_t> h_sm(N, 0);
+        std::string err;
+        int nthreads = 1;
+#ifdef _OPENMP
+        nthreads = omp_get_max_threads();
+#endif
+#pragma omp parallel num_threads(nthreads)
+        {
+            LsqWork* w = lsq_work_new();
+            std::vector<double> pinv((size_t)K * M), ars(M);
+#pragma omp for schedule(dynamic, 128)
+            for (int64_t ci = 0; ci < (int64_t)N; ++ci) {
+                try {
+                    const uint32_t c = (uint32_t)ci, o = cell_old[c];
+                    const size_t tile = c / TILE, lane = c % TILE;
+                    uint8_t sm = 0;
+                    for (int s = 0; s < S; ++s) {
+                        const size_t si = (size_t)o * S + s;
+                        const uint32_t so = t.off_stencils[si];
+                        const int Ms = (int)(t.off_stencils[si + 1] - so);
+                        if (Ms == 0) continue;
+                        if (Ms != M || t.stencils[so] != o) throw Unsupported("unexpected stencil shape");
+                        teno_stencil_lsq(mv, t, si, *w, pinv.data(), ars.data());
+                        for (int j = 0; j < M; ++j)
+                            if (pinv[j] != 0.0) throw Unsupported("least-squares system took the full-rank branch");
+                        for (int k = 0; k < K; ++k)
+                            if (pinv[(size_t)k * M] != 0.0) throw Unsupported("least-squares system took the full-rank branch");
+                        sm |= (uint8_t)(1u << s);
+                        for (int j = 1; j < M; ++j) {
+                            const size_t b = ((tile * S + s) * MR + (j - 1)) * TILE + lane;
+                            h_nb[b] = cell_new[t.stencils[so + j]];
+                            h_ar[b] = ars[j];
+                            for (int k = 1; k < K; ++k)
+                                h_P[(((tile * S + s) * MR + (j - 1)) * KR + (k - 1)) * TILE + lane] = pinv[(size_t)k * M + j];
+                        }
+                        if (s == 0) {
+                            // basis shape values at the face quadrature points, in the
+                            // target cell's reference frame (face_reconstruction.cpp:985-1031)
+                            const double area0 = ars[0];
+                            const uint32_t* nc = mv.nodes_of_cell + mv.offsets_nodes_of_cell[o];
+                            const double* w0 = mv.node_coords + 2 * (size_t)nc[0];
+                            double J[4], Ji[4];
+                            tri_jacobian(w0, mv.node_coords + 2 * (size_t)nc[1], mv.node_coords + 2 * (size_t)nc[2], J);
+                            mat2_inverse(J, Ji);
+                            for (int fl = 0; fl < NF; ++fl) {
+                                const uint32_t f = mv.faces_of_cell[mv.offsets_faces_of_cell[o] + fl];
+                                const int side = mv.cells_of_face[2 * (size_t)f] == (int32_t)o ? 0 : 1;
+                                h_cface[(tile * NF + fl) * TILE + lane] = (uint32_t)face_new[f] * 2u + (uint32_t)side;
+                                const double* p0 = mv.node_coords + 2 * (size_t)mv.nodes_of_face[mv.offsets_nodes_of_face[f]];
+                                const double* p1 = mv.node_coords + 2 * (size_t)mv.nodes_of_face[mv.offsets_nodes_of_face[f] + 1];
+                                double x0[2], x1[2];
+                                for (int i = 0; i < 2; i++) {
+                                    x0[i] = p0[i] - w0[i];
+                                    x1[i] = p1[i] - w0[i];
+                                }
+                                mat2_vec(Ji, x0, x0);
+                                mat2_vec(Ji, x1, x1);
+                                for (int q = 0; q < nq; ++q) {
+                                    double xq[2];
+                                    for (int i = 0; i < 2; i++) xq[i] = (qf.pts[q] + 1.0) * 0.5 * (x1[i] - x0[i]) + x0[i];
+                                    for (int k = 1; k < K; ++k) {
+                                        const double b = basis_2d(t.basis, t.pidx[2 * k], t.pidx[2 * k + 1], xq[0], xq[1]);
+                                        const double shape = cfg.teno_variant == MGPU_TENO_CORRECTED ? b - t.ipt[k]
+                                                                                                   : b + (t.ipt[k] / area0);
+                                        h_phi[(((tile * NF + fl) * nq + q) * KR + (k - 1)) * TILE + lane] = shape;
+                                    }
+                                }
+                            }
+                        }
+                    }
+                    h_sm[c] = sm;
+                } catch (const std::exception& e) {
+#pragma omp critical
+                    err = e.what();
+                }
+            }
+            lsq_work_free(w);
+        }
+        if (!err.empty()) throw Unsupported(err);
+        teno.n_cells = (int)N;
+        for (int i = 0; i < KR; ++i)
+            for (int l = 0; l < KR; ++l) teno.oi[i * KR + l] = t.oi[(size_t)(i + 1) * K + (l + 1)];
+        nb.upload(h_nb);
+        ar.upload(h_ar);
+        P.upload(h_P);
+        phi.upload(h_phi);
+        cface.upload(h_cface);
+        smask.upload(h_sm);
+        teno.nb = nb.p;
+        teno.ar = ar.p;
+        teno.P = P.p;
+        teno.phi = phi.p;
+        teno.cface = cface.p;
+        teno.smask = smask.p;
+        // compulsory bytes of one reconstruction launch: tables, shapes, face
+        // slots, the state gathered once per cell, face states written
+        double tb = 0;
+        for (uint32_t c = 0; c < N; ++c) tb += __builtin_popcount(h_sm[c]) * (double)MR * (4 + 8 + 8 * KR);
+        recon_bytes = tb + (double)N * (NF * nq * KR * 8 + NF * 4 + 1 + 32) + (double)N * NF * nq * 32;
+    } else {
+        recon_bytes = (double)F_flux * (8 + 64) + (double)N * 32;
+    }
+
+    // --- BCs
+    bct.n = (int)bcs.size();
+    for (size_t i = 0; i < bcs.size(); ++i) {
+        bct.bc[i].type = bcs[i].type;
+        for (int k = 0; k < 6; ++k) bct.bc[i].data[k] = bcs[i].data[k];
+    }
+
+    // --- upload the rest
+    lr.upload(h_lr);
+    nrm.upload(h_nrm);
+    area.upload(h_area);
+    dxn.upload(h_dxn);
+    bcidx.upload(h_bc);
+    gat.upload(h_gat);
+    cfaces.upload(h_cf);
+    vol.upload(h_vol);
+    U.alloc((size_t)N * 4);
+    Ut.alloc((size_t)N * 4);
+    W.alloc((size_t)N * 4);
+    rhs.alloc((size_t)N * 4);
+    prim.alloc((size_t)N * 5);
+    rho_cell.alloc(N);
+    fv.alloc((size_t)F_real * nq * 8);
+    G.alloc((size_t)F_flux * 4);
+    scal.alloc(2);
+    flags.alloc(1);
+    rmax.alloc(1);
+    masks.alloc((size_t)N * 4);
+    staging.alloc((size_t)N * 5);
+    perm_old.upload(cell_old);
+    // compulsory bytes of one stage: reconstruction + flux (face states in,
+    // G out, face geometry) + update (G gathered, state in/out)
+    const double flux_b = (double)F_flux * (nq * 64 + 32 + 8 + 16 + 8 + 1);
+    const double upd_b = (double)N * (16 + 8 + 32 * 4) + (double)F_flux * 32 * 2;
+    stage_bytes = recon_bytes + flux_b + upd_b;
+    finalized = true;
+}
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+
+namespace {
+
+template <class F>
+int guarded(F&& fn) {
+    try {
+        return fn();
+    } catch (const CudaFail& e) {
+        set_error(e.what());
+        return MGPU_ERR_CUDA;
+    } catch (const ArgFail& e) {
+        set_error(e.what());
+        return MGPU_ERR_ARG;
+    } catch (const Unsupported& e) {
+        set_error(e.what());
+        return MGPU_ERR_UNSUPPORTED;
+    } catch (const std::bad_alloc&) {
+        set_error("host allocation failed");
+        return MGPU_ERR_HOST;
+    } catch (const std::exception& e) {
+        set_error(e.what());
+        return MGPU_ERR_HOST;
+    }
+}
+
+int need_ready(const mgpu_ctx* ctx) {
+    if (!ctx) {
+        set_error("null context");
+        return MGPU_ERR_ARG;
+    }
+    if (!ctx->finalized) {
+        set_error("context not finalized (call mgpu_finalize after adding boundaries)");
+        return MGPU_ERR_STATE;
+    }
+    return MGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* mgpu_last_error(void) { return g_error.c_str(); }
+int mgpu_version(void) { return 100; }
+
+void mgpu_config_defaults(mgpu_config* c) {
+    if (!c) return;
+    std::memset(c, 0, sizeof(*c));
+    c->recon = MGPU_RECON_TENO;
+    c->basis = MGPU_BASIS_LEGENDRE;
+    c->poly_order = 3;
+    c->max_stencil_size_factor = 2.0;
+    c->riemann_solver = MGPU_RIEMANN_HLLC;
+    c->time_integrator = MGPU_INTEGRATOR_SSPRK3;
+    c->gamma = 1.4;
+    c->p_ref = 101325.0;
+    c->T_ref = 298.15;
+    c->rho_ref = 1.225;
+    c->p_min = -1e20;
+    c->p_max = 1e20;
+    c->teno_variant = MGPU_TENO_REFERENCE;
+    c->precision = MGPU_PREC_FP64;
+    c->reorder = 1;
+    c->device = 0;
+}
+
+int mgpu_create(const mgpu_mesh* mesh, const mgpu_config* cfg, mgpu_ctx** out) {
+    return guarded([&] {
+        if (!mesh || !cfg || !out) throw ArgFail("mgpu_create: null argument");
+        if (cfg->recon != MGPU_RECON_FO && cfg->recon != MGPU_RECON_TENO) throw ArgFail("Unknown face reconstruction type.");
+        if (cfg->riemann_solver < 0 || cfg->riemann_solver > 2) throw ArgFail("Unknown Riemann solver type.");
+        if (cfg->time_integrator != MGPU_INTEGRATOR_SSPRK3) throw Unsupported("the GPU path implements SSPRK3");
+        if (cfg->precision != MGPU_PREC_FP64) throw Unsupported("unknown precision mode");
+        if (cfg->teno_variant != MGPU_TENO_REFERENCE && cfg->teno_variant != MGPU_TENO_CORRECTED)
+            throw ArgFail("unknown TENO variant");
+        if (cfg->basis != MGPU_BASIS_LEGENDRE && cfg->basis != MGPU_BASIS_MONOMIAL) throw ArgFail("Unknown basis type.");
+        if (!(cfg->gamma > 1.0) || !(cfg->p_ref > 0) || !(cfg->T_ref > 0) || !(cfg->rho_ref > 0))
+            throw ArgFail("invalid physics constants");
+        auto ctx = std::make_unique<mgpu_ctx>();
+        ctx->cfg = *cfg;
+        HostMesh& m = ctx->mesh;
+        m.n_nodes = mesh->n_nodes;
+        m.n_cells = mesh->n_cells;
+        m.n_faces = mesh->n_faces;
+        auto cp = [](auto& dst, const auto* src, size_t n) {
+            if (!src && n) throw ArgFail("mgpu_create: null mesh array");
+            dst.assign(src, src + n);
+        };
+        cp(m.node_coords, mesh->node_coords, 2 * (size_t)m.n_nodes);
+        cp(m.cell_coords, mesh->cell_coords, 2 * (size_t)m.n_cells);
+        cp(m.cell_volume, mesh->cell_volume, m.n_cells);
+        cp(m.face_area, mesh->face_area, m.n_faces);
+        cp(m.face_normals, mesh->face_normals, 2 * (size_t)m.n_faces);
+        cp(m.off_noc, mesh->offsets_nodes_of_cell, (size_t)m.n_cells + 1);
+        cp(m.noc, mesh->nodes_of_cell, m.off_noc.back());
+        cp(m.off_foc, mesh->offsets_faces_of_cell, (size_t)m.n_cells + 1);
+        cp(m.foc, mesh->faces_of_cell, m.off_foc.back());
+        cp(m.off_nof, mesh->offsets_nodes_of_face, (size_t)m.n_faces + 1);
+        cp(m.nof, mesh->nodes_of_face, m.off_nof.back());
+        cp(m.cof, mesh->cells_of_face, 2 * (size_t)m.n_faces);
+        cp(m.zone_off, mesh->zone_offsets, (size_t)mesh->n_zones + 1);
+        cp(m.zone_faces, mesh->zone_faces, m.zone_off.back());
+        for (uint32_t f : m.foc)
+            if (f >= m.n_faces) throw ArgFail("mesh: face index out of range");
+        for (uint32_t f : m.zone_faces)
+            if (f >= m.n_faces) throw ArgFail("mesh: zone face out of range");
+        for (uint32_t n : m.noc)
+            if (n >= m.n_nodes) throw ArgFail("mesh: node index out of range");
+        for (uint32_t n : m.nof)
+            if (n >= m.n_nodes) throw ArgFail("mesh: node index out of range");
+        for (size_t i = 0; i < m.cof.size(); ++i)
+            if (m.cof[i] >= (int32_t)m.n_cells || m.cof[i] < -1) throw ArgFail("mesh: cells_of_face out of range");
+        // Euler::set_R_cp_cv (physics.cpp:69-73)
+        const double R = cfg->p_ref / (cfg->T_ref * cfg->rho_ref);
+        const double cp_ = R * cfg->gamma / (cfg->gamma - 1.0);
+        ctx->gas.gamma = cfg->gamma;
+        ctx->gas.R = R;
+        ctx->gas.cv = cp_ / cfg->gamma;
+        ctx->gas.p_min = cfg->p_min;
+        ctx->gas.p_max = cfg->p_max;
+        ck(cudaSetDevice(cfg->device), "cudaSetDevice");
+        ck(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        ctx->own_stream = true;
+        *out = ctx.release();
+        return MGPU_OK;
+    });
+}
+
+int mgpu_add_boundary(mgpu_ctx* ctx, uint32_t zone, int bc_type, const double* data, int n_data) {
+    return guarded([&] {
+        if (!ctx) throw ArgFail("null context");
+        if (ctx->finalized) throw ArgFail("boundaries must be added before mgpu_finalize");
+        if (zone == 0 || zone + 1 >= ctx->mesh.zone_off.size()) throw ArgFail("Boundary name not found in mesh.");
+        if (ctx->bcs.size() >= (size_t)MAX_BC) throw Unsupported("too many boundary conditions");
+        BcHost b{};
+        b.zone = zone;
+        b.type = bc_type;
+        if (bc_type == MGPU_BC_UPT) {
+            // BoundaryUPT::init (boundary_upt.cpp:38-73): data = (u, v, p, T)
+            if (!data || n_data < 4) throw ArgFail("Missing u, p or T for boundary.");
+            const double u0 = data[0], u1 = data[1], p = data[2], T = data[3];
+            const double rho = p / (ctx->gas.R * T);
+            const double e = ctx->gas.cv * T;
+            const double h = e + p / rho;
+            const double d[6] = {rho, u0, u1, p, T, h};
+            std::memcpy(b.data, d, sizeof(d));
+        } else if (bc_type == MGPU_BC_P_OUT) {
+            if (!data || n_data < 1) throw ArgFail("Missing p for boundary.");
+            b.data[0] = data[0];
+        } else if (bc_type < 0 || bc_type > MGPU_BC_P_OUT) {
+            throw ArgFail("Unknown boundary type.");
+        }
+        ctx->bcs.push_back(b);
+        return MGPU_OK;
+    });
+}
+
+int mgpu_finalize(mgpu_ctx* ctx) {
+    return guarded([&] {
+        if (!ctx) throw ArgFail("null context");
+        if (ctx->finalized) return MGPU_OK;
+        ck(cudaSetDevice(ctx->cfg.device), "cudaSetDevice");
+        ctx->build();
+        return MGPU_OK;
+    });
+}
+
+int mgpu_destroy(mgpu_ctx* ctx) {
+    if (ctx) {
+        cudaSetDevice(ctx->cfg.device);
+        if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+        delete ctx;
+    }
+    return MGPU_OK;
+}
+
+int mgpu_set_stream(mgpu_ctx* ctx, void* stream) {
+    return guarded([&] {
+        if (!ctx) throw ArgFail("null context");
+        if (ctx->stream) ck(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+        if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+        if (stream) {
+            ctx->stream = (cudaStream_t)stream;
+            ctx->own_stream = false;
+        } else {
+            ck(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+            ctx->own_stream = true;
+        }
+        if (ctx->step_exec) {
+            cudaGraphExecDestroy(ctx->step_exec);
+            ctx->step_exec = nullptr;
+        }
+        return MGPU_OK;
+    });
+}
+
+int mgpu_synchronize(mgpu_ctx* ctx) {
+    return guarded([&] {
+        if (!ctx) throw ArgFail("null context");
+        ck(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+        return MGPU_OK;
+    });
+}
+
+int mgpu_set_state(mgpu_ctx* ctx, const double* Uh, const double* primh) {
+    if (int rc = need_ready(ctx)) return rc;
+    return guarded([&] {
+        if (!Uh) throw ArgFail("null state");
+        ctx->upload_cells(ctx->U.p, Uh, 4);
+        if (primh) {
+            ctx->upload_cells(ctx->prim.p, primh, 5);
+        } else {
+            ck(launch_primitives_batch(ctx->gas, ctx->N, ctx->U.p, ctx->prim.p, ctx->stream), "primitives");
+        }
+        ck(cudaMemsetAsync(ctx->flags.p, 0, sizeof(unsigned), ctx->stream), "cudaMemsetAsync");
+        ck(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+        return MGPU_OK;
+    });
+}
+
+int mgpu_get_state(mgpu_ctx* ctx, double* Uh, double* primh) {
+    if (int rc = need_ready(ctx)) return rc;
+    return guarded([&] {
+        if (Uh) ctx->download_cells(ctx->U.p, Uh, 4);
+        if (primh) ctx->download_cells(ctx->prim.p, primh, 5);
+        return MGPU_OK;
+    });
+}
+
+int mgpu_calc_face_values(mgpu_ctx* ctx, const double* Uh, double* face, uint8_t* tmask) {
+    if (int rc = need_ready(ctx)) return rc;
+    return guarded([&] {
+        if (!Uh || !face) throw ArgFail("null argument");
+        ctx->upload_cells(ctx->Ut.p, Uh, 4);
+        ck(cudaMemsetAsync(ctx->fv.p, 0, ctx->fv.bytes(), ctx->stream), "cudaMemsetAsync");
+        ctx->reconstruct(ctx->Ut.p, ctx->masks.p);
+        const int nq = ctx->nq;
+        std::vector<double> tmp((size_t)ctx->F_real * nq * 8);
+        ck(cudaMemcpyAsync(tmp.data(), ctx->fv.p, tmp.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream),
+           "D2H");
+        std::vector<uint8_t> mk((size_t)ctx->N * 4);
+        if (tmask)
+            ck(cudaMemcpyAsync(mk.data(), ctx->masks.p, mk.size(), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+        ck(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+        std::memset(face, 0, (size_t)ctx->mesh.n_faces * nq * 8 * sizeof(double));
+        for (uint32_t i = 0; i < ctx->F_real; ++i)
+            std::memcpy(face + (size_t)ctx->face_old[i] * nq * 8, &tmp[(size_t)i * nq * 8], nq * 8 * sizeof(double));
+        if (tmask)
+            for (uint32_t c = 0; c < ctx->N; ++c) std::memcpy(tmask + (size_t)ctx->cell_old[c] * 4, &mk[(size_t)c * 4], 4);
+        return MGPU_OK;
+    });
+}
+
+int mgpu_calc_rhs(mgpu_ctx* ctx, const double* Uh, double* rhsh) {
+    if (int rc = need_ready(ctx)) return rc;
+    return guarded([&] {
+        if (!Uh || !rhsh) throw ArgFail("null argument");
+        ctx->upload_cells(ctx->Ut.p, Uh, 4);
+        ctx->reconstruct(ctx->Ut.p, nullptr);
+        ctx->flux(ctx->Ut.p);
+        UpdateArgs a = ctx->update_args();
+        ck(launch_update(a, ctx->gas, 0, ctx->stream), "update");
+        ctx->download_cells(ctx->rhs.p, rhsh, 4);
+        return MGPU_OK;
+    });
+}
+
+int mgpu_calc_dt(mgpu_ctx* ctx, double cfl, double* dt, double* cfl_local) {
+    if (int rc = need_ready(ctx)) return rc;
+    return guarded([&] {
+        if (!dt) throw ArgFail("null argument");
+        ctx->spectral_and_dt(cfl, false);
+        double h = 0;
+        ck(cudaMemcpyAsync(&h, ctx->dt_ptr(), sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+        ck(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+        *dt = h;
+        if (cfl_local) {
+            ctx->download_cells(ctx->rho_cell.p, cfl_local, 1);
+            for (uint32_t c = 0; c < ctx->N; ++c) cfl_local[c] = h * cfl_local[c];
+        }
+        if (h < 0.0) {
+            set_error("dt negative: " + std::to_string(h) + ".");
+            return MGPU_ERR_NAN;
+        }
+        return MGPU_OK;
+    });
+}
+
+int mgpu_take_step(mgpu_ctx* ctx, double dt) {
+    if (int rc = need_ready(ctx)) return rc;
+    return guarded([&] {
+        ck(launch_set_scalar(ctx->dt_ptr(), dt, ctx->stream), "set dt");
+        ctx->stage(1);
+        ctx->stage(2);
+        ctx->stage(3);
+        return MGPU_OK;
+    });
+}
+
+int mgpu_run(mgpu_ctx* ctx, double cfl, uint32_t n_steps, double* t_out) {
+    if (int rc = need_ready(ctx)) return rc;
+    return guarded([&] {
+        ck(launch_set_scalar(ctx->t_ptr(), 0.0, ctx->stream), "set t");
+        if (ctx->timing) {
+            for (uint32_t s = 0; s < n_steps; ++s) ctx->cfl_step(cfl);
+        } else {
+            if (!ctx->step_exec || ctx->step_cfl != cfl) {
+                if (ctx->step_exec) {
+                    cudaGraphExecDestroy(ctx->step_exec);
+                    ctx->step_exec = nullptr;
+                }
+                cudaGraph_t g = nullptr;
+                ck(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+                try {
+                    ctx->cfl_step(cfl);
+                } catch (...) {
+                    cudaStreamEndCapture(ctx->stream, &g);
+                    if (g) cudaGraphDestroy(g);
+                    throw;
+                }
+                ck(cudaStreamEndCapture(ctx->stream, &g), "cudaStreamEndCapture");
+                cudaError_t e = cudaGraphInstantiate(&ctx->step_exec, g, 0);
+                cudaGraphDestroy(g);
+                ck(e, "cudaGraphInstantiate");
+                ctx->step_cfl = cfl;
+            }
+            for (uint32_t s = 0; s < n_steps; ++s) ck(cudaGraphLaunch(ctx->step_exec, ctx->stream), "cudaGraphLaunch");
+        }
+        if (t_out) {
+            double h = 0;
+            ck(cudaMemcpyAsync(&h, ctx->t_ptr(), sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+            ck(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+            *t_out = h;
+        }
+        return MGPU_OK;
+    });
+}
+
+int mgpu_status(mgpu_ctx* ctx, uint32_t* flags) {
+    if (int rc = need_ready(ctx)) return rc;
+    return guarded([&] {
+        unsigned h = 0;
+        ck(cudaMemcpyAsync(&h, ctx->flags.p, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+        ck(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+        if (flags) *flags = h;
+        return h ? MGPU_ERR_NAN : MGPU_OK;
+    });
+}
+
+int mgpu_enable_kernel_timing(mgpu_ctx* ctx, int enable) {
+    return guarded([&] {
+        if (!ctx) throw ArgFail("null context");
+        ck(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+        ctx->timing = enable != 0;
+        ctx->marks_used = 0;
+        return MGPU_OK;
+    });
+}
+
+int mgpu_kernel_times(mgpu_ctx* ctx, double* ms, uint32_t* launches) {
+    return guarded([&] {
+        if (!ctx || !ms || !launches) throw ArgFail("null argument");
+        ck(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+        for (int i = 0; i < 4; ++i) {
+            ms[i] = 0.0;
+            launches[i] = 0;
+        }
+        for (size_t i = 0; i < ctx->marks_used; ++i) {
+            float t = 0.f;
+            ck(cudaEventElapsedTime(&t, ctx->marks[i].a, ctx->marks[i].b), "cudaEventElapsedTime");
+            ms[ctx->marks[i].cls] += t;
+            launches[ctx->marks[i].cls] += 1;
+        }
+        ctx->marks_used = 0;
+        return MGPU_OK;
+    });
+}
+
+int mgpu_traffic_model(mgpu_ctx* ctx, double* recon_bytes, double* stage_bytes) {
+    if (int rc = need_ready(ctx)) return rc;
+    if (recon_bytes) *recon_bytes = ctx->recon_bytes;
+    if (stage_bytes) *stage_bytes = ctx->stage_bytes;
+    return MGPU_OK;
+}
+
+uint32_t mgpu_n_cells(const mgpu_ctx* ctx) { return ctx ? ctx->mesh.n_cells : 0; }
+
+int mgpu_riemann_flux_batch(int solver, uint32_t n, const double* n_unit, const double* rho_l, const double* u_l,
+                            const double* p_l, const double* gamma_l, const double* h_l, const double* rho_r,
+                            const double* u_r, const double* p_r, const double* gamma_r, const double* h_r,
+                            double* flux) {
+    return guarded([&] {
+        if (solver < 0 || solver > 2) throw ArgFail("Unknown Riemann solver type.");
+        if (n == 0) return MGPU_OK;
+        if (!n_unit || !rho_l || !u_l || !p_l || !gamma_l || !h_l || !rho_r || !u_r || !p_r || !gamma_r || !h_r || !flux)
+            throw ArgFail("null argument");
+        std::vector<double> in((size_t)n * 14);
+        for (uint32_t i = 0; i < n; ++i) {
+            double* b = &in[(size_t)i * 14];
+            b[0] = n_unit[2 * i]; b[1] = n_unit[2 * i + 1];
+            b[2] = rho_l[i]; b[3] = u_l[2 * i]; b[4] = u_l[2 * i + 1]; b[5] = p_l[i]; b[6] = gamma_l[i]; b[7] = h_l[i];
+            b[8] = rho_r[i]; b[9] = u_r[2 * i]; b[10] = u_r[2 * i + 1]; b[11] = p_r[i]; b[12] = gamma_r[i]; b[13] = h_r[i];
+        }
+        DevArray<double> din, dout;
+        din.upload(in);
+        dout.alloc((size_t)n * 4);
+        ck(launch_riemann_batch(solver, n, din.p, dout.p, 0), "riemann launch");
+        ck(cudaMemcpy(flux, dout.p, (size_t)n * 4 * sizeof(double), cudaMemcpyDeviceToHost), "D2H");
+        return MGPU_OK;
+    });
+}
+
+int mgpu_primitives_batch(double gamma, double p_ref, double T_ref, double rho_ref, double p_min, double p_max,
+                          uint32_t n, const double* Uh, double* Wh) {
+    return guarded([&] {
+        if (n == 0) return MGPU_OK;
+        if (!Uh || !Wh) throw ArgFail("null argument");
+        GasParams g{};
+        const double R = p_ref / (T_ref * rho_ref);
+        const double cp_ = R * gamma / (gamma - 1.0);
+        g.gamma = gamma;
+        g.R = R;
+        g.cv = cp_ / gamma;
+        g.p_min = p_min;
+        g.p_max = p_max;
+        std::vector<double> u(Uh, Uh + (size_t)n * 4);
+        DevArray<double> du, dw;
+        du.upload(u);
+        dw.alloc((size_t)n * 5);
+        ck(launch_primitives_batch(g, n, du.p, dw.p, 0), "primitives launch");
+        ck(cudaMemcpy(Wh, dw.p, (size_t)n * 5 * sizeof(double), cudaMemcpyDeviceToHost), "D2H");
+        return MGPU_OK;
+    });
+}
+
+int mgpu_probe_fp64_gflops(int device, double* gflops) {
+    return guarded([&] {
+        if (!gflops) throw ArgFail("null argument");
+        ck(run_fp64_probe(device, gflops), "fp64 probe");
+        return MGPU_OK;
+    });
+}
+
+}  // extern "C"

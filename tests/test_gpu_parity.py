@@ -1,0 +1,235 @@
+"""Parity of the GPU path (through the C ABI) with the CPU oracle.
+
+Tolerance: the spec bar, 1e-12 relative per cell and variable per stage
+and 1e-10 after 100 steps, relative to max(|ref|, 1e-3 * max|ref| of the
+variable).  The FP64 kernels keep the reference's operation order without
+FMA contraction, so most values are expected to agree bit for bit; the tests
+also report and bound the bit-identical fraction.
+"""
+
+import numpy as np
+import pytest
+
+import mallard_gb300 as mg
+from cases import four_quadrant, make_pair, perturbed, real_faces, smooth, sod, uniform
+from conftest import rel_err
+
+pytestmark = pytest.mark.gpu
+
+STAGE_TOL = 1e-12
+RUN_TOL = 1e-10
+
+
+def tri_mesh(n=24, seed=None):
+    m = mg.Mesh.generate("cartesian_tri", n, n, 1.0, 1.0)
+    if seed is not None:
+        m.permute_cells(seed)
+    return m
+
+
+def assert_close(a, b, tol, min_exact=0.0, what=""):
+    fin = np.isfinite(b)
+    np.testing.assert_array_equal(np.isfinite(a), fin, err_msg=f"{what}: non-finite pattern differs")
+    err = rel_err(np.where(fin, a, 0.0), np.where(fin, b, 0.0))
+    assert np.nanmax(err) <= tol, f"{what}: max rel err {np.nanmax(err):.3e}"
+    exact = np.mean((a == b) | ~fin)
+    assert exact >= min_exact, f"{what}: bit-identical fraction {exact:.4f}"
+    return exact
+
+
+# ---- reconstruction -----------------------------------------------------------
+
+@pytest.mark.parametrize("variant", ["reference", "corrected"])
+@pytest.mark.parametrize("ic", [four_quadrant, smooth, perturbed])
+def test_face_values_and_masks(variant, ic):
+    m = tri_mesh(24, seed=20261203)
+    s, oc = make_pair(m, variant=variant)
+    U, _ = ic(m)
+    F, M = s.calc_face_values(U, masks=True)
+    Fo, Mo = oc.face_values(U, masks=True)
+    np.testing.assert_array_equal(M, Mo, err_msg="TENO decision masks differ")
+    f, interior = real_faces(m)
+    a = np.concatenate([F[f][:, :, 0].reshape(len(f), -1), F[f[interior]][:, :, 1].reshape(interior.sum(), -1)])
+    b = np.concatenate([Fo[f][:, :, 0].reshape(len(f), -1), Fo[f[interior]][:, :, 1].reshape(interior.sum(), -1)])
+    assert_close(a, b, STAGE_TOL, min_exact=0.99, what="face values")
+
+
+@pytest.mark.parametrize("p", [1, 2])
+def test_face_values_lower_orders(p):
+    m = tri_mesh(16, seed=3)
+    s, oc = make_pair(m, poly_order=p)
+    U, _ = perturbed(m)
+    F, M = s.calc_face_values(U, masks=True)
+    Fo, Mo = oc.face_values(U, masks=True)
+    np.testing.assert_array_equal(M, Mo)
+    f, _ = real_faces(m)
+    assert_close(F[f][:, :, 0], Fo[f][:, :, 0], STAGE_TOL, min_exact=0.99, what=f"p={p}")
+
+
+# ---- residual -----------------------------------------------------------------
+
+@pytest.mark.parametrize("riemann", ["Rusanov", "HLL", "HLLC"])
+@pytest.mark.parametrize("variant", ["reference", "corrected"])
+def test_residual_teno(riemann, variant):
+    m = tri_mesh(24, seed=20261203)
+    s, oc = make_pair(m, riemann=riemann, variant=variant)
+    for ic in (four_quadrant, perturbed):
+        U, _ = ic(m)
+        assert_close(s.calc_rhs(U), oc.calc_rhs(U), STAGE_TOL, min_exact=0.95, what=f"{riemann} {ic.__name__}")
+
+
+@pytest.mark.parametrize("bc", ["symmetry", "extrapolation", "wall_adiabatic", "upt", "p_out"])
+def test_residual_each_boundary_type(bc):
+    m = tri_mesh(16)
+    bcs = {"left": bc, "right": "extrapolation", "top": bc, "bottom": "symmetry"}
+    s, oc = make_pair(m, bcs=bcs, variant="corrected")
+    U, _ = perturbed(m, seed=5)
+    assert_close(s.calc_rhs(U), oc.calc_rhs(U), STAGE_TOL, min_exact=0.95, what=bc)
+
+
+def test_residual_zone_without_boundary_condition():
+    """A zone with no [[boundaries]] entry contributes no flux, as in the reference."""
+    m = tri_mesh(12)
+    s, oc = make_pair(m, bcs={"left": "symmetry", "bottom": "extrapolation"})
+    U, _ = perturbed(m)
+    assert_close(s.calc_rhs(U), oc.calc_rhs(U), STAGE_TOL, min_exact=0.95)
+
+
+@pytest.mark.parametrize("riemann", ["Rusanov", "HLLC"])
+def test_residual_first_order_quads(riemann):
+    m = mg.Mesh.generate("wedge", 30, 10, 4.0, 1.5)
+    bcs = {"left": "upt", "right": "p_out", "top": "symmetry", "bottom": "wall_adiabatic"}
+    s, oc = make_pair(m, recon="FO", riemann=riemann, bcs=bcs, p_min=1e-6)
+    U, _ = perturbed(m, seed=9)
+    assert_close(s.calc_rhs(U), oc.calc_rhs(U), STAGE_TOL, min_exact=0.99)
+
+
+def test_residual_delaunay_mesh():
+    from test_host import delaunay_mesh
+    m = delaunay_mesh(20, 14, seed=8)
+    s, oc = make_pair(m, variant="corrected")
+    U, _ = perturbed(m, seed=2)
+    assert_close(s.calc_rhs(U), oc.calc_rhs(U), STAGE_TOL, min_exact=0.95)
+
+
+def test_uniform_state_is_preserved():
+    m = tri_mesh(20, seed=1)
+    s, oc = make_pair(m)
+    U, _ = uniform(m)
+    r = s.calc_rhs(U)
+    assert np.abs(r).max() < 1e-9
+    assert_close(r, oc.calc_rhs(U), 1.0, what="uniform")
+
+
+def test_reorder_does_not_change_results():
+    """Internal cell order is invisible: the gather keeps the reference's summation order."""
+    m = tri_mesh(20, seed=4)
+    a, _ = make_pair(m, reorder=True)
+    b, _ = make_pair(m, reorder=False)
+    U, _ = four_quadrant(m)
+    np.testing.assert_array_equal(a.calc_rhs(U), b.calc_rhs(U))
+
+
+# ---- time step ----------------------------------------------------------------
+
+def test_calc_dt_matches():
+    m = tri_mesh(20, seed=6)
+    s, oc = make_pair(m)
+    U, W = four_quadrant(m)
+    s.set_state(U, W)
+    oc.set_state(U, W)
+    dt, cl = s.calc_dt(0.5)
+    dto, clo = oc.calc_dt(0.5)
+    assert dt == dto
+    assert_close(cl, clo, STAGE_TOL, min_exact=0.99, what="cfl_local")
+
+
+@pytest.mark.parametrize("variant", ["reference", "corrected"])
+def test_take_step_matches(variant):
+    m = tri_mesh(20, seed=6)
+    s, oc = make_pair(m, variant=variant)
+    U, W = smooth(m)
+    s.set_state(U, W)
+    oc.set_state(U, W)
+    s.take_step(1e-3)
+    oc.take_step(1e-3)
+    Ug, Wg = s.get_state()
+    Uo, Wo = oc.get_state()
+    assert_close(Ug, Uo, STAGE_TOL, min_exact=0.95, what="U")
+    assert_close(Wg, Wo, STAGE_TOL, min_exact=0.95, what="primitives")
+
+
+@pytest.mark.parametrize("variant", ["reference", "corrected"])
+def test_100_steps_smooth(variant):
+    m = tri_mesh(16, seed=20261203)
+    s, oc = make_pair(m, variant=variant)
+    U, W = smooth(m)
+    s.set_state(U, W)
+    oc.set_state(U, W)
+    t_gpu = s.run(0.5, 100)
+    t_ora = oc.run(0.5, 100)
+    assert abs(t_gpu - t_ora) <= 1e-12 * t_ora
+    Ug, _ = s.get_state()
+    Uo, _ = oc.get_state()
+    assert np.isfinite(Uo).all()
+    assert_close(Ug, Uo, RUN_TOL, what="U after 100 steps")
+    assert s.status() == 0
+
+
+def test_10_steps_four_quadrant_corrected():
+    m = tri_mesh(32, seed=20261203)
+    s, oc = make_pair(m, variant="corrected")
+    U, W = four_quadrant(m)
+    s.set_state(U, W)
+    oc.set_state(U, W)
+    s.run(0.5, 10)
+    oc.run(0.5, 10)
+    Ug, _ = s.get_state()
+    Uo, _ = oc.get_state()
+    assert np.isfinite(Uo).all()
+    assert_close(Ug, Uo, RUN_TOL, what="U after 10 steps")
+
+
+def test_100_steps_first_order_sod():
+    """The reference's Sod example (first order, HLLC, symmetry walls) on quads."""
+    m = mg.Mesh.generate("cartesian", 200, 1, 1.0, 0.005)
+    bcs = {z: "symmetry" for z in ("left", "right", "top", "bottom")}
+    s, oc = make_pair(m, recon="FO", bcs=bcs)
+    U, W = sod(m)
+    s.set_state(U, W)
+    oc.set_state(U, W)
+    s.run(1.0, 100)
+    oc.run(1.0, 100)
+    assert_close(s.get_state()[0], oc.get_state()[0], RUN_TOL, min_exact=0.9)
+
+
+def test_100_steps_first_order_wedge():
+    """The reference's wedge example: upt inflow, p_out outflow, symmetry, p_min clip."""
+    m = mg.Mesh.generate("wedge", 60, 20, 4.0, 1.5)
+    s = mg.Solver(m, face_reconstruction="FO", riemann_solver="HLLC", p_min=1e-6, boundaries=[
+        {"name": "left", "type": "upt", "u": [600.0, 0.0], "p": 101325.0, "T": 300.0},
+        {"name": "right", "type": "p_out", "p": 101325.0},
+        {"name": "top", "type": "symmetry"}, {"name": "bottom", "type": "symmetry"}])
+    from oracle import OracleCase, OracleMesh
+    om = OracleMesh.from_arrays(m)
+    oc = OracleCase(om, recon="FO", riemann="HLLC", p_min=1e-6)
+    oc.add_boundary(3, "upt", (600.0, 0.0, 101325.0, 300.0))
+    oc.add_boundary(1, "p_out", (101325.0,))
+    oc.add_boundary(2, "symmetry")
+    oc.add_boundary(4, "symmetry")
+    U, W = mg.initial_state(m, {"type": "constant", "u": [600.0, 0.0], "p": 101325.0, "T": 300.0}, s.gas)
+    s.set_state(U, W)
+    oc.set_state(U, W)
+    s.run(1.0, 100)
+    oc.run(1.0, 100)
+    assert_close(s.get_state()[0], oc.get_state()[0], RUN_TOL, min_exact=0.9)
+
+
+def test_nan_state_is_flagged():
+    m = tri_mesh(8)
+    s, _ = make_pair(m)
+    U, W = smooth(m)
+    U[3, 0] = np.nan
+    s.set_state(U, W)
+    s.take_step(1e-4)
+    assert s.status() & 1
