@@ -313,6 +313,10 @@ void mgpu_ctx::build() {
             const uint32_t f = mv.zone_faces[k];
             if (face_bc[f] != -3) throw ArgFail("a face belongs to more than one zone");
             face_bc[f] = zone_bc[z];
+            // interior faces join two cells, boundary faces have none on side 1
+            const int32_t right = mv.cells_of_face[2 * (size_t)f + 1];
+            if ((z == 0) != (right >= 0)) throw ArgFail("zone and cells_of_face disagree on a boundary face");
+            if (mv.cells_of_face[2 * (size_t)f] < 0) throw ArgFail("a face has no cell on side 0");
         }
     for (uint32_t c = 0; c < N; ++c) {
         const uint32_t nf = mv.offsets_faces_of_cell[c + 1] - mv.offsets_faces_of_cell[c];

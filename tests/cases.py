@@ -46,6 +46,13 @@ def smooth(mesh, amp=0.2, u=0.3, v=0.2):
     return mg.state_from_primitives(rho, 0 * x + u, 0 * x + v, p, **GAS)
 
 
+def pulse(mesh, amp=0.2, width2=0.02):
+    """An acoustic pulse at rest in the centre of the unit square."""
+    x, y = mesh.cell_coords[:, 0], mesh.cell_coords[:, 1]
+    g = np.exp(-((x - 0.5) ** 2 + (y - 0.5) ** 2) / width2)
+    return mg.state_from_primitives(1.0 + amp * g, 0 * x, 0 * x, 1.0 + amp * g, **GAS)
+
+
 def uniform(mesh, rho=1.3, u=0.4, v=-0.25, p=0.9):
     n = mesh.n_cells
     return mg.state_from_primitives(np.full(n, rho), np.full(n, u), np.full(n, v), np.full(n, p), **GAS)
@@ -55,7 +62,6 @@ def perturbed(mesh, seed=1234, base=smooth, scale=0.05):
     """A seeded random perturbation of a base state (cell-wise, positive)."""
     rng = np.random.default_rng(seed)
     U, _ = base(mesh)
-    W = mg.primitives(U) if False else None  # noqa: F841 (primitives recomputed by the callee)
     rho = U[:, 0] * (1.0 + scale * rng.uniform(-1, 1, mesh.n_cells))
     u = U[:, 1] / U[:, 0] + scale * rng.uniform(-1, 1, mesh.n_cells)
     v = U[:, 2] / U[:, 0] + scale * rng.uniform(-1, 1, mesh.n_cells)

@@ -40,9 +40,9 @@ def test_riemann_random_states_bit_identical(solver):
     ref = np.array([o.riemann_flux(solver, nrm[i], rl[i], ul[i], pl[i], g[i], hl[i], rr[i], ur[i], pr[i], g[i], hr[i])
                     for i in range(n)])
     exact = (F == ref).all(1).mean()
-    # pow() in the two-rarefaction estimate may differ in the last bit between
-    # the CPU and GPU math libraries; everything else is bit-identical.
-    assert exact > 0.97, exact
+    # pow() in the two-rarefaction estimate (TRRS) may differ in its last bit
+    # between the GPU and the host libm; every other branch is bit-identical.
+    assert exact == 1.0 if solver == "Rusanov" else exact > 0.9, exact
     np.testing.assert_allclose(F, ref, rtol=1e-13, atol=1e-14)
 
 
