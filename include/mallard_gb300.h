@@ -193,6 +193,23 @@ int mgpu_run(mgpu_ctx* ctx, double cfl, uint32_t n_steps, double* t_out);
 /* Device error flags: bit 0 non-finite state, bit 1 non-positive dt. */
 int mgpu_status(mgpu_ctx* ctx, uint32_t* flags);
 
+/* The CFL time step of the resident state (as mgpu_calc_dt) for callers
+ * that cannot allocate device memory while they step: code that captures its
+ * time loop into a CUDA graph (no allocation during capture), code whose
+ * device memory comes from its own allocator or a fixed pool, real-time
+ * loops.  This entry point has no counterpart in the reference.
+ *   dt_device               device pointer to one double (caller-owned): dt
+ *   spectral_radius_device  optional device array [n_cells] in the caller's
+ *                           cell order: per-cell spectral radius (the
+ *                           reference's cfl_local before its scaling by dt)
+ * Enqueued on the context's stream; it does not synchronise.  It calls no
+ * cudaMalloc/cudaFree: its reduction scratch is a static device array of
+ * 512 KiB (one partial per 256 cells), so meshes above 16,777,216 cells are
+ * rejected with MGPU_ERR_ARG.  The first call on each device looks up that
+ * array's address, so make it before any stream capture.  Calls share the
+ * array: calls that overlap on the GPU race. */
+int mgpu_calc_dt_noalloc(mgpu_ctx* ctx, double cfl, double* dt_device, double* spectral_radius_device);
+
 /* Diagnostics for measurement.  Kernel timing brackets every launch of the
  * reconstruction, flux, update and CFL kernels with CUDA events on the
  * launching stream; mgpu_kernel_times returns, per kernel class

@@ -106,6 +106,7 @@ def lib():
         "mgpu_take_step": (i32, [vp, f64]),
         "mgpu_run": (i32, [vp, f64, u32, P(f64)]),
         "mgpu_status": (i32, [vp, P(u32)]),
+        "mgpu_calc_dt_noalloc": (i32, [vp, f64, vp, vp]),
         "mgpu_enable_kernel_timing": (i32, [vp, i32]),
         "mgpu_kernel_times": (i32, [vp, vp, vp]),
         "mgpu_traffic_model": (i32, [vp, P(f64), P(f64)]),

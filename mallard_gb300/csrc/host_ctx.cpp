@@ -1031,3 +1031,26 @@ int mgpu_probe_fp64_gflops(int device, double* gflops) {
 }
 
 }  // extern "C"
+
+namespace mgpu {
+
+// The spectral-radius inputs of a finalized context, for entry points that
+// live in other translation units (noalloc.cu).  Allocates nothing.
+bool ctx_spectral_view(mgpu_ctx* ctx, SpecArgs* s, const uint32_t** cell_old, cudaStream_t* stream, int* device) {
+    if (!ctx || !ctx->finalized || !s || !cell_old || !stream || !device) return false;
+    *s = SpecArgs{};
+    s->n_cells = (int)ctx->N;
+    s->cfaces = ctx->cfaces.p;
+    s->lr = ctx->lr.p;
+    s->nrm = ctx->nrm.p;
+    s->dxn = ctx->dxn.p;
+    s->U = ctx->U.p;
+    s->prim = ctx->prim.p;
+    s->gamma = ctx->gas.gamma;
+    *cell_old = ctx->perm_old.p;
+    *stream = ctx->stream;
+    *device = ctx->cfg.device;
+    return true;
+}
+
+}  // namespace mgpu

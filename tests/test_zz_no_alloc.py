@@ -1,0 +1,64 @@
+"""mgpu_calc_dt_noalloc: the CFL time step for callers that cannot allocate
+device memory while stepping (graph capture, foreign allocators, fixed
+pools).  It must give the same dt and per-cell spectral radius as
+mgpu_calc_dt, including on consecutive calls that reuse its static scratch.
+
+This file is collected last on purpose.
+"""
+
+import ctypes
+
+import numpy as np
+import pytest
+
+import mallard_gb300 as mg
+from mallard_gb300 import _native as N
+from cases import four_quadrant
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12  # the per-stage tolerance of the parity tests
+
+
+def _dev_ptr(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def test_calc_dt_noalloc_matches_calc_dt_on_two_calls():
+    torch = pytest.importorskip("torch")
+    m = mg.Mesh.generate("cartesian_tri", 48, 40, 1.0, 1.0)
+    m.permute_cells(11)
+    s = mg.Solver(m, teno_variant="corrected", boundaries=[{"name": z, "type": "extrapolation"}
+                                                          for z in ("right", "top", "left", "bottom")])
+    U, W = four_quadrant(m)
+    s.set_state(U, W)
+    lib = N.lib()
+    dt_dev = torch.full((1,), -1.0, dtype=torch.float64, device="cuda")
+    rho_dev = torch.full((m.n_cells,), -1.0, dtype=torch.float64, device="cuda")
+    for call in range(2):
+        dt_ref, cfl_local = s.calc_dt(0.5)
+        N.check(lib.mgpu_calc_dt_noalloc(s._h, 0.5, _dev_ptr(dt_dev), _dev_ptr(rho_dev)))
+        s.synchronize()
+        dt = float(dt_dev.cpu().numpy()[0])
+        rho = rho_dev.cpu().numpy()
+        assert abs(dt - dt_ref) <= TOL * abs(dt_ref), (call, dt, dt_ref)
+        np.testing.assert_allclose(dt_ref * rho, cfl_local, rtol=TOL, atol=0)
+        s.take_step(dt_ref)  # the second call sees a new state in the same scratch
+    s.close()
+
+
+def test_calc_dt_noalloc_after_a_larger_mesh():
+    """A smaller mesh after a larger one: stale partial slots are never read."""
+    torch = pytest.importorskip("torch")
+    lib = N.lib()
+    dt_dev = torch.zeros(1, dtype=torch.float64, device="cuda")
+    for n in (64, 12):
+        m = mg.Mesh.generate("cartesian_tri", n, n, 1.0, 1.0)
+        s = mg.Solver(m, teno_variant="corrected", boundaries=[{"name": "left", "type": "symmetry"}])
+        U, W = four_quadrant(m)
+        s.set_state(U, W)
+        dt_ref, _ = s.calc_dt(0.3)
+        N.check(lib.mgpu_calc_dt_noalloc(s._h, 0.3, _dev_ptr(dt_dev), None))
+        s.synchronize()
+        assert abs(float(dt_dev.cpu().numpy()[0]) - dt_ref) <= TOL * abs(dt_ref)
+        s.close()
