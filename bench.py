@@ -51,6 +51,10 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=1024, help="quads per side (cells = 2 n^2)")
     ap.add_argument("--variant", default="corrected", choices=["reference", "corrected"])
+    ap.add_argument("--precision", default="fp64_fast", choices=["fp64", "fp64_fast"],
+                    help="fp64: the reference's rounding (bit-faithful); fp64_fast: FMA-contracted FP64")
+    ap.add_argument("--forms", default="fp64,fp32",
+                    help="other precision forms to time on the same workload (comma list, '' for none)")
     ap.add_argument("--cpu-sample-n", type=int, default=CPU_SAMPLE_N)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -70,7 +74,7 @@ def case_mesh(n):
 def workload_config(args, n):
     return {"workload": f"four-quadrant Riemann, cartesian_tri {n}x{n} quads -> {2 * n * n} triangles, "
                         f"seeded permutation + RCM, TENO p3 legendre + HLLC, SSPRK3 CFL {CFL}, transmissive BCs",
-            "cells": 2 * n * n, "teno_variant": args.variant, "seed": SEED, "precision": "fp64",
+            "cells": 2 * n * n, "teno_variant": args.variant, "seed": SEED, "precision": args.precision,
             "l2": "inputs larger than L2 (TENO tables ~7 KB/cell); no flush", "parallelism": "replicas"}
 
 
@@ -177,6 +181,43 @@ def run_reference(args):
 # GPU leg
 # ---------------------------------------------------------------------------
 
+def time_form(m, args, precision, U0, W0, device, U_ref):
+    """Rate of another precision form on the same mesh and state, and its
+    error against the headline form after the same W + K steps."""
+    import numpy as np
+    import torch
+
+    import mallard_gb300 as mg
+    s = mg.Solver(m, face_reconstruction="TENO", basis_type="legendre", basis_order=3, riemann_solver="HLLC",
+                  boundaries=[{"name": z, "type": "extrapolation"} for z in ("right", "top", "left", "bottom")],
+                  teno_variant=args.variant, reorder=True, device=device, precision=precision)
+    stream = torch.cuda.Stream()
+    s.set_stream(stream.cuda_stream)
+    s.set_state(U0, W0)
+    s.launch(CFL, args.warmup)
+    s.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    s.launch(CFL, args.steps)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    U, _ = s.get_state()
+    s.close()
+    vol = m.cell_volume
+    out = {"value": m.n_cells * args.steps / (ms * 1e-3) / 1e6, "ms_per_step": ms / args.steps,
+           "finite": bool(np.isfinite(U).all())}
+    if np.isfinite(U_ref).all() and out["finite"]:
+        d = np.abs(U[:, 0] - U_ref[:, 0])
+        out["density_l1_rel_err"] = float(np.sum(vol * d) / np.sum(vol * np.abs(U_ref[:, 0])))
+        out["density_linf_rel_err"] = float(d.max() / np.abs(U_ref[:, 0]).max())
+        out["mass_rel_diff"] = float(abs(np.sum(vol * U[:, 0]) - np.sum(vol * U_ref[:, 0])) / np.sum(vol * U_ref[:, 0]))
+        out["energy_rel_diff"] = float(abs(np.sum(vol * U[:, 3]) - np.sum(vol * U_ref[:, 3])) /
+                                       np.sum(vol * U_ref[:, 3]))
+    return out
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -207,7 +248,7 @@ def run_ours(args):
     m = case_mesh(args.n)
     solver = mg.Solver(m, face_reconstruction="TENO", basis_type="legendre", basis_order=3, riemann_solver="HLLC",
                        boundaries=[{"name": z, "type": "extrapolation"} for z in ("right", "top", "left", "bottom")],
-                       teno_variant=args.variant, reorder=True, device=local)
+                       teno_variant=args.variant, reorder=True, device=local, precision=args.precision)
     setup_s = time.perf_counter() - t_setup
     stream = torch.cuda.Stream()
     solver.set_stream(stream.cuda_stream)
@@ -287,6 +328,12 @@ def run_ours(args):
     fp64_achieved = flops_cell * cells / recon_avg_s / 1e9
     gpu_launches = args.steps * 11
 
+    # ---- other forms on the same workload: rate and error against the FP64 state
+    forms = {}
+    for prec in [p for p in args.forms.split(",") if p and p != args.precision]:
+        forms[prec] = time_form(m, args, prec, U0, W0, local, Uend)
+    forms[args.precision] = {"value": value, "ms_per_step": ms_max / args.steps, "finite": finite}
+
     cpu = None
     if rank == 0 and world >= 1 and not args.no_cpu_baseline:
         rate, threads, secs, ccells = cpu_oracle_rate(args.cpu_sample_n, 2, 1, args.variant)
@@ -310,6 +357,7 @@ def run_ours(args):
                               "frac": fp64_achieved / fp64_peak, "flops_per_cell": flops_cell,
                               "peak_source": "measured FMA-chain probe on this GPU"},
                 "kernels": kshare, "stage_bytes": stage_bytes, "finite": finite, "status_flags": flags,
+                "forms": forms,
                 "setup_s": setup_s, "cpu_baseline": cpu}
         print(json.dumps(line), flush=True)
     solver.close()

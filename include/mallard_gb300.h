@@ -79,8 +79,17 @@ enum {
  * 1 = corrected cut-off weights, zero-mean evaluation basis and a
  * positivity fallback in the face flux (same work per cell). */
 enum { MGPU_TENO_REFERENCE = 0, MGPU_TENO_CORRECTED = 1 };
-/* Arithmetic of the GPU path. */
-enum { MGPU_PREC_FP64 = 0 };
+/* Arithmetic of the GPU path.
+ * FP64      : FP64 with the reference's rounding (no FMA contraction, the
+ *             reference's operation order); bit-identical to the reference's
+ *             serial CPU build wherever the math libraries agree.
+ * FP64_FAST : FP64 with FMA contraction and reduced-instruction forms of the
+ *             smoothness indicator and x^6; agrees to ~1e-15 relative.
+ * FP32      : reconstruction and face flux in FP32 (TENO with the corrected
+ *             weighting only); tables, geometry, the conserved state and its
+ *             RK accumulation stay FP64, and face states near vacuum are
+ *             recovered in FP64. */
+enum { MGPU_PREC_FP64 = 0, MGPU_PREC_FP64_FAST = 1, MGPU_PREC_FP32 = 2 };
 
 /* ---- mesh view: exactly the reference Mesh's public arrays (mesh.h:228-253)
  * plus its face zones (zone 0 is "interior", mesh.h:98-104). ------------- */

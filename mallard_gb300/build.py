@@ -37,7 +37,7 @@ def cuda_home():
 def _sources():
     cu = sorted(SRC.glob("*.cu"))
     cpp = sorted(SRC.glob("*.cpp"))
-    headers = sorted(SRC.glob("*.h")) + sorted(INCLUDE.glob("*.h"))
+    headers = sorted(SRC.glob("*.h")) + sorted(SRC.glob("*.cuh")) + sorted(INCLUDE.glob("*.h"))
     return cu, cpp, headers
 
 
@@ -48,7 +48,9 @@ def _jobs(cuda):
     jobs = []
     for s in cu:
         o = OUT / (s.stem + ".o")
-        jobs.append((o, [nvcc, ARCH, "-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
+        # *_fast.cu may contract a*b+c into FMA; everything else keeps two roundings
+        fmad = "-fmad=true" if s.stem.endswith("_fast") else "-fmad=false"
+        jobs.append((o, [nvcc, ARCH, "-O3", "-lineinfo", fmad, "-std=c++17", "-Xcompiler", "-fPIC",
                          "-Xptxas", "-v", "-c", str(s), "-o", str(o)]))
     cxx = os.environ.get("CXX", "g++")
     for s in cpp:

@@ -49,7 +49,9 @@ struct TenoArgs {
     const double* phi;
     const uint32_t* cface;
     const uint8_t* smask;
-    double oi[KR_MAX * KR_MAX];  // oscillation indicator without dof 0, row-major (K-1)^2
+    double oi[KR_MAX * KR_MAX];   // oscillation indicator without dof 0, row-major (K-1)^2
+    double oi2[KR_MAX * KR_MAX];  // same, upper triangle with doubled off-diagonals (fast form)
+    float oi2f[KR_MAX * KR_MAX];  // oi2 in FP32 (FP32-bulk form)
 };
 
 struct FluxArgs {
@@ -91,12 +93,30 @@ struct SpecArgs {
     double gamma;
 };
 
-// Launchers (kernels.cu).  All return cudaGetLastError() of the launch.
-cudaError_t launch_teno(const TenoArgs& a, int K, int M, int nq, int variant, const double* U, double* fv,
-                        uint8_t* masks, cudaStream_t s);
+// Launchers.  All return cudaGetLastError() of the launch.
+// TENO and face flux exist twice: exact:: keeps the reference's rounding
+// (teno_flux_exact.cu), fast:: contracts to FMA (teno_flux_fast.cu).
+#define MGPU_DECLARE_TENO_FLUX                                                                              \
+    cudaError_t launch_teno(const TenoArgs& a, int K, int M, int nq, int variant, const double* U, double* fv, \
+                            uint8_t* masks, cudaStream_t s);                                                  \
+    cudaError_t launch_flux(const FluxArgs& a, const GasParams& g, const BcTable& bct, int rsolver, int nq,  \
+                            bool positivity, cudaStream_t s);
+namespace exact {
+MGPU_DECLARE_TENO_FLUX
+}
+namespace fast {
+MGPU_DECLARE_TENO_FLUX
+}
+#undef MGPU_DECLARE_TENO_FLUX
+// FP32-bulk form (fp32_fast.cu): face states in FP32, flux written in FP64.
+namespace f32 {
+cudaError_t launch_teno(const TenoArgs& a, int K, int M, int nq, const double* U, float* fv, uint8_t* masks,
+                        cudaStream_t s);
+cudaError_t launch_flux(const FluxArgs& a, const float* fv, const GasParams& g, const BcTable& bct, int rsolver,
+                        int nq, cudaStream_t s);
+}  // namespace f32
+// kernels.cu
 cudaError_t launch_first_order(int n_faces, const int2* lr, const double* U, double* fv, cudaStream_t s);
-cudaError_t launch_flux(const FluxArgs& a, const GasParams& g, const BcTable& bct, int rsolver, int nq,
-                        bool positivity, cudaStream_t s);
 cudaError_t launch_update(const UpdateArgs& a, const GasParams& g, int stage, cudaStream_t s);
 cudaError_t launch_spectral(const SpecArgs& a, cudaStream_t s);
 cudaError_t launch_dt(const unsigned long long* rmax_bits, double cfl, double* dt, double* t, unsigned* flags,

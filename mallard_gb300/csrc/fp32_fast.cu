@@ -1,0 +1,275 @@
+// fp32_fast.cu -- the FP32-bulk form of the reconstruction and face flux.
+//
+// Arithmetic split (everything else stays FP64):
+//  * FP32: TENO coefficients, smoothness indicators, stencil selection, face
+//    evaluation, face states, primitive recovery, Riemann flux;
+//  * FP64: the coefficient tables, transformed areas and face shapes in HBM
+//    (converted to FP32 as they are loaded), geometry (normals, areas,
+//    volumes), the conserved state and its accumulation across RK stages
+//    (the FP64 update kernel), and primitive recovery near vacuum: when the
+//    internal energy is under 1e-3 of the total the face state is recovered
+//    in FP64.
+// Stencil selection uses ratios of smoothness indicators: (SI+eps)^-6 itself
+// overflows FP32, but w_s / sum w = 1 / sum_d ((SI_s+eps)/(SI_d+eps))^6 does
+// not.  Only the corrected weighting is built in this form.
+#include <cstdint>
+
+#include "physics.cuh"
+
+namespace mgpu {
+namespace f32 {
+namespace {
+
+__device__ __forceinline__ float f(double x) { return __double2float_rn(x); }
+
+template <int K, int M, int NQ>
+__global__ void __launch_bounds__(128) teno32_kernel(const TenoArgs a, const double* __restrict__ U,
+                                                     float* __restrict__ fv, uint8_t* __restrict__ masks) {
+    constexpr int KR = K - 1, MR = M - 1, NF = 3, S = 4;
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const int cell = gt >> 2, v = gt & 3;
+    if (cell >= a.n_cells) return;
+    const int tile = cell >> 3, lane = cell & 7;
+    const float uc = f(U[(size_t)cell * NC + v]);
+    const unsigned sm = a.smask[cell];
+
+    float coef[S][KR];
+    float x[S];
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+#pragma unroll
+        for (int k = 0; k < KR; ++k) coef[s][k] = 0.0f;
+        x[s] = 0.0f;
+        if (!((sm >> s) & 1u)) continue;
+        const size_t base = ((size_t)tile * S + s) * MR;
+        const uint32_t* nbp = a.nb + base * TILE + lane;
+        const double* arp = a.ar + base * TILE + lane;
+        const double* Pp = a.P + base * KR * TILE + lane;
+#pragma unroll 4
+        for (int j = 0; j < MR; ++j) {
+            const uint32_t nbj = __ldg(nbp + j * TILE);
+            const float b = f(__ldg(arp + j * TILE)) * (f(__ldg(U + (size_t)nbj * NC + v)) - uc);
+#pragma unroll
+            for (int k = 0; k < KR; ++k) coef[s][k] = fmaf(f(__ldg(Pp + (j * KR + k) * TILE)), b, coef[s][k]);
+        }
+        float si = 0.0f;
+#pragma unroll
+        for (int i = 0; i < KR; ++i) {
+            float oa = a.oi2f[i * KR + i] * coef[s][i];
+#pragma unroll
+            for (int l = i + 1; l < KR; ++l) oa = fmaf(a.oi2f[i * KR + l], coef[s][l], oa);
+            si = fmaf(coef[s][i], oa, si);
+        }
+        x[s] = si + 1.0e-12f;
+    }
+
+    // stencil selection in ratio form
+    float rx[S];
+#pragma unroll
+    for (int s = 1; s < S; ++s) rx[s] = ((sm >> s) & 1u) ? 1.0f / x[s] : 0.0f;
+    float r = 0.0f;
+#pragma unroll
+    for (int d = 1; d < S; ++d) {
+        const float q = x[0] * rx[d], q2 = q * q;
+        r = fmaf(q2 * q2, q2, r);
+    }
+    unsigned mask = 0;
+    float w[S] = {0.0f, 0.0f, 0.0f, 0.0f};
+    if (r < 9999999.0f) {  // w0 / (w0 + sum_d w_d) > 1e-7
+        mask = 1;
+        w[0] = 1.0f;
+    } else {
+        int npass = 0;
+#pragma unroll
+        for (int s = 1; s < S; ++s) {
+            if (!((sm >> s) & 1u)) continue;
+            float t = 0.0f;
+#pragma unroll
+            for (int d = 1; d < S; ++d) {
+                const float q = x[s] * rx[d], q2 = q * q;
+                t = fmaf(q2 * q2, q2, t);
+            }
+            if (t < 1.0e5f) {  // w_s / sum_d w_d > 1e-5
+                mask |= 1u << s;
+                ++npass;
+            }
+        }
+        const float share = npass ? 1.0f / (float)npass : 0.0f;
+#pragma unroll
+        for (int s = 1; s < S; ++s) w[s] = ((mask >> s) & 1u) ? share : 0.0f;
+    }
+    if (masks) masks[(size_t)cell * NC + v] = (uint8_t)mask;
+#pragma unroll
+    for (int s = 0; s < S; ++s)
+#pragma unroll
+        for (int k = 0; k < KR; ++k) coef[s][k] *= w[s];
+
+#pragma unroll
+    for (int fl = 0; fl < NF; ++fl) {
+        const uint32_t slot = __ldg(a.cface + ((size_t)tile * NF + fl) * TILE + lane);
+        const size_t fi = slot >> 1;
+        const unsigned side = slot & 1u;
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+            const double* php = a.phi + (((size_t)tile * NF + fl) * NQ + q) * KR * TILE + lane;
+            float phi[KR];
+#pragma unroll
+            for (int k = 0; k < KR; ++k) phi[k] = f(__ldg(php + k * TILE));
+            float out = uc;
+#pragma unroll
+            for (int s = 0; s < S; ++s) {
+                if (w[s] == 0.0f) continue;
+#pragma unroll
+                for (int k = 0; k < KR; ++k) out = fmaf(coef[s][k], phi[k], out);
+            }
+            fv[((fi * NQ + q) * 2 + side) * NC + v] = out;
+        }
+    }
+}
+
+// Primitive recovery of a face state: FP32, or FP64 when the internal energy
+// is a small remainder of the total (near vacuum pressure).
+__device__ __forceinline__ void primitives_guarded(const GasParams& g, const float* U, float* W) {
+    primitives(g, U, W);
+    const float rho = U[0];
+    const float E = U[3] / rho;
+    const float e = W[3] * f(g.cv);
+    if (!(e > 1.0e-3f * E)) {
+        const double Ud[4] = {U[0], U[1], U[2], U[3]};
+        double Wd[5];
+        primitives(g, Ud, Wd);
+#pragma unroll
+        for (int i = 0; i < NPR; ++i) W[i] = f(Wd[i]);
+    }
+}
+
+template <int RS, int NQ>
+__global__ void __launch_bounds__(128) flux32_kernel(const FluxArgs a, const float* __restrict__ fv,
+                                                     const GasParams g, const BcTable bct) {
+    const int fi = blockIdx.x * blockDim.x + threadIdx.x;
+    if (fi >= a.n_faces) return;
+    const int2 lr = a.lr[fi];
+    const double2 nn = a.nrm[fi];
+    const float n[2] = {f(nn.x), f(nn.y)};
+    const int bi = a.bc[fi];
+    const int type = bi < 0 ? -1 : bct.bc[bi].type;
+    const float gam = f(g.gamma);
+    float F[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+        const float4* fq = reinterpret_cast<const float4*>(fv + ((size_t)fi * NQ + q) * 8);
+        float cl[4], cr[4], pl[5], pr[5], Ft[4];
+        {
+            const float4 x = fq[0];
+            cl[0] = x.x; cl[1] = x.y; cl[2] = x.z; cl[3] = x.w;
+        }
+        if (type < 0) {
+            const float4 x = fq[1];
+            cr[0] = x.x; cr[1] = x.y; cr[2] = x.z; cr[3] = x.w;
+        }
+        if (!admissible(g, cl))
+#pragma unroll
+            for (int i = 0; i < 4; i++) cl[i] = f(a.U[(size_t)lr.x * NC + i]);
+        if (type < 0 && !admissible(g, cr))
+#pragma unroll
+            for (int i = 0; i < 4; i++) cr[i] = f(a.U[(size_t)lr.y * NC + i]);
+        primitives_guarded(g, cl, pl);
+        if (type == MGPU_BC_WALL_ADIABATIC) {
+            Ft[0] = 0.0f;
+            Ft[1] = pl[2] * n[0];
+            Ft[2] = pl[2] * n[1];
+            Ft[3] = 0.0f;
+        } else {
+            if (type < 0) {
+                primitives_guarded(g, cr, pr);
+            } else if (type == MGPU_BC_SYMMETRY) {
+#pragma unroll
+                for (int i = 0; i < 4; i++) cr[i] = cl[i];
+#pragma unroll
+                for (int i = 0; i < NPR; i++) pr[i] = pl[i];
+                const float un = pl[0] * n[0] + pl[1] * n[1];
+                pr[0] = pl[0] - 2.0f * un * n[0];
+                pr[1] = pl[1] - 2.0f * un * n[1];
+            } else if (type == MGPU_BC_EXTRAPOLATION) {
+#pragma unroll
+                for (int i = 0; i < 4; i++) cr[i] = cl[i];
+#pragma unroll
+                for (int i = 0; i < NPR; i++) pr[i] = pl[i];
+            } else if (type == MGPU_BC_UPT) {
+                const double* d = bct.bc[bi].data;
+                cr[0] = f(d[0]);
+#pragma unroll
+                for (int i = 0; i < NPR; i++) pr[i] = f(d[i + 1]);
+            } else {  // MGPU_BC_P_OUT
+                const float rho_l = cl[0];
+                const float um = sqrtf(pl[0] * pl[0] + pl[1] * pl[1]);
+                const float sos = sqrtf(gam * pl[2] / rho_l);
+                const float po = (um < sos) ? f(bct.bc[bi].data[0]) : pl[2];
+                const float T = pl[3];
+                const float rho = po / (f(g.R) * T);
+                const float e = f(g.cv) * T;
+                cr[0] = rho;
+                pr[0] = pl[0];
+                pr[1] = pl[1];
+                pr[2] = po;
+                pr[3] = T;
+                pr[4] = e + po / rho;
+            }
+            riemann<RS>(Ft, n, cl[0], pl, pl[2], gam, pl[4], cr[0], pr, pr[2], gam, pr[4]);
+        }
+#pragma unroll
+        for (int i = 0; i < 4; i++) F[i] = fmaf(f(a.qw[q]), Ft[i], F[i]);
+    }
+    const double area = a.area[fi];
+    double2* Gf = reinterpret_cast<double2*>(a.G + (size_t)fi * 4);
+    Gf[0] = make_double2(area * (double)(F[0] * 0.5f), area * (double)(F[1] * 0.5f));
+    Gf[1] = make_double2(area * (double)(F[2] * 0.5f), area * (double)(F[3] * 0.5f));
+}
+
+template <int RS, int NQ>
+cudaError_t flux_go(const FluxArgs& a, const float* fv, const GasParams& g, const BcTable& bct, cudaStream_t s) {
+    const unsigned blocks = (unsigned)((a.n_faces + 127) / 128);
+    if (blocks) flux32_kernel<RS, NQ><<<blocks, 128, 0, s>>>(a, fv, g, bct);
+    return cudaGetLastError();
+}
+
+template <int RS>
+cudaError_t flux_nq(const FluxArgs& a, const float* fv, const GasParams& g, const BcTable& bct, int nq,
+                    cudaStream_t s) {
+    switch (nq) {
+        case 1: return flux_go<RS, 1>(a, fv, g, bct, s);
+        case 2: return flux_go<RS, 2>(a, fv, g, bct, s);
+    }
+    return cudaErrorInvalidValue;
+}
+
+template <int K, int M, int NQ>
+cudaError_t teno_go(const TenoArgs& a, const double* U, float* fv, uint8_t* masks, cudaStream_t s) {
+    const long long threads = (long long)a.n_cells * 4;
+    const unsigned blocks = (unsigned)((threads + 127) / 128);
+    if (blocks) teno32_kernel<K, M, NQ><<<blocks, 128, 0, s>>>(a, U, fv, masks);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_teno(const TenoArgs& a, int K, int M, int nq, const double* U, float* fv, uint8_t* masks,
+                        cudaStream_t s) {
+    if (K == 10 && M == 20 && nq == 2) return teno_go<10, 20, 2>(a, U, fv, masks, s);
+    if (K == 6 && M == 12 && nq == 1) return teno_go<6, 12, 1>(a, U, fv, masks, s);
+    if (K == 3 && M == 6 && nq == 1) return teno_go<3, 6, 1>(a, U, fv, masks, s);
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_flux(const FluxArgs& a, const float* fv, const GasParams& g, const BcTable& bct, int rsolver,
+                        int nq, cudaStream_t s) {
+    switch (rsolver) {
+        case MGPU_RIEMANN_RUSANOV: return flux_nq<MGPU_RIEMANN_RUSANOV>(a, fv, g, bct, nq, s);
+        case MGPU_RIEMANN_HLL: return flux_nq<MGPU_RIEMANN_HLL>(a, fv, g, bct, nq, s);
+        case MGPU_RIEMANN_HLLC: return flux_nq<MGPU_RIEMANN_HLLC>(a, fv, g, bct, nq, s);
+    }
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace f32
+}  // namespace mgpu

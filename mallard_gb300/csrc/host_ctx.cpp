@@ -141,6 +141,7 @@ struct mgpu_ctx {
 
     // device state and work arrays
     DevArray<double> U, Ut, W, prim, vol, fv, G, rho_cell, rhs, scal;  // scal: dt, t
+    DevArray<float> fv32;  // face states of the FP32-bulk form
     DevArray<unsigned> flags;
     DevArray<unsigned long long> rmax;
     DevArray<int2> lr;
@@ -201,9 +202,17 @@ struct mgpu_ctx {
         ck(cudaEventRecord(m.b, stream), "cudaEventRecord");
     }
 
+    bool fast() const { return cfg.precision == MGPU_PREC_FP64_FAST; }
+    bool single() const { return cfg.precision == MGPU_PREC_FP32; }
+
     void reconstruct(const double* Uin, uint8_t* mask_out) {
-        if (cfg.recon == MGPU_RECON_TENO) {
-            timed(0, [&] { return launch_teno(teno, K, M, nq, cfg.teno_variant, Uin, fv.p, mask_out, stream); });
+        if (single()) {
+            timed(0, [&] { return f32::launch_teno(teno, K, M, nq, Uin, fv32.p, mask_out, stream); });
+        } else if (cfg.recon == MGPU_RECON_TENO) {
+            timed(0, [&] {
+                return fast() ? fast::launch_teno(teno, K, M, nq, cfg.teno_variant, Uin, fv.p, mask_out, stream)
+                              : exact::launch_teno(teno, K, M, nq, cfg.teno_variant, Uin, fv.p, mask_out, stream);
+            });
         } else {
             timed(0, [&] { return launch_first_order((int)F_flux, lr.p, Uin, fv.p, stream); });
         }
@@ -221,7 +230,14 @@ struct mgpu_ctx {
         a.U = Uin;
         for (int i = 0; i < 4; i++) a.qw[i] = qw[i];
         const bool pos = cfg.recon == MGPU_RECON_TENO && cfg.teno_variant == MGPU_TENO_CORRECTED;
-        timed(1, [&] { return launch_flux(a, gas, bct, cfg.riemann_solver, nq, pos, stream); });
+        if (single()) {
+            timed(1, [&] { return f32::launch_flux(a, fv32.p, gas, bct, cfg.riemann_solver, nq, stream); });
+            return;
+        }
+        timed(1, [&] {
+            return fast() ? fast::launch_flux(a, gas, bct, cfg.riemann_solver, nq, pos, stream)
+                          : exact::launch_flux(a, gas, bct, cfg.riemann_solver, nq, pos, stream);
+        });
     }
 
     UpdateArgs update_args() {
@@ -525,7 +541,11 @@ void mgpu_ctx::build() {
         if (!err.empty()) throw Unsupported(err);
         teno.n_cells = (int)N;
         for (int i = 0; i < KR; ++i)
-            for (int l = 0; l < KR; ++l) teno.oi[i * KR + l] = t.oi[(size_t)(i + 1) * K + (l + 1)];
+            for (int l = 0; l < KR; ++l) {
+                teno.oi[i * KR + l] = t.oi[(size_t)(i + 1) * K + (l + 1)];
+                teno.oi2[i * KR + l] = l < i ? 0.0 : (l == i ? 1.0 : 2.0) * t.oi[(size_t)(i + 1) * K + (l + 1)];
+                teno.oi2f[i * KR + l] = (float)teno.oi2[i * KR + l];
+            }
         nb.upload(h_nb);
         ar.upload(h_ar);
         P.upload(h_P);
@@ -569,7 +589,8 @@ void mgpu_ctx::build() {
     rhs.alloc((size_t)N * 4);
     prim.alloc((size_t)N * 5);
     rho_cell.alloc(N);
-    fv.alloc((size_t)F_real * nq * 8);
+    if (cfg.precision == MGPU_PREC_FP32) fv32.alloc((size_t)F_real * nq * 8);
+    else fv.alloc((size_t)F_real * nq * 8);
     G.alloc((size_t)F_flux * 4);
     scal.alloc(2);
     flags.alloc(1);
@@ -659,7 +680,12 @@ int mgpu_create(const mgpu_mesh* mesh, const mgpu_config* cfg, mgpu_ctx** out) {
         if (cfg->recon != MGPU_RECON_FO && cfg->recon != MGPU_RECON_TENO) throw ArgFail("Unknown face reconstruction type.");
         if (cfg->riemann_solver < 0 || cfg->riemann_solver > 2) throw ArgFail("Unknown Riemann solver type.");
         if (cfg->time_integrator != MGPU_INTEGRATOR_SSPRK3) throw Unsupported("the GPU path implements SSPRK3");
-        if (cfg->precision != MGPU_PREC_FP64) throw Unsupported("unknown precision mode");
+        if (cfg->precision != MGPU_PREC_FP64 && cfg->precision != MGPU_PREC_FP64_FAST &&
+            cfg->precision != MGPU_PREC_FP32)
+            throw Unsupported("unknown precision mode");
+        if (cfg->precision == MGPU_PREC_FP32 &&
+            (cfg->recon != MGPU_RECON_TENO || cfg->teno_variant != MGPU_TENO_CORRECTED))
+            throw Unsupported("the FP32 form implements TENO with the corrected weighting");
         if (cfg->teno_variant != MGPU_TENO_REFERENCE && cfg->teno_variant != MGPU_TENO_CORRECTED)
             throw ArgFail("unknown TENO variant");
         if (cfg->basis != MGPU_BASIS_LEGENDRE && cfg->basis != MGPU_BASIS_MONOMIAL) throw ArgFail("Unknown basis type.");
@@ -821,12 +847,24 @@ int mgpu_calc_face_values(mgpu_ctx* ctx, const double* Uh, double* face, uint8_t
     return guarded([&] {
         if (!Uh || !face) throw ArgFail("null argument");
         ctx->upload_cells(ctx->Ut.p, Uh, 4);
-        ck(cudaMemsetAsync(ctx->fv.p, 0, ctx->fv.bytes(), ctx->stream), "cudaMemsetAsync");
+        const bool sgl = ctx->single();
+        if (sgl) ck(cudaMemsetAsync(ctx->fv32.p, 0, ctx->fv32.bytes(), ctx->stream), "cudaMemsetAsync");
+        else ck(cudaMemsetAsync(ctx->fv.p, 0, ctx->fv.bytes(), ctx->stream), "cudaMemsetAsync");
         ctx->reconstruct(ctx->Ut.p, ctx->masks.p);
         const int nq = ctx->nq;
         std::vector<double> tmp((size_t)ctx->F_real * nq * 8);
-        ck(cudaMemcpyAsync(tmp.data(), ctx->fv.p, tmp.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream),
-           "D2H");
+        if (sgl) {
+            std::vector<float> t32(tmp.size());
+            ck(cudaMemcpyAsync(t32.data(), ctx->fv32.p, t32.size() * sizeof(float), cudaMemcpyDeviceToHost,
+                               ctx->stream),
+               "D2H");
+            ck(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+            for (size_t i = 0; i < t32.size(); ++i) tmp[i] = t32[i];
+        } else {
+            ck(cudaMemcpyAsync(tmp.data(), ctx->fv.p, tmp.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                               ctx->stream),
+               "D2H");
+        }
         std::vector<uint8_t> mk((size_t)ctx->N * 4);
         if (tmask)
             ck(cudaMemcpyAsync(mk.data(), ctx->masks.p, mk.size(), cudaMemcpyDeviceToHost, ctx->stream), "D2H");

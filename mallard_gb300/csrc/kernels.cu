@@ -14,258 +14,11 @@
 // residual is deterministic and identical to Kokkos::Serial's.
 #include <cstdint>
 
-#include "device.h"
+#include "physics.cuh"
 
 namespace mgpu {
 
 namespace {
-
-constexpr int NC = 4;
-constexpr int NPR = 5;
-
-// ---------------------------------------------------------------------------
-// Euler physics (src/physics/physics.h:842-867)
-// ---------------------------------------------------------------------------
-
-__device__ __forceinline__ void primitives(const GasParams& g, const double* U, double* W) {
-    const double rho = U[0];
-    const double u0 = U[1] / rho, u1 = U[2] / rho;
-    const double E = U[3] / rho;
-    const double e = E - 0.5 * (u0 * u0 + u1 * u1);
-    const double p = fmax(g.p_min, fmin(g.p_max, (g.gamma - 1.0) * rho * e));
-    W[0] = u0;
-    W[1] = u1;
-    W[2] = p;
-    W[3] = e / g.cv;
-    W[4] = e + p / rho;
-}
-
-// ---------------------------------------------------------------------------
-// Riemann solvers (src/numerics/riemann_solver.h:205-519)
-// ---------------------------------------------------------------------------
-
-// star-region estimates; W = {rho, u_n, p, gamma}
-__device__ __forceinline__ void pvrs(const double* L, const double* R, double& ps) {
-    const double al = sqrt(L[3] * L[2] / L[0]);
-    const double ar = sqrt(R[3] * R[2] / R[0]);
-    const double rho_m = 0.5 * (L[0] + R[0]);
-    const double a_m = 0.5 * (al + ar);
-    ps = 0.5 * (L[2] + R[2]) + 0.5 * (L[1] - R[1]) * rho_m * a_m;
-}
-
-__device__ __noinline__ void trrs(const double* L, const double* R, double& ps) {
-    const double al = sqrt(L[3] * L[2] / L[0]);
-    const double ar = sqrt(R[3] * R[2] / R[0]);
-    const double zl = (L[3] - 1.0) / (2.0 * L[3]);
-    const double zr = (R[3] - 1.0) / (2.0 * R[3]);
-    const double plr = pow((L[2] / R[2]), zl);
-    const double us = (plr * L[1] / al + R[1] / ar + 2.0 * (1.0 - plr) / (L[3] - 1.0)) / (plr / al + 1.0 / ar);
-    ps = 0.5 * (L[2] * pow((1.0 + (L[3] - 1.0) / (2.0 * al) * (L[1] - us)), (1.0 / zl)) +
-                R[2] * pow((1.0 + (R[3] - 1.0) / (2.0 * ar) * (us - R[1])), (1.0 / zr)));
-}
-
-__device__ __noinline__ void tsrs(const double* L, const double* R, double& ps) {
-    const double gl = (L[3] - 1.0) / (L[3] + 1.0);
-    const double gr = (R[3] - 1.0) / (R[3] + 1.0);
-    const double Al = 2.0 / (L[3] + 1.0) / L[0], Bl = gl * L[2];
-    const double Ar = 2.0 / (R[3] + 1.0) / R[0], Br = gr * R[2];
-    const double p0 = fmax(0.0, ps);
-    const double ql = sqrt(Al / (p0 + Bl));
-    const double qr = sqrt(Ar / (p0 + Br));
-    ps = (ql * L[2] + qr * R[2] - (R[1] - L[1])) / (ql + qr);
-}
-
-// ANRS (riemann_solver.h:308-329); only p_star is used by HLL/HLLC.
-__device__ __forceinline__ double anrs(const double* L, const double* R) {
-    const double pmax = fmax(L[2], R[2]), pmin = fmin(L[2], R[2]);
-    const double qmax = pmax / pmin;
-    double ps;
-    pvrs(L, R, ps);
-    if ((qmax < 2.0) && (pmin <= ps) && (ps <= pmax)) return ps;
-    if (ps < pmin) trrs(L, R, ps);
-    else tsrs(L, R, ps);
-    return ps;
-}
-
-template <int RS>
-__device__ __forceinline__ void riemann(double* F, const double* n, double rl, const double* ul, double pl, double gl,
-                                        double hl, double rr, const double* ur, double pr, double gr, double hr) {
-    const double unl = ul[0] * n[0] + ul[1] * n[1];
-    const double unr = ur[0] * n[0] + ur[1] * n[1];
-    const double qql = ul[0] * ul[0] + ul[1] * ul[1];
-    const double qqr = ur[0] * ur[0] + ur[1] * ur[1];
-    const double al = sqrt(gl * pl / rl);
-    const double ar = sqrt(gr * pr / rr);
-    const double El = (hl + 0.5 * qql) * rl - pl;
-    const double Er = (hr + 0.5 * qqr) * rr - pr;
-    const double Ul[4] = {rl, rl * ul[0], rl * ul[1], El};
-    const double Ur[4] = {rr, rr * ur[0], rr * ur[1], Er};
-    const double Fl[4] = {rl * unl, rl * ul[0] * unl + pl * n[0], rl * ul[1] * unl + pl * n[1], (El + pl) * unl};
-    const double Fr[4] = {rr * unr, rr * ur[0] * unr + pr * n[0], rr * ur[1] * unr + pr * n[1], (Er + pr) * unr};
-    if (RS == MGPU_RIEMANN_RUSANOV) {
-        const double smax = fmax(fabs(unl) + al, fabs(unr) + ar);
-#pragma unroll
-        for (int i = 0; i < 4; i++) F[i] = 0.5 * (Fl[i] + Fr[i] + smax * (Ul[i] - Ur[i]));
-        return;
-    }
-    const double Wl[4] = {rl, unl, pl, gl}, Wr[4] = {rr, unr, pr, gr};
-    const double ps = anrs(Wl, Wr);
-    const double ql = (ps <= pl) ? 1.0 : sqrt(1.0 + (gl + 1.0) / (2.0 * gl) * (ps / pl - 1.0));
-    const double qr = (ps <= pr) ? 1.0 : sqrt(1.0 + (gr + 1.0) / (2.0 * gr) * (ps / pr - 1.0));
-    const double Sl = unl - al * ql;
-    const double Sr = unr + ar * qr;
-    if (RS == MGPU_RIEMANN_HLL) {
-        if (0.0 <= Sl) {
-#pragma unroll
-            for (int i = 0; i < 4; i++) F[i] = Fl[i];
-        } else if (Sr <= 0.0) {
-#pragma unroll
-            for (int i = 0; i < 4; i++) F[i] = Fr[i];
-        } else {
-#pragma unroll
-            for (int i = 0; i < 4; i++) F[i] = (Sr * Fl[i] - Sl * Fr[i] + Sl * Sr * (Ur[i] - Ul[i])) / (Sr - Sl);
-        }
-        return;
-    }
-    const double Ss = (pr - pl + rl * unl * (Sl - unl) - rr * unr * (Sr - unr)) / (rl * (Sl - unl) - rr * (Sr - unr));
-    if (0.0 <= Sl) {
-#pragma unroll
-        for (int i = 0; i < 4; i++) F[i] = Fl[i];
-    } else if (Sr <= 0.0) {
-#pragma unroll
-        for (int i = 0; i < 4; i++) F[i] = Fr[i];
-    } else {
-        const double D[4] = {0.0, n[0], n[1], Ss};
-        const double Plr = 0.5 * (pl + pr + rl * (Sl - unl) * (Ss - unl) + rr * (Sr - unr) * (Ss - unr));
-        if (Ss >= 0.0) {
-#pragma unroll
-            for (int i = 0; i < 4; i++) F[i] = (Ss * (Sl * Ul[i] - Fl[i]) + Sl * Plr * D[i]) / (Sl - Ss);
-        } else {
-#pragma unroll
-            for (int i = 0; i < 4; i++) F[i] = (Ss * (Sr * Ur[i] - Fr[i]) + Sr * Plr * D[i]) / (Sr - Ss);
-        }
-    }
-}
-
-// Correctly rounded x^6 (up to a 2^-100 relative window) from an exact
-// double-double evaluation: x^2, x^4 = (x^2)^2, x^6 = x^4 x^2 with the
-// rounding error of every product carried along (Dekker/Ogita-Rump-Oishi
-// error-free products via fma).  Stands in for the reference's
-// pow(x, 6.0), which its C library evaluates to within 0.52 ulp.
-__device__ __forceinline__ double pow6(double x) {
-    const double h2 = x * x;
-    const double l2 = fma(x, x, -h2);
-    const double h4 = h2 * h2;
-    const double l4 = fma(h2, h2, -h4) + 2.0 * h2 * l2;
-    const double h6 = h4 * h2;
-    const double l6 = fma(h4, h2, -h6) + (h4 * l2 + l4 * h2);
-    return h6 + l6;
-}
-
-// ---------------------------------------------------------------------------
-// TENO reconstruction (face_reconstruction.cpp:866-1039)
-// ---------------------------------------------------------------------------
-// Four lanes per cell, one per conserved variable; eight cells per warp.
-// Each lane keeps the reduced coefficients of all four stencils in
-// registers until the weights are known, then writes its variable at the
-// quadrature points of the cell's three faces.
-
-template <int K, int M, int NQ, int VARIANT>
-__global__ void __launch_bounds__(128) teno_kernel(const TenoArgs a, const double* __restrict__ U,
-                                                   double* __restrict__ fv, uint8_t* __restrict__ masks) {
-    constexpr int KR = K - 1, MR = M - 1, NF = 3, S = 4;
-    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
-    const int cell = gt >> 2, v = gt & 3;
-    if (cell >= a.n_cells) return;
-    const int tile = cell >> 3, lane = cell & 7;
-    const double uc = U[(size_t)cell * NC + v];
-    const unsigned sm = a.smask[cell];
-
-    double coef[S][KR];
-    double w[S];
-#pragma unroll
-    for (int s = 0; s < S; ++s) {
-#pragma unroll
-        for (int k = 0; k < KR; ++k) coef[s][k] = 0.0;
-        w[s] = 0.0;
-        if (!((sm >> s) & 1u)) continue;
-        const size_t base = ((size_t)tile * S + s) * MR;
-        const uint32_t* nbp = a.nb + base * TILE + lane;
-        const double* arp = a.ar + base * TILE + lane;
-        const double* Pp = a.P + base * KR * TILE + lane;
-#pragma unroll 4
-        for (int j = 0; j < MR; ++j) {
-            const uint32_t nbj = __ldg(nbp + j * TILE);
-            const double b = __ldg(arp + j * TILE) * (__ldg(U + (size_t)nbj * NC + v) - uc);
-#pragma unroll
-            for (int k = 0; k < KR; ++k) coef[s][k] = coef[s][k] + __ldg(Pp + (j * KR + k) * TILE) * b;
-        }
-        // smoothness indicator a^T (OI a), dof 0 omitted (its coefficient is exactly zero)
-        double si = 0.0;
-#pragma unroll
-        for (int i = 0; i < KR; ++i) {
-            double oa = 0.0;
-#pragma unroll
-            for (int l = 0; l < KR; ++l) oa = oa + a.oi[i * KR + l] * coef[s][l];
-            si = si + coef[s][i] * oa;
-        }
-        w[s] = 1.0 / pow6(si + 1.0e-12);
-    }
-
-    // stencil selection (face_reconstruction.cpp:947-981)
-    double sd = 0.0;
-#pragma unroll
-    for (int s = 1; s < S; ++s) sd = sd + w[s];
-    unsigned mask = 0;
-    if (w[0] / (sd + w[0]) > 1.0e-7) {
-        w[0] = 1.0;
-#pragma unroll
-        for (int s = 1; s < S; ++s) w[s] = 0.0;
-        mask = 1;
-    } else {
-#pragma unroll
-        for (int s = 1; s < S; ++s)
-            if (w[s] / sd > 1.0e-5) {
-                w[s] = (1.0 / K);
-                mask |= 1u << s;
-            }
-        if (VARIANT == MGPU_TENO_CORRECTED) {
-            w[0] = 0.0;
-#pragma unroll
-            for (int s = 1; s < S; ++s)
-                if (!((mask >> s) & 1u)) w[s] = 0.0;
-        }
-        sd = 0.0;
-#pragma unroll
-        for (int s = 1; s < S; ++s) sd = sd + w[s];
-#pragma unroll
-        for (int s = 1; s < S; ++s) w[s] = w[s] / sd;
-    }
-    if (masks) masks[(size_t)cell * NC + v] = (uint8_t)mask;
-
-    // face states at the quadrature points
-#pragma unroll
-    for (int fl = 0; fl < NF; ++fl) {
-        const uint32_t slot = __ldg(a.cface + ((size_t)tile * NF + fl) * TILE + lane);
-        const size_t f = slot >> 1;
-        const unsigned side = slot & 1u;
-#pragma unroll
-        for (int q = 0; q < NQ; ++q) {
-            const double* php = a.phi + (((size_t)tile * NF + fl) * NQ + q) * KR * TILE + lane;
-            double phi[KR];
-#pragma unroll
-            for (int k = 0; k < KR; ++k) phi[k] = __ldg(php + k * TILE);
-            double out = uc;
-#pragma unroll
-            for (int s = 0; s < S; ++s) {
-                if (w[s] == 0.0) continue;
-#pragma unroll
-                for (int k = 0; k < KR; ++k) out = out + (w[s] * coef[s][k]) * phi[k];
-            }
-            fv[((f * NQ + q) * 2 + side) * NC + v] = out;
-        }
-    }
-}
 
 // FirstOrderFunctor (face_reconstruction.cpp:59-99): both sides take the
 // adjacent cell averages; boundary faces fill side 0 only.
@@ -277,102 +30,6 @@ __global__ void __launch_bounds__(256) first_order_kernel(int n_faces, const int
     const int2 c = lr[f];
     fv[(size_t)f * 8 + v] = U[(size_t)c.x * NC + v];
     if (c.y >= 0) fv[(size_t)f * 8 + 4 + v] = U[(size_t)c.y * NC + v];
-}
-
-// ---------------------------------------------------------------------------
-// Face flux (flux_functor.h:124-178 and src/boundary/boundary_*.cpp)
-// ---------------------------------------------------------------------------
-
-__device__ __forceinline__ bool admissible(const GasParams& g, const double* W) {
-    const double rho = W[0];
-    if (!(rho > 0.0)) return false;
-    const double u0 = W[1] / rho, u1 = W[2] / rho;
-    const double e = W[3] / rho - 0.5 * (u0 * u0 + u1 * u1);
-    return (g.gamma - 1.0) * rho * e > 0.0;
-}
-
-template <int RS, int NQ, bool POSITIVITY>
-__global__ void __launch_bounds__(128) flux_kernel(const FluxArgs a, const GasParams g, const BcTable bct) {
-    const int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= a.n_faces) return;
-    const int2 lr = a.lr[f];
-    const double2 nn = a.nrm[f];
-    const double n[2] = {nn.x, nn.y};
-    const int bi = a.bc[f];
-    const int type = bi < 0 ? -1 : bct.bc[bi].type;
-    double F[4] = {0.0, 0.0, 0.0, 0.0};
-#pragma unroll
-    for (int q = 0; q < NQ; ++q) {
-        const double2* fq = reinterpret_cast<const double2*>(a.fv + ((size_t)f * NQ + q) * 8);
-        double cl[4], cr[4], pl[5], pr[5], Ft[4];
-        {
-            const double2 x0 = fq[0], x1 = fq[1];
-            cl[0] = x0.x; cl[1] = x0.y; cl[2] = x1.x; cl[3] = x1.y;
-        }
-        if (type < 0) {
-            const double2 x2 = fq[2], x3 = fq[3];
-            cr[0] = x2.x; cr[1] = x2.y; cr[2] = x3.x; cr[3] = x3.y;
-        }
-        if (POSITIVITY) {
-            if (!admissible(g, cl))
-#pragma unroll
-                for (int i = 0; i < 4; i++) cl[i] = a.U[(size_t)lr.x * NC + i];
-            if (type < 0 && !admissible(g, cr))
-#pragma unroll
-                for (int i = 0; i < 4; i++) cr[i] = a.U[(size_t)lr.y * NC + i];
-        }
-        primitives(g, cl, pl);
-        if (type == MGPU_BC_WALL_ADIABATIC) {
-            Ft[0] = 0.0;
-            Ft[1] = pl[2] * n[0];
-            Ft[2] = pl[2] * n[1];
-            Ft[3] = 0.0;
-        } else {
-            if (type < 0) {
-                primitives(g, cr, pr);
-            } else if (type == MGPU_BC_SYMMETRY) {
-                // right state = left state with the velocity reflected
-#pragma unroll
-                for (int i = 0; i < 4; i++) cr[i] = cl[i];
-#pragma unroll
-                for (int i = 0; i < NPR; i++) pr[i] = pl[i];
-                const double un = pl[0] * n[0] + pl[1] * n[1];
-                pr[0] = pl[0] - 2.0 * un * n[0];
-                pr[1] = pl[1] - 2.0 * un * n[1];
-            } else if (type == MGPU_BC_EXTRAPOLATION) {
-#pragma unroll
-                for (int i = 0; i < 4; i++) cr[i] = cl[i];
-#pragma unroll
-                for (int i = 0; i < NPR; i++) pr[i] = pl[i];
-            } else if (type == MGPU_BC_UPT) {
-                const double* d = bct.bc[bi].data;
-                cr[0] = d[0];
-#pragma unroll
-                for (int i = 0; i < NPR; i++) pr[i] = d[i + 1];
-            } else {  // MGPU_BC_P_OUT
-                const double rho_l = cl[0];
-                const double um = sqrt(pl[0] * pl[0] + pl[1] * pl[1]);
-                const double sos = sqrt(g.gamma * pl[2] / rho_l);
-                const double po = (um < sos) ? bct.bc[bi].data[0] : pl[2];
-                const double T = pl[3];
-                const double rho = po / (g.R * T);
-                const double e = g.cv * T;
-                cr[0] = rho;
-                pr[0] = pl[0];
-                pr[1] = pl[1];
-                pr[2] = po;
-                pr[3] = T;
-                pr[4] = e + po / rho;
-            }
-            riemann<RS>(Ft, n, cl[0], pl, pl[2], g.gamma, pl[4], cr[0], pr, pr[2], g.gamma, pr[4]);
-        }
-#pragma unroll
-        for (int i = 0; i < 4; i++) F[i] += a.qw[q] * Ft[i];
-    }
-    const double area = a.area[f];
-    double2* Gf = reinterpret_cast<double2*>(a.G + (size_t)f * 4);
-    Gf[0] = make_double2(area * (F[0] * 0.5), area * (F[1] * 0.5));
-    Gf[1] = make_double2(area * (F[2] * 0.5), area * (F[3] * 0.5));
 }
 
 // ---------------------------------------------------------------------------
@@ -594,47 +251,7 @@ __global__ void fp64_probe_kernel(double* out, int iters, double seed) {
     if (s == 12345.678) out[0] = s;  // keeps the chains live
 }
 
-template <int K, int M, int NQ>
-cudaError_t teno_dispatch_variant(const TenoArgs& a, int variant, const double* U, double* fv, uint8_t* masks,
-                                  cudaStream_t s) {
-    const long long threads = (long long)a.n_cells * 4;
-    const unsigned blocks = (unsigned)((threads + 127) / 128);
-    if (blocks == 0) return cudaSuccess;
-    if (variant == MGPU_TENO_CORRECTED)
-        teno_kernel<K, M, NQ, MGPU_TENO_CORRECTED><<<blocks, 128, 0, s>>>(a, U, fv, masks);
-    else
-        teno_kernel<K, M, NQ, MGPU_TENO_REFERENCE><<<blocks, 128, 0, s>>>(a, U, fv, masks);
-    return cudaGetLastError();
-}
-
-template <int RS, int NQ>
-cudaError_t flux_dispatch_pos(const FluxArgs& a, const GasParams& g, const BcTable& bct, bool pos, cudaStream_t s) {
-    const unsigned blocks = (unsigned)((a.n_faces + 127) / 128);
-    if (blocks == 0) return cudaSuccess;
-    if (pos) flux_kernel<RS, NQ, true><<<blocks, 128, 0, s>>>(a, g, bct);
-    else flux_kernel<RS, NQ, false><<<blocks, 128, 0, s>>>(a, g, bct);
-    return cudaGetLastError();
-}
-
-template <int RS>
-cudaError_t flux_dispatch_nq(const FluxArgs& a, const GasParams& g, const BcTable& bct, int nq, bool pos,
-                             cudaStream_t s) {
-    switch (nq) {
-        case 1: return flux_dispatch_pos<RS, 1>(a, g, bct, pos, s);
-        case 2: return flux_dispatch_pos<RS, 2>(a, g, bct, pos, s);
-    }
-    return cudaErrorInvalidValue;
-}
-
 }  // namespace
-
-cudaError_t launch_teno(const TenoArgs& a, int K, int M, int nq, int variant, const double* U, double* fv,
-                        uint8_t* masks, cudaStream_t s) {
-    if (K == 10 && M == 20 && nq == 2) return teno_dispatch_variant<10, 20, 2>(a, variant, U, fv, masks, s);
-    if (K == 6 && M == 12 && nq == 1) return teno_dispatch_variant<6, 12, 1>(a, variant, U, fv, masks, s);
-    if (K == 3 && M == 6 && nq == 1) return teno_dispatch_variant<3, 6, 1>(a, variant, U, fv, masks, s);
-    return cudaErrorInvalidValue;
-}
 
 cudaError_t launch_first_order(int n_faces, const int2* lr, const double* U, double* fv, cudaStream_t s) {
     const long long threads = (long long)n_faces * 4;
@@ -642,16 +259,6 @@ cudaError_t launch_first_order(int n_faces, const int2* lr, const double* U, dou
     if (blocks == 0) return cudaSuccess;
     first_order_kernel<<<blocks, 256, 0, s>>>(n_faces, lr, U, fv);
     return cudaGetLastError();
-}
-
-cudaError_t launch_flux(const FluxArgs& a, const GasParams& g, const BcTable& bct, int rsolver, int nq,
-                        bool positivity, cudaStream_t s) {
-    switch (rsolver) {
-        case MGPU_RIEMANN_RUSANOV: return flux_dispatch_nq<MGPU_RIEMANN_RUSANOV>(a, g, bct, nq, positivity, s);
-        case MGPU_RIEMANN_HLL: return flux_dispatch_nq<MGPU_RIEMANN_HLL>(a, g, bct, nq, positivity, s);
-        case MGPU_RIEMANN_HLLC: return flux_dispatch_nq<MGPU_RIEMANN_HLLC>(a, g, bct, nq, positivity, s);
-    }
-    return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_update(const UpdateArgs& a, const GasParams& g, int stage, cudaStream_t s) {

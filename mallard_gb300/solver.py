@@ -80,7 +80,7 @@ class Solver:
                  max_stencil_size_factor=2.0, quadrature_order_cell=0, quadrature_order_face=0,
                  riemann_solver="HLLC", time_integrator="SSPRK3", gamma=1.4, p_ref=101325.0, T_ref=298.15,
                  rho_ref=1.225, p_min=-1e20, p_max=1e20, boundaries=(), teno_variant="reference", reorder=True,
-                 device=0):
+                 device=0, precision="fp64"):
         self._lib = N.lib()
         self.mesh = mesh
         self.gas = dict(gamma=gamma, p_ref=p_ref, T_ref=T_ref, rho_ref=rho_ref)
@@ -104,6 +104,10 @@ class Solver:
         cfg.gamma, cfg.p_ref, cfg.T_ref, cfg.rho_ref = gamma, p_ref, T_ref, rho_ref
         cfg.p_min, cfg.p_max = p_min, p_max
         cfg.teno_variant = N.TENO_VARIANTS[teno_variant]
+        if precision not in N.PRECISIONS:
+            raise RuntimeError(f"Unknown precision: {precision}.")
+        cfg.precision = N.PRECISIONS[precision]
+        self.precision = precision
         cfg.reorder = 1 if reorder else 0
         cfg.device = int(device)
         self.cfg = cfg

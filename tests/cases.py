@@ -79,7 +79,7 @@ BC_DATA = {
 
 
 def make_pair(mesh, recon="TENO", riemann="HLLC", variant="reference", bcs=None, poly_order=3, p_min=-1e20,
-              p_max=1e20, reorder=True):
+              p_max=1e20, reorder=True, precision="fp64"):
     """A GPU solver and an oracle case on the same mesh and numerics."""
     bcs = bcs or {name: "extrapolation" for name in mesh.zone_names[1:]}
     blist = []
@@ -89,7 +89,7 @@ def make_pair(mesh, recon="TENO", riemann="HLLC", variant="reference", bcs=None,
         blist.append(d)
     s = mg.Solver(mesh, face_reconstruction=recon, basis_type="legendre", basis_order=poly_order,
                   riemann_solver=riemann, boundaries=blist, teno_variant=variant, reorder=reorder, p_min=p_min,
-                  p_max=p_max, **GAS)
+                  p_max=p_max, precision=precision, **GAS)
     om = OracleMesh.from_arrays(mesh)
     oc = OracleCase(om, recon=recon, basis="legendre", poly_order=poly_order, riemann=riemann, p_min=p_min,
                     p_max=p_max, **GAS)

@@ -1,0 +1,67 @@
+"""The FP32-bulk form against the FP64 oracle (corrected TENO weighting).
+
+Reported and bounded: relative errors of face states and residuals per
+stage, and the L1 / L-infinity density error, mass and energy drift after
+100 steps.  Bounds are loose multiples of FP32 round-off; the benchmark's
+bar is 1e-3 relative L1 density error.
+"""
+
+import numpy as np
+import pytest
+
+from cases import four_quadrant, make_pair, perturbed, pulse, real_faces
+from test_gpu_parity import tri_mesh
+from conftest import rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("ic", [four_quadrant, perturbed])
+def test_fp32_face_values(ic):
+    m = tri_mesh(24, seed=20261203)
+    s, oc = make_pair(m, variant="corrected", precision="fp32")
+    U, _ = ic(m)
+    F, M = s.calc_face_values(U, masks=True)
+    Fo, Mo = oc.face_values(U, masks=True)
+    assert (M == Mo).mean() > 0.99
+    f, _ = real_faces(m)
+    agree = (M == Mo).all(1)
+    cells_ok = np.zeros(m.n_faces, dtype=bool)
+    cof = m.cells_of_face[f, 0]
+    cells_ok[f] = agree[cof]
+    sel = f[cells_ok[f]]
+    err = rel_err(F[sel][:, :, 0].reshape(len(sel), -1), Fo[sel][:, :, 0].reshape(len(sel), -1))
+    assert err.max() < 1e-4, err.max()
+
+
+@pytest.mark.parametrize("riemann", ["Rusanov", "HLLC"])
+def test_fp32_residual(riemann):
+    m = tri_mesh(24, seed=20261203)
+    s, oc = make_pair(m, riemann=riemann, variant="corrected", precision="fp32")
+    U, _ = perturbed(m)
+    err = rel_err(s.calc_rhs(U), oc.calc_rhs(U))
+    assert np.median(err) < 1e-5 and err.max() < 1e-2, (np.median(err), err.max())
+
+
+def test_fp32_100_steps_errors():
+    m = tri_mesh(32, seed=20261203)
+    bcs = {z: "symmetry" for z in ("left", "right", "top", "bottom")}
+    s, oc = make_pair(m, variant="corrected", bcs=bcs, precision="fp32")
+    U, W = pulse(m)
+    s.set_state(U, W)
+    oc.set_state(U, W)
+    s.run(0.5, 100)
+    oc.run(0.5, 100)
+    Ug, _ = s.get_state()
+    Uo, _ = oc.get_state()
+    vol = m.cell_volume
+    l1 = np.sum(vol * np.abs(Ug[:, 0] - Uo[:, 0])) / np.sum(vol * np.abs(Uo[:, 0]))
+    linf = np.max(np.abs(Ug[:, 0] - Uo[:, 0])) / np.max(np.abs(Uo[:, 0]))
+    mass0 = np.sum(vol * U[:, 0])
+    drift32 = abs(np.sum(vol * Ug[:, 0]) - mass0) / mass0
+    drift64 = abs(np.sum(vol * Uo[:, 0]) - mass0) / mass0
+    e_drift = abs(np.sum(vol * Ug[:, 3]) - np.sum(vol * Uo[:, 3])) / np.sum(vol * Uo[:, 3])
+    print(f"fp32 vs fp64 after 100 steps: L1 {l1:.2e} Linf {linf:.2e} mass drift fp32 {drift32:.2e} "
+          f"fp64 {drift64:.2e} energy diff {e_drift:.2e}")
+    assert l1 < 1e-5 and linf < 1e-4
+    assert drift32 < 1e-6 and e_drift < 1e-6
