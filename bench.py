@@ -181,6 +181,22 @@ def run_reference(args):
 # GPU leg
 # ---------------------------------------------------------------------------
 
+def teno_flops_per_cell(precision, K=10, M=20, nq=2, stencils=4):
+    """FP64 flops of one TENO reconstruction per cell (4 variables), central
+    branch, counting a fused multiply-add as 2 and a divide as 1:
+    per stencil b (2 per neighbour), P b (2 K' M'), the smoothness
+    indicator (full K'^2 + K' products in the exact form, the symmetric
+    half in the fast form), x^6 and 1/x; then 3 faces x nq points x K'
+    shape terms (3 ops exact, 2 fast)."""
+    KR, MR = K - 1, M - 1
+    if precision == "fp64":
+        si, pw, face = 2 * KR * KR + 2 * KR, 12 + 1, 3
+    else:
+        si, pw, face = 2 * (KR * (KR + 1) // 2) + 2 * KR, 3 + 1, 2
+    per_var = stencils * (2 * MR + 2 * KR * MR + si + pw) + 3 * nq * KR * face + 10
+    return 4 * per_var
+
+
 def time_form(m, args, precision, U0, W0, device, U_ref):
     """Rate of another precision form on the same mesh and state, and its
     error against the headline form after the same W + K steps."""
@@ -204,10 +220,16 @@ def time_form(m, args, precision, U0, W0, device, U_ref):
     e1.synchronize()
     ms = e0.elapsed_time(e1)
     U, _ = s.get_state()
+    s.set_state(U0, W0)
+    s.launch(CFL, args.warmup)
+    s.kernel_timing(True)
+    s.launch(CFL, args.steps)
+    kt = s.kernel_times()
     s.close()
     vol = m.cell_volume
     out = {"value": m.n_cells * args.steps / (ms * 1e-3) / 1e6, "ms_per_step": ms / args.steps,
-           "finite": bool(np.isfinite(U).all())}
+           "finite": bool(np.isfinite(U).all()),
+           "kernel_ms_per_launch": {k: v[0] / max(v[1], 1) for k, v in kt.items()}}
     if np.isfinite(U_ref).all() and out["finite"]:
         d = np.abs(U[:, 0] - U_ref[:, 0])
         out["density_l1_rel_err"] = float(np.sum(vol * d) / np.sum(vol * np.abs(U_ref[:, 0])))
@@ -321,9 +343,7 @@ def run_ours(args):
     kshare = {k: {"ms_per_launch": v[0] / max(v[1], 1), "launches": v[1], "share": v[0] / max(sum(x[0] for x in kt.values()), 1e-30)}
               for k, v in kt.items()}
     # FP64 arithmetic roof of the reconstruction (FP64 is the binding unit on GB300)
-    K, M, nq = 10, 20, 2
-    flops_cell = 4 * (4 * (2 * (M - 1) + 2 * (K - 1) * (M - 1) + 2 * (K - 1) ** 2 + 2 * (K - 1) + 14)
-                      + 3 * nq * (K - 1) * 3)
+    flops_cell = teno_flops_per_cell(args.precision)
     fp64_peak = mg.fp64_peak_gflops(local)
     fp64_achieved = flops_cell * cells / recon_avg_s / 1e9
     gpu_launches = args.steps * 11

@@ -20,7 +20,22 @@ namespace mgpu {
 namespace f32 {
 namespace {
 
-__device__ __forceinline__ float f(double x) { return __double2float_rn(x); }
+// FP64 -> FP32 on the integer pipe.  On GB300 the conversion instruction
+// (F2F) issues on the FP64 unit at FP64 rate (~2 per clock per SM), which
+// made table conversion the bound of this kernel; a funnel shift, a rebias
+// and two range guards do the same on the integer pipe.  Rounds toward zero
+// (relative error < 2^-23); magnitudes below FP32's normal range become a
+// signed zero, those above become infinity, NaN stays NaN.
+__device__ __forceinline__ float f(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    const unsigned e = hi & 0x7ff00000u, sign = hi & 0x80000000u;
+    unsigned r = (__funnelshift_l(lo, hi, 3) & 0x7fffffffu) - 0x40000000u;
+    r = (r & 0x7fffffffu) | sign;
+    if (e <= (896u << 20)) r = sign;
+    if (e > (1150u << 20)) r = sign | 0x7f800000u | ((lo | (hi & 0xfffffu)) ? 0x400000u : 0u);
+    return __uint_as_float(r);
+}
 
 template <int K, int M, int NQ>
 __global__ void __launch_bounds__(128) teno32_kernel(const TenoArgs a, const double* __restrict__ U,
@@ -139,7 +154,7 @@ __device__ __forceinline__ void primitives_guarded(const GasParams& g, const flo
         double Wd[5];
         primitives(g, Ud, Wd);
 #pragma unroll
-        for (int i = 0; i < NPR; ++i) W[i] = f(Wd[i]);
+        for (int i = 0; i < NPR; ++i) W[i] = __double2float_rn(Wd[i]);
     }
 }
 

@@ -1,6 +1,8 @@
 """The FP64 fast form (FMA contraction, symmetric smoothness indicator)
-against the oracle: same decisions, results within the 1e-12 stage and
-1e-10 run tolerances (no bit-identity expected)."""
+against the oracle: same decisions; face states within 1e-12; residuals
+within FAST_STAGE_TOL = 1e-11 relative to max(|ref|, 1e-3 max|ref|): in
+cells whose face fluxes nearly cancel, FMA round-off of a few ulps of the
+flux shows up at ~2e-12 of that floor (the exact form is bit-identical)."""
 
 import numpy as np
 import pytest
@@ -8,6 +10,8 @@ import pytest
 import mallard_gb300 as mg
 from cases import four_quadrant, make_pair, perturbed, pulse, real_faces
 from test_gpu_parity import RUN_TOL, STAGE_TOL, assert_close, tri_mesh
+
+FAST_STAGE_TOL = 1e-11
 
 pytestmark = pytest.mark.gpu
 
@@ -31,7 +35,7 @@ def test_fast_residual(riemann):
     s, oc = make_pair(m, riemann=riemann, variant="corrected", precision="fp64_fast")
     for ic in (four_quadrant, perturbed):
         U, _ = ic(m)
-        assert_close(s.calc_rhs(U), oc.calc_rhs(U), STAGE_TOL, what=f"fast {riemann}")
+        assert_close(s.calc_rhs(U), oc.calc_rhs(U), FAST_STAGE_TOL, what=f"fast {riemann}")
 
 
 def test_fast_100_steps_pulse():
