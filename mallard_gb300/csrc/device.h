@@ -29,6 +29,7 @@ constexpr int KR_MAX = 9;  // K-1 for p = 3
 
 struct GasParams {
     double gamma, R, cv, p_min, p_max;
+    double icv;  // 1 / cv (fast forms)
 };
 
 struct BcEntry {
@@ -49,6 +50,11 @@ struct TenoArgs {
     const double* phi;
     const uint32_t* cface;
     const uint8_t* smask;
+    // FP32-bulk form: the same tables in FP32, in groups of four entries so
+    // that a lane reads 16 bytes (transformed areas folded into P)
+    const uint32_t* nb4;  // [tiles][4][ceil((M-1)/4)][8][4]
+    const float* P4;      // [tiles][4][ceil((M-1)(K-1)/4)][8][4], entry j*(K-1)+k
+    const float* phi4;    // [tiles][ceil(3 n_q (K-1)/4)][8][4], entry (face*n_q+q)*(K-1)+k
     double oi[KR_MAX * KR_MAX];   // oscillation indicator without dof 0, row-major (K-1)^2
     double oi2[KR_MAX * KR_MAX];  // same, upper triangle with doubled off-diagonals (fast form)
     float oi2f[KR_MAX * KR_MAX];  // oi2 in FP32 (FP32-bulk form)
@@ -71,11 +77,13 @@ struct UpdateArgs {
     const int4* gat;        // per cell up to 4 (face*2 + negate) in the reference's summation order, -1 = none
     const double* G;
     const double* vol;
+    const double* ivol;     // 1 / volume (fast forms)
     const double* dt;       // device scalar
     double* U;              // stage-1 base; final state after stage 3
     double* Ut;             // stage state
     double* W;              // running sum U + dt/6 k1 + dt/6 k2
     double* prim;
+    double* snd;            // sound speed per cell, written with prim
     double* rhs;            // residual output (stage 0 only)
     unsigned* flags;
 };
@@ -86,8 +94,10 @@ struct SpecArgs {
     const int2* lr;
     const double2* nrm;
     const double* dxn;      // |s . n| with the reference's boundary rule, precomputed
+    const double* idxn;     // 1 / dxn (fast forms)
     const double* U;
     const double* prim;
+    const double* snd;      // sound speed per cell
     double* rho_cell;
     unsigned long long* rmax_bits;
     double gamma;
@@ -117,8 +127,9 @@ cudaError_t launch_flux(const FluxArgs& a, const float* fv, const GasParams& g, 
 }  // namespace f32
 // kernels.cu
 cudaError_t launch_first_order(int n_faces, const int2* lr, const double* U, double* fv, cudaStream_t s);
-cudaError_t launch_update(const UpdateArgs& a, const GasParams& g, int stage, cudaStream_t s);
-cudaError_t launch_spectral(const SpecArgs& a, cudaStream_t s);
+cudaError_t launch_update(const UpdateArgs& a, const GasParams& g, int stage, bool fast, cudaStream_t s);
+cudaError_t launch_spectral(const SpecArgs& a, bool fast, cudaStream_t s);
+cudaError_t launch_sound(int n, double gamma, const double* U, const double* prim, double* snd, cudaStream_t s);
 cudaError_t launch_dt(const unsigned long long* rmax_bits, double cfl, double* dt, double* t, unsigned* flags,
                       cudaStream_t s);
 cudaError_t launch_set_scalar(double* dst, double value, cudaStream_t s);

@@ -3,8 +3,8 @@
 // Arithmetic split (everything else stays FP64):
 //  * FP32: TENO coefficients, smoothness indicators, stencil selection, face
 //    evaluation, face states, primitive recovery, Riemann flux;
-//  * FP64: the coefficient tables, transformed areas and face shapes in HBM
-//    (converted to FP32 as they are loaded), geometry (normals, areas,
+//  * FP64: the table build (least squares, face shapes; the tables are
+//    rounded to FP32 once, on upload), geometry (normals, areas,
 //    volumes), the conserved state and its accumulation across RK stages
 //    (the FP64 update kernel), and primitive recovery near vacuum: when the
 //    internal energy is under 1e-3 of the total the face state is recovered
@@ -20,10 +20,10 @@ namespace mgpu {
 namespace f32 {
 namespace {
 
-// FP64 -> FP32 on the integer pipe.  On GB300 the conversion instruction
-// (F2F) issues on the FP64 unit at FP64 rate (~2 per clock per SM), which
-// made table conversion the bound of this kernel; a funnel shift, a rebias
-// and two range guards do the same on the integer pipe.  Rounds toward zero
+// FP64 -> FP32 on the integer pipe, for the state gathered from the FP64
+// stage arrays.  On GB300 the conversion instruction (F2F) issues on the
+// FP64 unit at FP64 rate (~2 per clock per SM); a funnel shift, a rebias and
+// two range guards do the same on the integer pipe.  Rounds toward zero
 // (relative error < 2^-23); magnitudes below FP32's normal range become a
 // signed zero, those above become infinity, NaN stays NaN.
 __device__ __forceinline__ float f(double x) {
@@ -41,6 +41,7 @@ template <int K, int M, int NQ>
 __global__ void __launch_bounds__(128) teno32_kernel(const TenoArgs a, const double* __restrict__ U,
                                                      float* __restrict__ fv, uint8_t* __restrict__ masks) {
     constexpr int KR = K - 1, MR = M - 1, NF = 3, S = 4;
+    constexpr int GJ = (MR + 3) / 4, GP = (MR * KR + 3) / 4, GF = (NF * NQ * KR + 3) / 4;
     const int gt = blockIdx.x * blockDim.x + threadIdx.x;
     const int cell = gt >> 2, v = gt & 3;
     if (cell >= a.n_cells) return;
@@ -56,16 +57,28 @@ __global__ void __launch_bounds__(128) teno32_kernel(const TenoArgs a, const dou
         for (int k = 0; k < KR; ++k) coef[s][k] = 0.0f;
         x[s] = 0.0f;
         if (!((sm >> s) & 1u)) continue;
-        const size_t base = ((size_t)tile * S + s) * MR;
-        const uint32_t* nbp = a.nb + base * TILE + lane;
-        const double* arp = a.ar + base * TILE + lane;
-        const double* Pp = a.P + base * KR * TILE + lane;
-#pragma unroll 4
-        for (int j = 0; j < MR; ++j) {
-            const uint32_t nbj = __ldg(nbp + j * TILE);
-            const float b = f(__ldg(arp + j * TILE)) * (f(__ldg(U + (size_t)nbj * NC + v)) - uc);
+        // differences to the target cell's average over the stencil
+        const uint4* nbp = reinterpret_cast<const uint4*>(a.nb4) + ((size_t)(tile * S + s) * GJ) * TILE + lane;
+        float d[GJ * 4];
 #pragma unroll
-            for (int k = 0; k < KR; ++k) coef[s][k] = fmaf(f(__ldg(Pp + (j * KR + k) * TILE)), b, coef[s][k]);
+        for (int g = 0; g < GJ; ++g) {
+            const uint4 n = __ldg(nbp + g * TILE);
+            const uint32_t id[4] = {n.x, n.y, n.z, n.w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+                if (g * 4 + e < MR) d[g * 4 + e] = f(__ldg(U + (size_t)id[e] * NC + v)) - uc;
+        }
+        // coefficients = (P x areas) . d, accumulated over the stencil in order
+        const float4* Pp = reinterpret_cast<const float4*>(a.P4) + ((size_t)(tile * S + s) * GP) * TILE + lane;
+#pragma unroll
+        for (int g = 0; g < GP; ++g) {
+            const float4 p4 = __ldg(Pp + g * TILE);
+            const float pv[4] = {p4.x, p4.y, p4.z, p4.w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int fl = g * 4 + e;
+                if (fl < MR * KR) coef[s][fl % KR] = fmaf(pv[e], d[fl / KR], coef[s][fl % KR]);
+            }
         }
         float si = 0.0f;
 #pragma unroll
@@ -114,11 +127,27 @@ __global__ void __launch_bounds__(128) teno32_kernel(const TenoArgs a, const dou
         for (int s = 1; s < S; ++s) w[s] = ((mask >> s) & 1u) ? share : 0.0f;
     }
     if (masks) masks[(size_t)cell * NC + v] = (uint8_t)mask;
+    // blended coefficients
+    float c[KR];
 #pragma unroll
-    for (int s = 0; s < S; ++s)
+    for (int k = 0; k < KR; ++k) {
+        float t = 0.0f;
 #pragma unroll
-        for (int k = 0; k < KR; ++k) coef[s][k] *= w[s];
+        for (int s = 0; s < S; ++s) t = fmaf(coef[s][k], w[s], t);
+        c[k] = t;
+    }
 
+    // face values: shapes of all face points, then one dot product each
+    const float4* php = reinterpret_cast<const float4*>(a.phi4) + (size_t)tile * GF * TILE + lane;
+    float phi[GF * 4];
+#pragma unroll
+    for (int g = 0; g < GF; ++g) {
+        const float4 p4 = __ldg(php + g * TILE);
+        phi[g * 4] = p4.x;
+        phi[g * 4 + 1] = p4.y;
+        phi[g * 4 + 2] = p4.z;
+        phi[g * 4 + 3] = p4.w;
+    }
 #pragma unroll
     for (int fl = 0; fl < NF; ++fl) {
         const uint32_t slot = __ldg(a.cface + ((size_t)tile * NF + fl) * TILE + lane);
@@ -126,17 +155,9 @@ __global__ void __launch_bounds__(128) teno32_kernel(const TenoArgs a, const dou
         const unsigned side = slot & 1u;
 #pragma unroll
         for (int q = 0; q < NQ; ++q) {
-            const double* php = a.phi + (((size_t)tile * NF + fl) * NQ + q) * KR * TILE + lane;
-            float phi[KR];
-#pragma unroll
-            for (int k = 0; k < KR; ++k) phi[k] = f(__ldg(php + k * TILE));
             float out = uc;
 #pragma unroll
-            for (int s = 0; s < S; ++s) {
-                if (w[s] == 0.0f) continue;
-#pragma unroll
-                for (int k = 0; k < KR; ++k) out = fmaf(coef[s][k], phi[k], out);
-            }
+            for (int k = 0; k < KR; ++k) out = fmaf(c[k], phi[(fl * NQ + q) * KR + k], out);
             fv[((fi * NQ + q) * 2 + side) * NC + v] = out;
         }
     }

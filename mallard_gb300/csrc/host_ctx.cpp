@@ -146,11 +146,13 @@ struct mgpu_ctx {
     DevArray<unsigned long long> rmax;
     DevArray<int2> lr;
     DevArray<double2> nrm;
-    DevArray<double> area, dxn;
+    DevArray<double> area, dxn, idxn, ivol, snd;
     DevArray<int8_t> bcidx;
     DevArray<int4> gat, cfaces;
     DevArray<uint32_t> nb, cface;
     DevArray<double> ar, P, phi;
+    DevArray<uint32_t> nb4;
+    DevArray<float> P4, phi4;
     DevArray<uint8_t> smask, masks;
     DevArray<double> staging;      // caller-order rows for state transfers
     DevArray<uint32_t> perm_old;   // internal cell -> caller cell
@@ -204,6 +206,8 @@ struct mgpu_ctx {
 
     bool fast() const { return cfg.precision == MGPU_PREC_FP64_FAST; }
     bool single() const { return cfg.precision == MGPU_PREC_FP32; }
+    // reciprocal-based update and time step (every form but the exact one)
+    bool rcp() const { return cfg.precision != MGPU_PREC_FP64; }
 
     void reconstruct(const double* Uin, uint8_t* mask_out) {
         if (single()) {
@@ -246,11 +250,13 @@ struct mgpu_ctx {
         a.gat = gat.p;
         a.G = G.p;
         a.vol = vol.p;
+        a.ivol = ivol.p;
         a.dt = dt_ptr();
         a.U = U.p;
         a.Ut = Ut.p;
         a.W = W.p;
         a.prim = prim.p;
+        a.snd = snd.p;
         a.rhs = rhs.p;
         a.flags = flags.p;
         return a;
@@ -261,7 +267,7 @@ struct mgpu_ctx {
         reconstruct(in, nullptr);
         flux(in);
         UpdateArgs a = update_args();
-        timed(2, [&] { return launch_update(a, gas, k, stream); });
+        timed(2, [&] { return launch_update(a, gas, k, rcp(), stream); });
     }
 
     void spectral_and_dt(double cfl, bool accumulate_t) {
@@ -272,12 +278,14 @@ struct mgpu_ctx {
         s.lr = lr.p;
         s.nrm = nrm.p;
         s.dxn = dxn.p;
+        s.idxn = idxn.p;
         s.U = U.p;
         s.prim = prim.p;
+        s.snd = snd.p;
         s.rho_cell = rho_cell.p;
         s.rmax_bits = rmax.p;
         s.gamma = gas.gamma;
-        timed(3, [&] { return launch_spectral(s, stream); });
+        timed(3, [&] { return launch_spectral(s, rcp(), stream); });
         ck(launch_dt(rmax.p, cfl, dt_ptr(), accumulate_t ? t_ptr() : nullptr, flags.p, stream), "dt launch");
     }
 
@@ -457,9 +465,25 @@ void mgpu_ctx::build() {
         if (!((K == 10 && M == 20 && nq == 2) || (K == 6 && M == 12 && nq == 1) || (K == 3 && M == 6 && nq == 1)))
             throw Unsupported("GPU TENO kernels exist for p = 1..3 with stencil factor 2 and default face quadrature");
         const int KR = K - 1, MR = M - 1, S = 4, NF = 3;
-        std::vector<uint32_t> h_nb(tiles * S * MR * TILE, 0), h_cface(tiles * NF * TILE, 0);
-        std::vector<double> h_ar(tiles * S * MR * TILE, 0.0), h_P(tiles * S * MR * KR * TILE, 0.0),
-            h_phi(tiles * NF * nq * KR * TILE, 0.0);
+        // FP32-bulk form: FP32 tables only, in groups of four for 16-byte
+        // loads (flat index j*(K-1)+k for P, (face*n_q+q)*(K-1)+k for phi),
+        // with the transformed areas folded into P
+        const bool f32 = single();
+        const size_t GJ = (MR + 3) / 4, GP = ((size_t)MR * KR + 3) / 4, GF = ((size_t)NF * nq * KR + 3) / 4;
+        auto at4 = [](size_t group, size_t lane, size_t e) { return (group * TILE + lane) * 4 + e; };
+        std::vector<uint32_t> h_cface(tiles * NF * TILE, 0), h_nb, h_nb4;
+        std::vector<double> h_ar, h_P, h_phi;
+        std::vector<float> h_P4, h_phi4;
+        if (f32) {
+            h_nb4.assign(tiles * S * GJ * TILE * 4, 0);
+            h_P4.assign(tiles * S * GP * TILE * 4, 0.0f);
+            h_phi4.assign(tiles * GF * TILE * 4, 0.0f);
+        } else {
+            h_nb.assign(tiles * S * MR * TILE, 0);
+            h_ar.assign(tiles * S * MR * TILE, 0.0);
+            h_P.assign(tiles * S * MR * KR * TILE, 0.0);
+            h_phi.assign(tiles * NF * nq * KR * TILE, 0.0);
+        }
         std::vector<uint8_t> h_sm(N, 0);
         std::string err;
         int nthreads = 1;
@@ -489,6 +513,16 @@ void mgpu_ctx::build() {
                             if (pinv[(size_t)k * M] != 0.0) throw Unsupported("least-squares system took the full-rank branch");
                         sm |= (uint8_t)(1u << s);
                         for (int j = 1; j < M; ++j) {
+                            if (f32) {
+                                const size_t jj = j - 1;
+                                h_nb4[at4((tile * S + s) * GJ + jj / 4, lane, jj % 4)] = cell_new[t.stencils[so + j]];
+                                for (int k = 1; k < K; ++k) {
+                                    const size_t fl = jj * KR + (k - 1);
+                                    h_P4[at4((tile * S + s) * GP + fl / 4, lane, fl % 4)] =
+                                        (float)(pinv[(size_t)k * M + j] * ars[j]);
+                                }
+                                continue;
+                            }
                             const size_t b = ((tile * S + s) * MR + (j - 1)) * TILE + lane;
                             h_nb[b] = cell_new[t.stencils[so + j]];
                             h_ar[b] = ars[j];
@@ -524,7 +558,12 @@ void mgpu_ctx::build() {
                                         const double b = basis_2d(t.basis, t.pidx[2 * k], t.pidx[2 * k + 1], xq[0], xq[1]);
                                         const double shape = cfg.teno_variant == MGPU_TENO_CORRECTED ? b - t.ipt[k]
                                                                                                    : b + (t.ipt[k] / area0);
-                                        h_phi[(((tile * NF + fl) * nq + q) * KR + (k - 1)) * TILE + lane] = shape;
+                                        if (f32) {
+                                            const size_t e = ((size_t)fl * nq + q) * KR + (k - 1);
+                                            h_phi4[at4(tile * GF + e / 4, lane, e % 4)] = (float)shape;
+                                        } else {
+                                            h_phi[(((tile * NF + fl) * nq + q) * KR + (k - 1)) * TILE + lane] = shape;
+                                        }
                                     }
                                 }
                             }
@@ -546,23 +585,33 @@ void mgpu_ctx::build() {
                 teno.oi2[i * KR + l] = l < i ? 0.0 : (l == i ? 1.0 : 2.0) * t.oi[(size_t)(i + 1) * K + (l + 1)];
                 teno.oi2f[i * KR + l] = (float)teno.oi2[i * KR + l];
             }
-        nb.upload(h_nb);
-        ar.upload(h_ar);
-        P.upload(h_P);
-        phi.upload(h_phi);
+        if (f32) {
+            nb4.upload(h_nb4);
+            P4.upload(h_P4);
+            phi4.upload(h_phi4);
+        } else {
+            nb.upload(h_nb);
+            ar.upload(h_ar);
+            P.upload(h_P);
+            phi.upload(h_phi);
+        }
         cface.upload(h_cface);
         smask.upload(h_sm);
         teno.nb = nb.p;
         teno.ar = ar.p;
         teno.P = P.p;
         teno.phi = phi.p;
+        teno.nb4 = nb4.p;
+        teno.P4 = P4.p;
+        teno.phi4 = phi4.p;
         teno.cface = cface.p;
         teno.smask = smask.p;
         // compulsory bytes of one reconstruction launch: tables, shapes, face
         // slots, the state gathered once per cell, face states written
         double tb = 0;
-        for (uint32_t c = 0; c < N; ++c) tb += __builtin_popcount(h_sm[c]) * (double)MR * (4 + 8 + 8 * KR);
-        recon_bytes = tb + (double)N * (NF * nq * KR * 8 + NF * 4 + 1 + 32) + (double)N * NF * nq * 32;
+        const double per_row = f32 ? 4 + 4.0 * KR : 4 + 8 + 8.0 * KR, fw = f32 ? 4 : 8;
+        for (uint32_t c = 0; c < N; ++c) tb += __builtin_popcount(h_sm[c]) * (double)MR * per_row;
+        recon_bytes = tb + (double)N * (NF * nq * KR * fw + NF * 4 + 1 + 32) + (double)N * NF * nq * 4 * fw;
     } else {
         recon_bytes = (double)F_flux * (8 + 64) + (double)N * 32;
     }
@@ -579,6 +628,13 @@ void mgpu_ctx::build() {
     nrm.upload(h_nrm);
     area.upload(h_area);
     dxn.upload(h_dxn);
+    if (rcp()) {
+        std::vector<double> h_idxn(F_real), h_ivol(N);
+        for (uint32_t i = 0; i < F_real; ++i) h_idxn[i] = 1.0 / h_dxn[i];
+        for (uint32_t c = 0; c < N; ++c) h_ivol[c] = 1.0 / h_vol[c];
+        idxn.upload(h_idxn);
+        ivol.upload(h_ivol);
+    }
     bcidx.upload(h_bc);
     gat.upload(h_gat);
     cfaces.upload(h_cf);
@@ -588,6 +644,7 @@ void mgpu_ctx::build() {
     W.alloc((size_t)N * 4);
     rhs.alloc((size_t)N * 4);
     prim.alloc((size_t)N * 5);
+    snd.alloc(N);
     rho_cell.alloc(N);
     if (cfg.precision == MGPU_PREC_FP32) fv32.alloc((size_t)F_real * nq * 8);
     else fv.alloc((size_t)F_real * nq * 8);
@@ -733,6 +790,7 @@ int mgpu_create(const mgpu_mesh* mesh, const mgpu_config* cfg, mgpu_ctx** out) {
         ctx->gas.cv = cp_ / cfg->gamma;
         ctx->gas.p_min = cfg->p_min;
         ctx->gas.p_max = cfg->p_max;
+        ctx->gas.icv = 1.0 / ctx->gas.cv;
         ck(cudaSetDevice(cfg->device), "cudaSetDevice");
         ck(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking), "cudaStreamCreate");
         ctx->own_stream = true;
@@ -827,6 +885,7 @@ int mgpu_set_state(mgpu_ctx* ctx, const double* Uh, const double* primh) {
         } else {
             ck(launch_primitives_batch(ctx->gas, ctx->N, ctx->U.p, ctx->prim.p, ctx->stream), "primitives");
         }
+        ck(launch_sound((int)ctx->N, ctx->gas.gamma, ctx->U.p, ctx->prim.p, ctx->snd.p, ctx->stream), "sound speed");
         ck(cudaMemsetAsync(ctx->flags.p, 0, sizeof(unsigned), ctx->stream), "cudaMemsetAsync");
         ck(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
         return MGPU_OK;
@@ -886,7 +945,7 @@ int mgpu_calc_rhs(mgpu_ctx* ctx, const double* Uh, double* rhsh) {
         ctx->reconstruct(ctx->Ut.p, nullptr);
         ctx->flux(ctx->Ut.p);
         UpdateArgs a = ctx->update_args();
-        ck(launch_update(a, ctx->gas, 0, ctx->stream), "update");
+        ck(launch_update(a, ctx->gas, 0, ctx->rcp(), ctx->stream), "update");
         ctx->download_cells(ctx->rhs.p, rhsh, 4);
         return MGPU_OK;
     });

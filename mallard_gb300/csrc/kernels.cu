@@ -37,7 +37,30 @@ __global__ void __launch_bounds__(256) first_order_kernel(int n_faces, const int
 // time_integrator.cpp:135-163, solver.cpp:533-578)
 // ---------------------------------------------------------------------------
 
-template <int STAGE>
+// Primitive recovery of the fast forms: one reciprocal of the density (and a
+// precomputed 1/cv) instead of five divisions.
+__device__ __forceinline__ void primitives_rcp(const GasParams& g, const double* U, double* W) {
+    const double rho = U[0], ir = 1.0 / rho;
+    const double u0 = U[1] * ir, u1 = U[2] * ir;
+    const double E = U[3] * ir;
+    const double e = E - 0.5 * (u0 * u0 + u1 * u1);
+    const double p = fmax(g.p_min, fmin(g.p_max, (g.gamma - 1.0) * rho * e));
+    W[0] = u0;
+    W[1] = u1;
+    W[2] = p;
+    W[3] = e * g.icv;
+    W[4] = e + p * ir;
+}
+
+// Sound speed of a cell, as the spectral radius evaluates it per face
+// (solver.cpp:662-696); stored once per cell, bit for bit the same value.
+__device__ __forceinline__ double sound_speed(double gamma, double rho, const double* W) {
+    return sqrt(gamma * W[2] / rho);
+}
+
+// FAST: residual times a precomputed 1/volume and primitives_rcp (the
+// FP64-fast and FP32 forms); otherwise the reference's divisions.
+template <int STAGE, bool FAST>
 __global__ void __launch_bounds__(256) update_kernel(const UpdateArgs a, const GasParams g) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= a.n_cells) return;
@@ -58,9 +81,15 @@ __global__ void __launch_bounds__(256) update_kernel(const UpdateArgs a, const G
             for (int i = 0; i < 4; i++) r[i] = r[i] + x[i];
         }
     }
-    const double vol = a.vol[c];
+    if (FAST) {
+        const double iv = a.ivol[c];
 #pragma unroll
-    for (int i = 0; i < 4; i++) r[i] = r[i] / vol;
+        for (int i = 0; i < 4; i++) r[i] = r[i] * iv;
+    } else {
+        const double vol = a.vol[c];
+#pragma unroll
+        for (int i = 0; i < 4; i++) r[i] = r[i] / vol;
+    }
     double2* out2;
     if (STAGE == 0) {
         out2 = reinterpret_cast<double2*>(a.rhs + (size_t)c * 4);
@@ -115,10 +144,12 @@ __global__ void __launch_bounds__(256) update_kernel(const UpdateArgs a, const G
         Uo2[0] = make_double2(u[0], u[1]);
         Uo2[1] = make_double2(u[2], u[3]);
         double p[5];
-        primitives(g, u, p);
+        if (FAST) primitives_rcp(g, u, p);
+        else primitives(g, u, p);
         double* po = a.prim + (size_t)c * NPR;
 #pragma unroll
         for (int i = 0; i < NPR; i++) po[i] = p[i];
+        a.snd[c] = sound_speed(g.gamma, u[0], p);
         bool ok = true;
 #pragma unroll
         for (int i = 0; i < 4; i++) ok = ok && isfinite(u[i]);
@@ -130,6 +161,17 @@ __global__ void __launch_bounds__(256) update_kernel(const UpdateArgs a, const G
 // Spectral radius and dt (solver.cpp:580-742)
 // ---------------------------------------------------------------------------
 
+// Per-cell sound speed from the state and primitives (after set_state).
+__global__ void __launch_bounds__(256) sound_kernel(int n, double gamma, const double* __restrict__ U,
+                                                    const double* __restrict__ prim, double* __restrict__ snd) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    snd[c] = sound_speed(gamma, U[(size_t)c * NC], prim + (size_t)c * NPR);
+}
+
+// The sound speeds come from the per-cell array written with the
+// primitives.  FAST multiplies by precomputed 1/dxn instead of dividing.
+template <bool FAST>
 __global__ void __launch_bounds__(256) spectral_kernel(const SpecArgs a) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     double tot = 0.0;
@@ -146,19 +188,25 @@ __global__ void __launch_bounds__(256) spectral_kernel(const SpecArgs a) {
             const int2 lr = a.lr[f];
             const int L = lr.x, R = lr.y < 0 ? lr.x : lr.y;
             const double2 n = a.nrm[f];
-            const double dxn = a.dxn[f];
-            const double rl = a.U[(size_t)L * NC], rr = a.U[(size_t)R * NC];
             const double* wl = a.prim + (size_t)L * NPR;
             const double* wr = a.prim + (size_t)R * NPR;
-            const double al = sqrt(a.gamma * wl[2] / rl), ar = sqrt(a.gamma * wr[2] / rr);
+            const double al = a.snd[L], ar = a.snd[R];
             const double af = 0.5 * (al + ar);
             const double uf0 = 0.5 * (wl[0] + wr[0]), uf1 = 0.5 * (wl[1] + wr[1]);
             const double un = fabs(uf0 * n.x + uf1 * n.y);
-            conv += un / dxn;
-            const double t = af / dxn;
-            acou += t * t;
+            if (FAST) {
+                const double idx = a.idxn[f];
+                conv += un * idx;
+                const double t = af * idx;
+                acou += t * t;
+            } else {
+                const double dxn = a.dxn[f];
+                conv += un / dxn;
+                const double t = af / dxn;
+                acou += t * t;
+            }
         }
-        const double geom = 3.0 / nf;
+        const double geom = nf == 3 ? 1.0 : 0.75;  // 3.0 / nf, exactly
         conv *= 1.37 * geom;
         acou = 1.37 * sqrt(geom * acou);
         tot = conv + acou;
@@ -261,23 +309,36 @@ cudaError_t launch_first_order(int n_faces, const int2* lr, const double* U, dou
     return cudaGetLastError();
 }
 
-cudaError_t launch_update(const UpdateArgs& a, const GasParams& g, int stage, cudaStream_t s) {
-    const unsigned blocks = (unsigned)((a.n_cells + 255) / 256);
-    if (blocks == 0) return cudaSuccess;
+template <bool FAST>
+cudaError_t update_go(const UpdateArgs& a, const GasParams& g, int stage, unsigned blocks, cudaStream_t s) {
     switch (stage) {
-        case 0: update_kernel<0><<<blocks, 256, 0, s>>>(a, g); break;
-        case 1: update_kernel<1><<<blocks, 256, 0, s>>>(a, g); break;
-        case 2: update_kernel<2><<<blocks, 256, 0, s>>>(a, g); break;
-        case 3: update_kernel<3><<<blocks, 256, 0, s>>>(a, g); break;
+        case 0: update_kernel<0, FAST><<<blocks, 256, 0, s>>>(a, g); break;
+        case 1: update_kernel<1, FAST><<<blocks, 256, 0, s>>>(a, g); break;
+        case 2: update_kernel<2, FAST><<<blocks, 256, 0, s>>>(a, g); break;
+        case 3: update_kernel<3, FAST><<<blocks, 256, 0, s>>>(a, g); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
 }
 
-cudaError_t launch_spectral(const SpecArgs& a, cudaStream_t s) {
+cudaError_t launch_update(const UpdateArgs& a, const GasParams& g, int stage, bool fast, cudaStream_t s) {
     const unsigned blocks = (unsigned)((a.n_cells + 255) / 256);
     if (blocks == 0) return cudaSuccess;
-    spectral_kernel<<<blocks, 256, 0, s>>>(a);
+    return fast ? update_go<true>(a, g, stage, blocks, s) : update_go<false>(a, g, stage, blocks, s);
+}
+
+cudaError_t launch_spectral(const SpecArgs& a, bool fast, cudaStream_t s) {
+    const unsigned blocks = (unsigned)((a.n_cells + 255) / 256);
+    if (blocks == 0) return cudaSuccess;
+    if (fast) spectral_kernel<true><<<blocks, 256, 0, s>>>(a);
+    else spectral_kernel<false><<<blocks, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sound(int n, double gamma, const double* U, const double* prim, double* snd, cudaStream_t s) {
+    const unsigned blocks = (unsigned)((n + 255) / 256);
+    if (blocks == 0) return cudaSuccess;
+    sound_kernel<<<blocks, 256, 0, s>>>(n, gamma, U, prim, snd);
     return cudaGetLastError();
 }
 
