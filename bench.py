@@ -41,6 +41,7 @@ UNIT = "Mcell-updates/s"
 SEED = 20261203
 CFL = 0.5
 CPU_SAMPLE_N = 256
+SEL_THRESHOLD = 0.98
 
 
 def parse():
@@ -53,7 +54,7 @@ def parse():
     ap.add_argument("--variant", default="corrected", choices=["reference", "corrected"])
     ap.add_argument("--precision", default="fp64_fast", choices=["fp64", "fp64_fast"],
                     help="fp64: the reference's rounding (bit-faithful); fp64_fast: FMA-contracted FP64")
-    ap.add_argument("--forms", default="fp64,fp32",
+    ap.add_argument("--forms", default="fp64,fp32,fp32_learned",
                     help="other precision forms to time on the same workload (comma list, '' for none)")
     ap.add_argument("--cpu-sample-n", type=int, default=CPU_SAMPLE_N)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -197,7 +198,21 @@ def teno_flops_per_cell(precision, K=10, M=20, nq=2, stencils=4):
     return 4 * per_var
 
 
-def time_form(m, args, precision, U0, W0, device, U_ref):
+def load_selector(device):
+    """The trained selector weights shipped with the package; trains a quick
+    one on the GPU when they are missing."""
+    from mallard_gb300.selector import Selector, default_weights_path
+    path = default_weights_path()
+    if path.exists():
+        sel = Selector(device=device)
+        sel.load(path)
+        return sel, str(path.relative_to(ROOT))
+    from mallard_gb300.train_selector import train
+    sel, _ = train(None, quick=True, log=lambda *a: print(*a, file=sys.stderr))
+    return sel, "trained at startup (quick)"
+
+
+def time_form(m, args, precision, U0, W0, device, U_ref, selector=None):
     """Rate of another precision form on the same mesh and state, and its
     error against the headline form after the same W + K steps."""
     import numpy as np
@@ -207,6 +222,8 @@ def time_form(m, args, precision, U0, W0, device, U_ref):
     s = mg.Solver(m, face_reconstruction="TENO", basis_type="legendre", basis_order=3, riemann_solver="HLLC",
                   boundaries=[{"name": z, "type": "extrapolation"} for z in ("right", "top", "left", "bottom")],
                   teno_variant=args.variant, reorder=True, device=device, precision=precision)
+    if selector is not None:
+        s.attach_selector(selector[0], threshold=SEL_THRESHOLD)
     stream = torch.cuda.Stream()
     s.set_stream(stream.cuda_stream)
     s.set_state(U0, W0)
@@ -220,6 +237,7 @@ def time_form(m, args, precision, U0, W0, device, U_ref):
     e1.synchronize()
     ms = e0.elapsed_time(e1)
     U, _ = s.get_state()
+    stats = s.selector_stats() if selector is not None else None
     s.set_state(U0, W0)
     s.launch(CFL, args.warmup)
     s.kernel_timing(True)
@@ -229,7 +247,15 @@ def time_form(m, args, precision, U0, W0, device, U_ref):
     vol = m.cell_volume
     out = {"value": m.n_cells * args.steps / (ms * 1e-3) / 1e6, "ms_per_step": ms / args.steps,
            "finite": bool(np.isfinite(U).all()),
-           "kernel_ms_per_launch": {k: v[0] / max(v[1], 1) for k, v in kt.items()}}
+           "kernel_ms_per_launch": {k: v[0] / max(v[1], 1) for k, v in kt.items() if v[1]}}
+    if stats is not None:
+        out["selector"] = {"weights": selector[1], "central_threshold": SEL_THRESHOLD,
+                           "directional_predictions": "not trusted (full TENO)",
+                           "predict": "once per step, from the step's initial state",
+                           "confident_cells": stats["confident_cells"] / stats["cells"],
+                           "confident_variables": stats["confident_variables"] / (4 * stats["cells"]),
+                           "stencils_evaluated_frac": stats["stencils_evaluated"] / stats["stencils_full"],
+                           "error_flag": stats["error"]}
     if np.isfinite(U_ref).all() and out["finite"]:
         d = np.abs(U[:, 0] - U_ref[:, 0])
         out["density_l1_rel_err"] = float(np.sum(vol * d) / np.sum(vol * np.abs(U_ref[:, 0])))
@@ -351,7 +377,10 @@ def run_ours(args):
     # ---- other forms on the same workload: rate and error against the FP64 state
     forms = {}
     for prec in [p for p in args.forms.split(",") if p and p != args.precision]:
-        forms[prec] = time_form(m, args, prec, U0, W0, local, Uend)
+        if prec == "fp32_learned":
+            forms[prec] = time_form(m, args, "fp32", U0, W0, local, Uend, selector=load_selector(local))
+        else:
+            forms[prec] = time_form(m, args, prec, U0, W0, local, Uend)
     forms[args.precision] = {"value": value, "ms_per_step": ms_max / args.steps, "finite": finite}
 
     cpu = None

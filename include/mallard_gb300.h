@@ -219,11 +219,76 @@ int mgpu_status(mgpu_ctx* ctx, uint32_t* flags);
  * array: calls that overlap on the GPU race. */
 int mgpu_calc_dt_noalloc(mgpu_ctx* ctx, double cfl, double* dt_device, double* spectral_radius_device);
 
+/* ---- learned TENO stencil selector ------------------------------------
+ * No counterpart in the reference.  A 96-64-64-32 MLP (GELU) predicts, per
+ * cell and conserved variable, the stencil decision of the corrected TENO
+ * form (face_reconstruction.cpp:939-981): class 0 = central stencil only,
+ * class m = 1..7 = the directional stencils whose bit is set in m.  Inputs
+ * per variable: the 19 central-stencil differences divided by their range,
+ * the scaled log10 of that range, the three directional ranges relative to
+ * it, and a zero (24 x 4 = 96).  Parameters are packed FP32: W1 [96][64],
+ * b1 [64], W2 [64][64], b2 [64], W3 [64][32], b3 [32] (MGPU_SEL_PARAMS).
+ * Training runs on the GPU (FP32 kernels, softmax cross-entropy per head,
+ * Adam); inference runs on the tcgen05 tensor cores in BF16 with FP32
+ * accumulation.  Attached to an FP32-form context (p = 3) it replaces the
+ * smoothness indicators of every variable whose predicted class reaches
+ * the probability threshold, and the cell evaluates only the stencils its
+ * variables need; a variable below the threshold runs full TENO. */
+#define MGPU_SEL_INPUTS 96
+#define MGPU_SEL_OUTPUTS 32
+#define MGPU_SEL_CLASSES 8
+#define MGPU_SEL_PARAMS 12448
+typedef struct mgpu_selector mgpu_selector;
+/* Seeded uniform(+-1/sqrt(fan_in)) weights, zero biases. */
+int mgpu_selector_create(int device, uint64_t seed, mgpu_selector** out);
+void mgpu_selector_destroy(mgpu_selector* sel);
+int mgpu_selector_get_params(mgpu_selector* sel, float* params);
+/* Also resets the Adam moments. */
+int mgpu_selector_set_params(mgpu_selector* sel, const float* params);
+/* The training set lives on the device: rows X [n][96] FP32 and labels
+ * Y [n][4] (class per variable). */
+int mgpu_selector_dataset_size(const mgpu_selector* sel, uint64_t* n);
+int mgpu_selector_clear(mgpu_selector* sel);
+int mgpu_selector_add_samples(mgpu_selector* sel, const float* X, const uint8_t* Y, uint64_t n);
+int mgpu_selector_get_samples(mgpu_selector* sel, uint64_t first, uint64_t n, float* X, uint8_t* Y);
+/* Appends the current state of an FP64 or FP64-fast context (corrected TENO,
+ * p = 3): every cell where some variable leaves the central stencil, and
+ * each all-central cell with probability keep_central (seeded). */
+int mgpu_selector_harvest(mgpu_selector* sel, mgpu_ctx* ctx, double keep_central, uint64_t seed, uint64_t* added);
+/* One forward + backward pass over host rows: gradient of the mean
+ * cross-entropy (over rows and heads) in the packed parameter layout. */
+int mgpu_selector_gradient(mgpu_selector* sel, const float* X, const uint8_t* Y, uint32_t n, float* grad,
+                           float* loss);
+/* Minibatch Adam (beta 0.9/0.999, eps 1e-8) over the dataset, shuffled per
+ * epoch with seed + epoch; epoch_loss[epochs] receives each epoch's mean
+ * loss (may be NULL). */
+int mgpu_selector_train(mgpu_selector* sel, uint32_t epochs, uint32_t batch, float lr, uint64_t seed,
+                        float* epoch_loss);
+/* Tensor-core inference over host rows: logits [n][32] and predictions
+ * [n][4] (predicted TENO mask, bit 7 set when the predicted class has at
+ * least probability thr_central if it is the central class, thr_directional
+ * otherwise; a threshold outside (0, 1] is never reached); either output
+ * may be NULL.  MGPU_ERR_TIMEOUT when a bounded wait in the kernel ran out. */
+int mgpu_selector_infer(mgpu_selector* sel, const float* X, uint32_t n, float thr_central, float thr_directional,
+                        float* logits, uint8_t* pred);
+/* Attaches a copy of the selector's current weights to an FP32-form context
+ * (thr_central in (0, 1]; thr_directional above 1 trusts no directional
+ * prediction); sel NULL or thr_central <= 0 detaches. */
+int mgpu_set_selector(mgpu_ctx* ctx, mgpu_selector* sel, float thr_central, float thr_directional);
+/* By default the selector predicts once per time step, from the step's
+ * initial state, and the three SSPRK3 stages use those predictions;
+ * every_stage != 0 predicts at every stage instead. */
+int mgpu_set_selector_every_stage(mgpu_ctx* ctx, int every_stage);
+/* Counts over the last reconstruction with the selector: [0] cells,
+ * [1] cells with every variable confident, [2] confident variables,
+ * [3] stencils evaluated, [4] stencils full TENO evaluates, [5] error flag. */
+int mgpu_selector_stats(mgpu_ctx* ctx, uint64_t* counts);
+
 /* Diagnostics for measurement.  Kernel timing brackets every launch of the
- * reconstruction, flux, update and CFL kernels with CUDA events on the
- * launching stream; mgpu_kernel_times returns, per kernel class
- * (0 recon, 1 flux, 2 update, 3 cfl), the summed milliseconds and launch
- * counts since the last reset. */
+ * reconstruction, flux, update, CFL and selector kernels with CUDA events on
+ * the launching stream; mgpu_kernel_times returns, per kernel class
+ * (0 recon, 1 flux, 2 update, 3 cfl, 4 selector), the summed milliseconds
+ * and launch counts since the last reset (arrays of 5). */
 int mgpu_enable_kernel_timing(mgpu_ctx* ctx, int enable);
 int mgpu_kernel_times(mgpu_ctx* ctx, double* ms, uint32_t* launches);
 /* Algorithmic (compulsory) bytes one reconstruction launch and one full

@@ -115,6 +115,21 @@ def lib():
         "mgpu_riemann_flux_batch": (i32, [i32, u32] + [vp] * 12),
         "mgpu_primitives_batch": (i32, [f64, f64, f64, f64, f64, f64, u32, vp, vp]),
         "mgpu_probe_fp64_gflops": (i32, [i32, P(f64)]),
+        "mgpu_selector_create": (i32, [i32, u64, P(vp)]),
+        "mgpu_selector_destroy": (None, [vp]),
+        "mgpu_selector_get_params": (i32, [vp, vp]),
+        "mgpu_selector_set_params": (i32, [vp, vp]),
+        "mgpu_selector_dataset_size": (i32, [vp, P(u64)]),
+        "mgpu_selector_clear": (i32, [vp]),
+        "mgpu_selector_add_samples": (i32, [vp, vp, vp, u64]),
+        "mgpu_selector_get_samples": (i32, [vp, u64, u64, vp, vp]),
+        "mgpu_selector_harvest": (i32, [vp, vp, f64, u64, P(u64)]),
+        "mgpu_selector_gradient": (i32, [vp, vp, vp, u32, vp, P(C.c_float)]),
+        "mgpu_selector_train": (i32, [vp, u32, u32, C.c_float, u64, vp]),
+        "mgpu_selector_infer": (i32, [vp, vp, u32, C.c_float, C.c_float, vp, vp]),
+        "mgpu_set_selector": (i32, [vp, vp, C.c_float, C.c_float]),
+        "mgpu_selector_stats": (i32, [vp, vp]),
+        "mgpu_set_selector_every_stage": (i32, [vp, i32]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

@@ -122,6 +122,9 @@ MGPU_DECLARE_TENO_FLUX
 namespace f32 {
 cudaError_t launch_teno(const TenoArgs& a, int K, int M, int nq, const double* U, float* fv, uint8_t* masks,
                         cudaStream_t s);
+// with the learned selector's predictions (p = 3 only)
+cudaError_t launch_teno_selected(const TenoArgs& a, int K, int M, int nq, const double* U, const uint8_t* pred,
+                                 float* fv, uint8_t* masks, cudaStream_t s);
 cudaError_t launch_flux(const FluxArgs& a, const float* fv, const GasParams& g, const BcTable& bct, int rsolver,
                         int nq, cudaStream_t s);
 }  // namespace f32

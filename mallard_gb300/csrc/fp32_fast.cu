@@ -37,17 +37,36 @@ __device__ __forceinline__ float f(double x) {
     return __uint_as_float(r);
 }
 
-template <int K, int M, int NQ>
+// SEL: per (cell, variable) predictions of the learned selector (pred:
+// predicted mask, bit 7 = confident).  A confident variable takes the
+// predicted stencils with equal weights and computes no smoothness
+// indicator; a cell evaluates only the stencils that one of its variables
+// needs, all of them as soon as one variable is not confident.
+template <int K, int M, int NQ, bool SEL>
 __global__ void __launch_bounds__(128) teno32_kernel(const TenoArgs a, const double* __restrict__ U,
-                                                     float* __restrict__ fv, uint8_t* __restrict__ masks) {
+                                                     float* __restrict__ fv, uint8_t* __restrict__ masks,
+                                                     const uint8_t* __restrict__ pred) {
     constexpr int KR = K - 1, MR = M - 1, NF = 3, S = 4;
     constexpr int GJ = (MR + 3) / 4, GP = (MR * KR + 3) / 4, GF = (NF * NQ * KR + 3) / 4;
     const int gt = blockIdx.x * blockDim.x + threadIdx.x;
     const int cell = gt >> 2, v = gt & 3;
+    // lanes of cells that exist (the four lanes of a cell share its fate)
+    const unsigned live = __ballot_sync(0xffffffffu, cell < a.n_cells);
     if (cell >= a.n_cells) return;
     const int tile = cell >> 3, lane = cell & 7;
     const float uc = f(U[(size_t)cell * NC + v]);
     const unsigned sm = a.smask[cell];
+    unsigned need = sm, pm = 0;
+    bool conf = false;
+    if (SEL) {
+        const unsigned p = pred[(size_t)cell * NC + v];
+        pm = p & sm & 0xFu;
+        conf = (p & 0x80u) && pm;
+        unsigned my = conf ? pm : sm;
+        my |= __shfl_xor_sync(live, my, 1);
+        my |= __shfl_xor_sync(live, my, 2);
+        need = my;
+    }
 
     float coef[S][KR];
     float x[S];
@@ -56,7 +75,7 @@ __global__ void __launch_bounds__(128) teno32_kernel(const TenoArgs a, const dou
 #pragma unroll
         for (int k = 0; k < KR; ++k) coef[s][k] = 0.0f;
         x[s] = 0.0f;
-        if (!((sm >> s) & 1u)) continue;
+        if (!((need >> s) & 1u)) continue;
         // differences to the target cell's average over the stencil
         const uint4* nbp = reinterpret_cast<const uint4*>(a.nb4) + ((size_t)(tile * S + s) * GJ) * TILE + lane;
         float d[GJ * 4];
@@ -80,6 +99,7 @@ __global__ void __launch_bounds__(128) teno32_kernel(const TenoArgs a, const dou
                 if (fl < MR * KR) coef[s][fl % KR] = fmaf(pv[e], d[fl / KR], coef[s][fl % KR]);
             }
         }
+        if (SEL && conf) continue;
         float si = 0.0f;
 #pragma unroll
         for (int i = 0; i < KR; ++i) {
@@ -91,6 +111,18 @@ __global__ void __launch_bounds__(128) teno32_kernel(const TenoArgs a, const dou
         x[s] = si + 1.0e-12f;
     }
 
+    unsigned mask = 0;
+    float w[S] = {0.0f, 0.0f, 0.0f, 0.0f};
+    if (SEL && conf) {
+        mask = pm;
+        if (pm & 1u) {
+            w[0] = 1.0f;
+        } else {
+            const float share = 1.0f / (float)__popc(pm);
+#pragma unroll
+            for (int s = 1; s < S; ++s) w[s] = ((pm >> s) & 1u) ? share : 0.0f;
+        }
+    } else {
     // stencil selection in ratio form
     float rx[S];
 #pragma unroll
@@ -101,8 +133,6 @@ __global__ void __launch_bounds__(128) teno32_kernel(const TenoArgs a, const dou
         const float q = x[0] * rx[d], q2 = q * q;
         r = fmaf(q2 * q2, q2, r);
     }
-    unsigned mask = 0;
-    float w[S] = {0.0f, 0.0f, 0.0f, 0.0f};
     if (r < 9999999.0f) {  // w0 / (w0 + sum_d w_d) > 1e-7
         mask = 1;
         w[0] = 1.0f;
@@ -125,6 +155,7 @@ __global__ void __launch_bounds__(128) teno32_kernel(const TenoArgs a, const dou
         const float share = npass ? 1.0f / (float)npass : 0.0f;
 #pragma unroll
         for (int s = 1; s < S; ++s) w[s] = ((mask >> s) & 1u) ? share : 0.0f;
+    }
     }
     if (masks) masks[(size_t)cell * NC + v] = (uint8_t)mask;
     // blended coefficients
@@ -279,11 +310,12 @@ cudaError_t flux_nq(const FluxArgs& a, const float* fv, const GasParams& g, cons
     return cudaErrorInvalidValue;
 }
 
-template <int K, int M, int NQ>
-cudaError_t teno_go(const TenoArgs& a, const double* U, float* fv, uint8_t* masks, cudaStream_t s) {
+template <int K, int M, int NQ, bool SEL>
+cudaError_t teno_go(const TenoArgs& a, const double* U, float* fv, uint8_t* masks, const uint8_t* pred,
+                    cudaStream_t s) {
     const long long threads = (long long)a.n_cells * 4;
     const unsigned blocks = (unsigned)((threads + 127) / 128);
-    if (blocks) teno32_kernel<K, M, NQ><<<blocks, 128, 0, s>>>(a, U, fv, masks);
+    if (blocks) teno32_kernel<K, M, NQ, SEL><<<blocks, 128, 0, s>>>(a, U, fv, masks, pred);
     return cudaGetLastError();
 }
 
@@ -291,9 +323,15 @@ cudaError_t teno_go(const TenoArgs& a, const double* U, float* fv, uint8_t* mask
 
 cudaError_t launch_teno(const TenoArgs& a, int K, int M, int nq, const double* U, float* fv, uint8_t* masks,
                         cudaStream_t s) {
-    if (K == 10 && M == 20 && nq == 2) return teno_go<10, 20, 2>(a, U, fv, masks, s);
-    if (K == 6 && M == 12 && nq == 1) return teno_go<6, 12, 1>(a, U, fv, masks, s);
-    if (K == 3 && M == 6 && nq == 1) return teno_go<3, 6, 1>(a, U, fv, masks, s);
+    if (K == 10 && M == 20 && nq == 2) return teno_go<10, 20, 2, false>(a, U, fv, masks, nullptr, s);
+    if (K == 6 && M == 12 && nq == 1) return teno_go<6, 12, 1, false>(a, U, fv, masks, nullptr, s);
+    if (K == 3 && M == 6 && nq == 1) return teno_go<3, 6, 1, false>(a, U, fv, masks, nullptr, s);
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_teno_selected(const TenoArgs& a, int K, int M, int nq, const double* U, const uint8_t* pred,
+                                 float* fv, uint8_t* masks, cudaStream_t s) {
+    if (K == 10 && M == 20 && nq == 2) return teno_go<10, 20, 2, true>(a, U, fv, masks, pred, s);
     return cudaErrorInvalidValue;
 }
 

@@ -23,54 +23,12 @@
 #include <omp.h>
 #endif
 
-#include "device.h"
-#include "host.h"
+#include "host_ctx.h"
 
 namespace mgpu {
 
 namespace {
 thread_local std::string g_error;
-
-struct CudaFail : std::runtime_error {
-    using std::runtime_error::runtime_error;
-};
-struct ArgFail : std::runtime_error {
-    using std::runtime_error::runtime_error;
-};
-struct Unsupported : std::runtime_error {
-    using std::runtime_error::runtime_error;
-};
-
-void ck(cudaError_t e, const char* what) {
-    if (e != cudaSuccess) throw CudaFail(std::string(what) + ": " + cudaGetErrorString(e));
-}
-
-template <class T>
-struct DevArray {
-    T* p = nullptr;
-    size_t n = 0;
-    DevArray() = default;
-    DevArray(const DevArray&) = delete;
-    DevArray& operator=(const DevArray&) = delete;
-    ~DevArray() { release(); }
-    void release() {
-        if (p) cudaFree(p);
-        p = nullptr;
-        n = 0;
-    }
-    void alloc(size_t count) {
-        release();
-        if (count == 0) count = 1;
-        ck(cudaMalloc(&p, count * sizeof(T)), "cudaMalloc");
-        n = count;
-        ck(cudaMemset(p, 0, count * sizeof(T)), "cudaMemset");
-    }
-    void upload(const std::vector<T>& v) {
-        alloc(v.size());
-        if (!v.empty()) ck(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), "cudaMemcpy H2D");
-    }
-    size_t bytes() const { return n * sizeof(T); }
-};
 
 // reverse Cuthill-McKee over the face-neighbour graph; returns old_of_new
 std::vector<uint32_t> rcm_order(uint32_t n, const std::vector<std::vector<uint32_t>>& adj) {
@@ -105,12 +63,6 @@ std::vector<uint32_t> rcm_order(uint32_t n, const std::vector<std::vector<uint32
     return order;
 }
 
-struct BcHost {
-    uint32_t zone;
-    int type;
-    double data[6];
-};
-
 }  // namespace
 
 void set_error(const std::string& msg) { g_error = msg; }
@@ -119,201 +71,6 @@ void set_error(const std::string& msg) { g_error = msg; }
 
 using namespace mgpu;
 
-struct mgpu_ctx {
-    mgpu_config cfg{};
-    HostMesh mesh;
-    std::vector<BcHost> bcs;
-    bool finalized = false;
-    GasParams gas{};
-    BcTable bct{};
-    int nq = 1, K = 0, M = 0;
-    double qw[4] = {0, 0, 0, 0};
-
-    cudaStream_t stream = nullptr;
-    bool own_stream = false;
-
-    // numbering: internal <-> caller
-    uint32_t N = 0;
-    std::vector<uint32_t> cell_new, cell_old;
-    uint32_t F_flux = 0, F_real = 0;
-    std::vector<int32_t> face_new;
-    std::vector<uint32_t> face_old;
-
-    // device state and work arrays
-    DevArray<double> U, Ut, W, prim, vol, fv, G, rho_cell, rhs, scal;  // scal: dt, t
-    DevArray<float> fv32;  // face states of the FP32-bulk form
-    DevArray<unsigned> flags;
-    DevArray<unsigned long long> rmax;
-    DevArray<int2> lr;
-    DevArray<double2> nrm;
-    DevArray<double> area, dxn, idxn, ivol, snd;
-    DevArray<int8_t> bcidx;
-    DevArray<int4> gat, cfaces;
-    DevArray<uint32_t> nb, cface;
-    DevArray<double> ar, P, phi;
-    DevArray<uint32_t> nb4;
-    DevArray<float> P4, phi4;
-    DevArray<uint8_t> smask, masks;
-    DevArray<double> staging;      // caller-order rows for state transfers
-    DevArray<uint32_t> perm_old;   // internal cell -> caller cell
-    TenoArgs teno{};
-
-    // CUDA graph of one CFL step, keyed by cfl
-    cudaGraphExec_t step_exec = nullptr;
-    double step_cfl = -1.0;
-
-    // per-launch timing
-    bool timing = false;
-    struct Mark {
-        int cls;
-        cudaEvent_t a, b;
-    };
-    std::vector<Mark> marks;
-    size_t marks_used = 0;
-    double recon_bytes = 0, stage_bytes = 0;
-
-    ~mgpu_ctx() {
-        if (step_exec) cudaGraphExecDestroy(step_exec);
-        for (auto& m : marks) {
-            cudaEventDestroy(m.a);
-            cudaEventDestroy(m.b);
-        }
-        if (own_stream && stream) cudaStreamDestroy(stream);
-    }
-
-    double* dt_ptr() { return scal.p; }
-    double* t_ptr() { return scal.p + 1; }
-
-    // ---- launch helpers ---------------------------------------------------
-    template <class F>
-    void timed(int cls, F&& launch) {
-        if (!timing) {
-            ck(launch(), "kernel launch");
-            return;
-        }
-        if (marks_used == marks.size()) {
-            Mark m{cls, nullptr, nullptr};
-            ck(cudaEventCreate(&m.a), "cudaEventCreate");
-            ck(cudaEventCreate(&m.b), "cudaEventCreate");
-            marks.push_back(m);
-        }
-        Mark& m = marks[marks_used++];
-        m.cls = cls;
-        ck(cudaEventRecord(m.a, stream), "cudaEventRecord");
-        ck(launch(), "kernel launch");
-        ck(cudaEventRecord(m.b, stream), "cudaEventRecord");
-    }
-
-    bool fast() const { return cfg.precision == MGPU_PREC_FP64_FAST; }
-    bool single() const { return cfg.precision == MGPU_PREC_FP32; }
-    // reciprocal-based update and time step (every form but the exact one)
-    bool rcp() const { return cfg.precision != MGPU_PREC_FP64; }
-
-    void reconstruct(const double* Uin, uint8_t* mask_out) {
-        if (single()) {
-            timed(0, [&] { return f32::launch_teno(teno, K, M, nq, Uin, fv32.p, mask_out, stream); });
-        } else if (cfg.recon == MGPU_RECON_TENO) {
-            timed(0, [&] {
-                return fast() ? fast::launch_teno(teno, K, M, nq, cfg.teno_variant, Uin, fv.p, mask_out, stream)
-                              : exact::launch_teno(teno, K, M, nq, cfg.teno_variant, Uin, fv.p, mask_out, stream);
-            });
-        } else {
-            timed(0, [&] { return launch_first_order((int)F_flux, lr.p, Uin, fv.p, stream); });
-        }
-    }
-
-    void flux(const double* Uin) {
-        FluxArgs a{};
-        a.n_faces = (int)F_flux;
-        a.lr = lr.p;
-        a.nrm = nrm.p;
-        a.area = area.p;
-        a.bc = bcidx.p;
-        a.fv = fv.p;
-        a.G = G.p;
-        a.U = Uin;
-        for (int i = 0; i < 4; i++) a.qw[i] = qw[i];
-        const bool pos = cfg.recon == MGPU_RECON_TENO && cfg.teno_variant == MGPU_TENO_CORRECTED;
-        if (single()) {
-            timed(1, [&] { return f32::launch_flux(a, fv32.p, gas, bct, cfg.riemann_solver, nq, stream); });
-            return;
-        }
-        timed(1, [&] {
-            return fast() ? fast::launch_flux(a, gas, bct, cfg.riemann_solver, nq, pos, stream)
-                          : exact::launch_flux(a, gas, bct, cfg.riemann_solver, nq, pos, stream);
-        });
-    }
-
-    UpdateArgs update_args() {
-        UpdateArgs a{};
-        a.n_cells = (int)N;
-        a.gat = gat.p;
-        a.G = G.p;
-        a.vol = vol.p;
-        a.ivol = ivol.p;
-        a.dt = dt_ptr();
-        a.U = U.p;
-        a.Ut = Ut.p;
-        a.W = W.p;
-        a.prim = prim.p;
-        a.snd = snd.p;
-        a.rhs = rhs.p;
-        a.flags = flags.p;
-        return a;
-    }
-
-    void stage(int k) {
-        const double* in = (k == 1) ? U.p : Ut.p;
-        reconstruct(in, nullptr);
-        flux(in);
-        UpdateArgs a = update_args();
-        timed(2, [&] { return launch_update(a, gas, k, rcp(), stream); });
-    }
-
-    void spectral_and_dt(double cfl, bool accumulate_t) {
-        ck(cudaMemsetAsync(rmax.p, 0, sizeof(unsigned long long), stream), "cudaMemsetAsync");
-        SpecArgs s{};
-        s.n_cells = (int)N;
-        s.cfaces = cfaces.p;
-        s.lr = lr.p;
-        s.nrm = nrm.p;
-        s.dxn = dxn.p;
-        s.idxn = idxn.p;
-        s.U = U.p;
-        s.prim = prim.p;
-        s.snd = snd.p;
-        s.rho_cell = rho_cell.p;
-        s.rmax_bits = rmax.p;
-        s.gamma = gas.gamma;
-        timed(3, [&] { return launch_spectral(s, rcp(), stream); });
-        ck(launch_dt(rmax.p, cfl, dt_ptr(), accumulate_t ? t_ptr() : nullptr, flags.p, stream), "dt launch");
-    }
-
-    void cfl_step(double cfl) {
-        spectral_and_dt(cfl, true);
-        stage(1);
-        stage(2);
-        stage(3);
-    }
-
-    // ---- host <-> device in caller numbering ------------------------------
-    // One copy engine transfer of the caller's buffer (pinned or pageable)
-    // into a staging array, then a permutation kernel on the device.
-    void upload_cells(double* dst, const double* src, int width) {
-        const size_t bytes = (size_t)N * width * sizeof(double);
-        ck(cudaMemcpyAsync(staging.p, src, bytes, cudaMemcpyHostToDevice, stream), "H2D");
-        ck(launch_permute_rows((int)N, width, perm_old.p, staging.p, dst, false, stream), "permute");
-        ck(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
-    }
-    void download_cells(const double* src, double* dst, int width) {
-        const size_t bytes = (size_t)N * width * sizeof(double);
-        ck(launch_permute_rows((int)N, width, perm_old.p, src, staging.p, true, stream), "permute");
-        ck(cudaMemcpyAsync(dst, staging.p, bytes, cudaMemcpyDeviceToHost, stream), "D2H");
-        ck(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
-    }
-
-    void build();
-};
 
 // ---------------------------------------------------------------------------
 // mgpu_finalize: numbering, geometry precomputation, TENO tables, upload
@@ -667,44 +424,6 @@ void mgpu_ctx::build() {
 // C ABI
 // ---------------------------------------------------------------------------
 
-namespace {
-
-template <class F>
-int guarded(F&& fn) {
-    try {
-        return fn();
-    } catch (const CudaFail& e) {
-        set_error(e.what());
-        return MGPU_ERR_CUDA;
-    } catch (const ArgFail& e) {
-        set_error(e.what());
-        return MGPU_ERR_ARG;
-    } catch (const Unsupported& e) {
-        set_error(e.what());
-        return MGPU_ERR_UNSUPPORTED;
-    } catch (const std::bad_alloc&) {
-        set_error("host allocation failed");
-        return MGPU_ERR_HOST;
-    } catch (const std::exception& e) {
-        set_error(e.what());
-        return MGPU_ERR_HOST;
-    }
-}
-
-int need_ready(const mgpu_ctx* ctx) {
-    if (!ctx) {
-        set_error("null context");
-        return MGPU_ERR_ARG;
-    }
-    if (!ctx->finalized) {
-        set_error("context not finalized (call mgpu_finalize after adding boundaries)");
-        return MGPU_ERR_STATE;
-    }
-    return MGPU_OK;
-}
-
-}  // namespace
-
 extern "C" {
 
 const char* mgpu_last_error(void) { return g_error.c_str(); }
@@ -1047,7 +766,7 @@ int mgpu_kernel_times(mgpu_ctx* ctx, double* ms, uint32_t* launches) {
     return guarded([&] {
         if (!ctx || !ms || !launches) throw ArgFail("null argument");
         ck(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
-        for (int i = 0; i < 4; ++i) {
+        for (int i = 0; i < 5; ++i) {
             ms[i] = 0.0;
             launches[i] = 0;
         }

@@ -1,0 +1,97 @@
+// selector.cuh -- the learned TENO stencil selector: features and constants
+// shared by the harvest, training and inference kernels.
+//
+// The selector is a 96-64-64-32 MLP evaluated once per cell.  Its input is,
+// for each conserved variable v (24 entries per variable):
+//   [0,19)  differences U_j - U_c over the central stencil's 19 neighbours
+//           (stencil order), divided by the variable's range over that
+//           stencil (target included);
+//   19      log10 of that range, scaled: (log10 r + 6) / 6 clamped to
+//           [-1, 1]; -1 when the range is zero (below 1e-30);
+//   20..22  range over directional stencil d (target included) divided by
+//           the central range, clipped to 4 and scaled by 1/4; -1 when the
+//           stencil does not exist (boundary face);
+//   23      zero.
+// Its output is 4 heads (one per variable) of 8 logits over TENO's
+// decisions for that variable: class 0 = central stencil only, class
+// m = 1..7 = directional stencils whose bit is set in m pass the cut-off
+// (the kernels' mask >> 1).  The network has no counterpart in the
+// reference; the decisions it learns are those of
+// face_reconstruction.cpp:939-981 as computed by the corrected TENO form.
+#pragma once
+
+#include <cstdint>
+
+#include "device.h"
+#include "selector_params.h"
+
+namespace mgpu {
+namespace sel {
+
+// GELU, tanh form: 0.5 x (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3)))
+__device__ __forceinline__ float gelu(float x) {
+    const float c = 0.7978845608028654f;
+    return 0.5f * x * (1.0f + tanhf(c * (x + 0.044715f * x * x * x)));
+}
+__device__ __forceinline__ float gelu_grad(float x) {
+    const float c = 0.7978845608028654f;
+    const float t = tanhf(c * (x + 0.044715f * x * x * x));
+    return 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * c * (1.0f + 3.0f * 0.044715f * x * x);
+}
+
+// Neighbour j of stencil s of a cell, in either tiled layout:
+// nb [tiles][4][M-1][8] (FP64 forms) or nb4 [tiles][4][ceil((M-1)/4)][8][4] (FP32 form).
+template <bool NB4>
+__device__ __forceinline__ uint32_t stencil_cell(const TenoArgs& a, int tile, int lane, int s, int j) {
+    if (NB4) {
+        constexpr int GJ = (MR + 3) / 4;
+        return __ldg(a.nb4 + ((((size_t)tile * S + s) * GJ + j / 4) * TILE + lane) * 4 + (j & 3));
+    }
+    return __ldg(a.nb + (((size_t)tile * S + s) * MR + j) * TILE + lane);
+}
+
+// Features of variable v of one cell, from the FP64 state (values rounded
+// to FP32 first, as the FP32 form reads them).  Writes PER_VAR floats.
+// to_f converts an FP64 state value to FP32.
+template <bool NB4, class ToF>
+__device__ __forceinline__ void features(const TenoArgs& a, const double* __restrict__ U, int cell, int v,
+                                         unsigned smask, ToF to_f, float* x) {
+    const int tile = cell >> 3, lane = cell & 7;
+    const float uc = to_f(__ldg(U + (size_t)cell * 4 + v));
+    float lo = 0.0f, hi = 0.0f;
+#pragma unroll
+    for (int j = 0; j < MR; ++j) {
+        const uint32_t n = stencil_cell<NB4>(a, tile, lane, 0, j);
+        const float d = to_f(__ldg(U + (size_t)n * 4 + v)) - uc;
+        x[j] = d;
+        lo = fminf(lo, d);
+        hi = fmaxf(hi, d);
+    }
+    // ranges below 1e-30 count as zero (their reciprocal would overflow)
+    const float r0 = hi - lo > 1.0e-30f ? hi - lo : 0.0f;
+    const float inv = r0 > 0.0f ? 1.0f / r0 : 0.0f;
+#pragma unroll
+    for (int j = 0; j < MR; ++j) x[j] *= inv;
+    x[MR] = r0 > 0.0f ? fminf(1.0f, fmaxf(-1.0f, (log10f(r0) + 6.0f) * (1.0f / 6.0f))) : -1.0f;
+#pragma unroll
+    for (int s = 1; s < S; ++s) {
+        float f = -1.0f;
+        if ((smask >> s) & 1u) {
+            float l = 0.0f, h = 0.0f;
+#pragma unroll 4
+            for (int j = 0; j < MR; ++j) {
+                const uint32_t n = stencil_cell<NB4>(a, tile, lane, s, j);
+                const float d = to_f(__ldg(U + (size_t)n * 4 + v)) - uc;
+                l = fminf(l, d);
+                h = fmaxf(h, d);
+            }
+            const float rs = h - l;
+            f = r0 > 0.0f ? fminf(rs * inv, 4.0f) * 0.25f : (rs > 0.0f ? 1.0f : 0.0f);
+        }
+        x[MR + s] = f;
+    }
+    x[PER_VAR - 1] = 0.0f;
+}
+
+}  // namespace sel
+}  // namespace mgpu

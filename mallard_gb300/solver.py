@@ -229,11 +229,31 @@ class Solver:
         N.check(self._lib.mgpu_enable_kernel_timing(self._h, 1 if enable else 0))
 
     def kernel_times(self):
-        """{class: (ms total, launches)} for recon, flux, update, cfl."""
-        ms = np.zeros(4)
-        n = np.zeros(4, dtype=np.uint32)
+        """{class: (ms total, launches)} for recon, flux, update, cfl, selector."""
+        ms = np.zeros(5)
+        n = np.zeros(5, dtype=np.uint32)
         N.check(self._lib.mgpu_kernel_times(self._h, N.ptr(ms), N.ptr(n)))
-        return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(("recon", "flux", "update", "cfl"))}
+        return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(("recon", "flux", "update", "cfl", "selector"))}
+
+    # ---- learned stencil selector (FP32 form) --------------------------------
+    def attach_selector(self, selector, threshold=0.98, directional_threshold=2.0, every_stage=False):
+        """Drive this FP32-form solver's TENO decisions with a trained
+        selector: a variable predicted central with probability >= threshold
+        skips the smoothness indicators and the directional stencils; a
+        directional prediction is trusted only at >= directional_threshold
+        (the default 2 trusts none).  Predictions are made once per time step
+        unless every_stage.  selector None detaches."""
+        N.check(self._lib.mgpu_set_selector(self._h, selector._h if selector is not None else None,
+                                            float(threshold) if selector is not None else 0.0,
+                                            float(directional_threshold)))
+        N.check(self._lib.mgpu_set_selector_every_stage(self._h, 1 if every_stage else 0))
+
+    def selector_stats(self):
+        """Counts over the last reconstruction with the selector attached."""
+        c = np.zeros(6, dtype=np.uint64)
+        N.check(self._lib.mgpu_selector_stats(self._h, N.ptr(c)))
+        keys = ("cells", "confident_cells", "confident_variables", "stencils_evaluated", "stencils_full", "error")
+        return {k: int(c[i]) for i, k in enumerate(keys)}
 
     def traffic_model(self):
         r, s = C.c_double(), C.c_double()

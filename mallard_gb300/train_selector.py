@@ -1,0 +1,127 @@
+"""Train the learned TENO stencil selector on the GPU and save its weights.
+
+    python -m mallard_gb300.train_selector [--out PATH] [--quick]
+
+Training pairs are harvested from the FP64 solver's own runs (corrected
+TENO, p = 3, HLLC, SSPRK3, CFL 0.5) at seeded random initial states of
+three problem families:
+  * Sod-type shock tubes on a 1000 x 8 strip of triangles (symmetry
+    boundaries), random left/right states and diaphragm position;
+  * two-dimensional four-quadrant Riemann problems on the unit square
+    (transmissive boundaries), random quadrant states and split point,
+    harvested over the first steps;
+  * cylindrical explosions (random centre, radius and states).
+Each harvest keeps every cell where some variable leaves the central
+stencil and a fraction of the all-central cells.  The network is then
+trained with minibatch Adam by the library's own kernels.
+"""
+
+import argparse
+import time
+from pathlib import Path
+
+import numpy as np
+
+from . import Mesh, Solver, state_from_primitives
+from .selector import Selector, default_weights_path
+
+GAS = dict(gamma=1.4, p_ref=101325.0, T_ref=298.15, rho_ref=1.225)
+
+
+def _solver(mesh, bc):
+    blist = [{"name": z, "type": bc} for z in mesh.zone_names[1:]]
+    return Solver(mesh, face_reconstruction="TENO", basis_type="legendre", basis_order=3, riemann_solver="HLLC",
+                  boundaries=blist, teno_variant="corrected", precision="fp64_fast", **GAS)
+
+
+def _run_and_harvest(sel, mesh, bc, U, W, steps, every, keep, seed):
+    rows = 0
+    with _solver(mesh, bc) as s:
+        s.set_state(U, W)
+        for k in range(steps // every):
+            s.run(0.5, every)
+            if s.status() != 0:
+                break
+            rows += sel.harvest(s, keep_central=keep, seed=seed * 1000 + k)
+    return rows
+
+
+def harvest_all(sel, seed=0, quick=False, log=print):
+    r = np.random.default_rng(seed)
+    rows = 0
+    # shock tubes, 1000 x 8 strip (a one-cell strip makes the p = 3 least-squares
+    # systems degenerate)
+    strip = Mesh.generate("cartesian_tri", 1000, 8, 1.0, 0.008)
+    x = strip.cell_coords[:, 0]
+    for i in range(4 if quick else 16):
+        left = (r.uniform(0.5, 2.0), r.uniform(-0.5, 0.5), r.uniform(0.5, 2.0))
+        right = (r.uniform(0.05, 0.5), r.uniform(-0.5, 0.5), r.uniform(0.05, 0.5))
+        if r.random() < 0.5:
+            left, right = right, left
+        xd = r.uniform(0.3, 0.7)
+        sel_l = x < xd
+        rho = np.where(sel_l, left[0], right[0])
+        u = np.where(sel_l, left[1], right[1])
+        p = np.where(sel_l, left[2], right[2])
+        U, W = state_from_primitives(rho, u, 0 * u, p, **GAS)
+        rows += _run_and_harvest(sel, strip, "symmetry", U, W, 200, 40, 0.05, 10 + i)
+    log(f"  shock tubes: {rows} rows")
+    # four-quadrant problems
+    n = 128 if quick else 256
+    sq = Mesh.generate("cartesian_tri", n, n, 1.0, 1.0)
+    cx, cy = sq.cell_coords[:, 0], sq.cell_coords[:, 1]
+    for i in range(2 if quick else 6):
+        sx, sy = r.uniform(0.3, 0.8, 2)
+        q = [(r.uniform(0.1, 2.0), r.uniform(-1.5, 1.5), r.uniform(-1.5, 1.5), r.uniform(0.03, 2.0)) for _ in range(4)]
+        prim = np.zeros((sq.n_cells, 4))
+        for k, m in enumerate(((cx >= sx) & (cy >= sy), (cx < sx) & (cy >= sy), (cx < sx) & (cy < sy),
+                               (cx >= sx) & (cy < sy))):
+            prim[m] = q[k]
+        U, W = state_from_primitives(prim[:, 0], prim[:, 1], prim[:, 2], prim[:, 3], **GAS)
+        rows += _run_and_harvest(sel, sq, "extrapolation", U, W, 40, 10, 0.05, 100 + i)
+    log(f"  + four-quadrant: {rows} rows")
+    # cylindrical explosions
+    for i in range(2 if quick else 6):
+        c = r.uniform(0.3, 0.7, 2)
+        rad = r.uniform(0.1, 0.3)
+        inn = (cx - c[0]) ** 2 + (cy - c[1]) ** 2 < rad * rad
+        a = (r.uniform(0.5, 2.0), r.uniform(0.5, 2.0))
+        b = (r.uniform(0.1, 0.5), r.uniform(0.05, 0.4))
+        if r.random() < 0.3:
+            a, b = b, a
+        rho = np.where(inn, a[0], b[0])
+        p = np.where(inn, a[1], b[1])
+        U, W = state_from_primitives(rho, 0 * rho, 0 * rho, p, **GAS)
+        rows += _run_and_harvest(sel, sq, "extrapolation", U, W, 120 if quick else 240, 30, 0.05, 200 + i)
+    log(f"  + explosions: {rows} rows")
+    return rows
+
+
+def train(out=None, seed=0, quick=False, epochs=None, log=print):
+    t0 = time.time()
+    sel = Selector(seed=seed + 1)
+    rows = harvest_all(sel, seed=seed, quick=quick, log=log)
+    t1 = time.time()
+    epochs = epochs or (6 if quick else 12)
+    losses = sel.train(epochs=epochs, batch=4096, lr=2e-3, seed=seed + 2)
+    t2 = time.time()
+    log(f"harvest {rows} rows in {t1 - t0:.1f} s; train {epochs} epochs in {t2 - t1:.1f} s; "
+        f"loss {losses[0]:.4f} -> {losses[-1]:.4f}")
+    if out:
+        Path(out).parent.mkdir(parents=True, exist_ok=True)
+        sel.save(out, rows=rows, losses=losses, seed=seed, epochs=epochs)
+    return sel, losses
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--out", default=str(default_weights_path()))
+    ap.add_argument("--seed", type=int, default=20261203)
+    ap.add_argument("--quick", action="store_true")
+    ap.add_argument("--epochs", type=int, default=None)
+    a = ap.parse_args()
+    train(a.out, seed=a.seed, quick=a.quick, epochs=a.epochs)
+
+
+if __name__ == "__main__":
+    main()

@@ -22,13 +22,24 @@ QUADRANTS = {
 }
 
 
-def four_quadrant(mesh, split=0.8):
+def four_quadrant(mesh, split=0.8, states=None):
+    """states: optional (rho, u, v, p) for UR, UL, LL, LR."""
     x, y = mesh.cell_coords[:, 0], mesh.cell_coords[:, 1]
     r, t = x >= split, y >= split
     prim = np.zeros((mesh.n_cells, 4))
-    for key, sel in (("UR", r & t), ("UL", ~r & t), ("LL", ~r & ~t), ("LR", r & ~t)):
-        prim[sel] = QUADRANTS[key]
+    for i, (key, sel) in enumerate((("UR", r & t), ("UL", ~r & t), ("LL", ~r & ~t), ("LR", r & ~t))):
+        prim[sel] = QUADRANTS[key] if states is None else states[i]
     return mg.state_from_primitives(prim[:, 0], prim[:, 1], prim[:, 2], prim[:, 3], **GAS)
+
+
+def explosion(mesh, center=(0.5, 0.5), radius=0.2, inside=(1.0, 1.0), outside=(0.125, 0.1)):
+    """Cylindrical Sod problem: (rho, p) inside and outside a circle, at rest."""
+    x, y = mesh.cell_coords[:, 0] - center[0], mesh.cell_coords[:, 1] - center[1]
+    inn = x * x + y * y < radius * radius
+    rho = np.where(inn, inside[0], outside[0])
+    p = np.where(inn, inside[1], outside[1])
+    z = np.zeros(mesh.n_cells)
+    return mg.state_from_primitives(rho, z, z, p, **GAS)
 
 
 def sod(mesh, split=0.5):
