@@ -1,25 +1,37 @@
 """Benchmark of the Mallard residual-and-update path on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--n 1024]
+                    [--form fp32_learned] [--forms fp64,fp64_fast,fp32]
 
 Workload (the 2D four-quadrant Riemann configuration): cartesian_tri mesh of
 n x n quads split into 2 n^2 triangles (n = 1024 -> 2,097,152 cells) on the
 unit square, relabelled by a seeded random cell permutation (seed 20261203)
 and reverse-Cuthill-McKee ordered inside the library; TENO p = 3 (legendre),
 HLLC, SSPRK3 with CFL 0.5, extrapolation (transmissive) boundaries, gamma
-1.4, quadrant states split at x = y = 0.8.  Synthetic, seeded data; FP64.
-The TENO weighting is the corrected variant (same work per cell as the
+1.4, quadrant states split at x = y = 0.8.  Synthetic, seeded data.  The
+TENO weighting is the corrected variant (same work per cell as the
 reference's weighting, which turns this state non-finite within one step).
 
+Forms (all on the GPU, same mesh, state and steps):
+  fp64          the plain path, the reference's arithmetic (the parity path)
+  fp64_fast     FP64 with FMA contraction
+  fp32          reconstruction and flux in FP32, state and accumulation FP64
+  fp32_learned  fp32 + the learned stencil selector (the headline by default)
+The headline line carries the headline form's rate, and "forms" every
+form's rate, per-kernel times and its density L1 / L-infinity and mass /
+energy differences against the plain FP64 state after the same steps.
+
 One step = spectral radius + dt + three stages of (reconstruction, face flux,
-residual gather + update), all on the GPU, replayed as a CUDA graph.  Inputs
-(tables ~14 GB) are far larger than L2, so no explicit flush is done.
+residual gather + update), plus one selector inference per step in the
+learned form, all on the GPU, replayed as a CUDA graph.  Inputs (tables
+7-15 GB) are far larger than L2, so no explicit flush is done.
 
 Metric: Mcell-updates/s = cells x steps / seconds / 1e6 (one cell-update =
 one cell advanced one full SSPRK3 step).
 
 --impl reference times the CPU oracle (the restatement of the reference's
-algorithm, all host threads) on a 256 x 256 sample of the same workload.
+algorithm, FP64, all host threads) on a 256 x 256 sample of the same
+workload.
 """
 
 import argparse
@@ -52,10 +64,12 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=1024, help="quads per side (cells = 2 n^2)")
     ap.add_argument("--variant", default="corrected", choices=["reference", "corrected"])
-    ap.add_argument("--precision", default="fp64_fast", choices=["fp64", "fp64_fast"],
-                    help="fp64: the reference's rounding (bit-faithful); fp64_fast: FMA-contracted FP64")
-    ap.add_argument("--forms", default="fp64,fp32,fp32_learned",
-                    help="other precision forms to time on the same workload (comma list, '' for none)")
+    ap.add_argument("--form", default="fp32_learned", choices=["fp64", "fp64_fast", "fp32", "fp32_learned"],
+                    help="headline form: fp64 = the reference's rounding (bit-faithful); fp64_fast = FMA-contracted "
+                         "FP64; fp32 = FP32-bulk reconstruction and flux; fp32_learned = fp32 + learned selector")
+    ap.add_argument("--forms", default="fp64,fp64_fast,fp32",
+                    help="other forms timed on the same workload (comma list, '' for none); fp64 is also the "
+                         "error reference")
     ap.add_argument("--cpu-sample-n", type=int, default=CPU_SAMPLE_N)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -75,8 +89,8 @@ def case_mesh(n):
 def workload_config(args, n):
     return {"workload": f"four-quadrant Riemann, cartesian_tri {n}x{n} quads -> {2 * n * n} triangles, "
                         f"seeded permutation + RCM, TENO p3 legendre + HLLC, SSPRK3 CFL {CFL}, transmissive BCs",
-            "cells": 2 * n * n, "teno_variant": args.variant, "seed": SEED, "precision": args.precision,
-            "l2": "inputs larger than L2 (TENO tables ~7 KB/cell); no flush", "parallelism": "replicas"}
+            "cells": 2 * n * n, "teno_variant": args.variant, "seed": SEED,
+            "l2": "inputs larger than L2 (TENO tables 3.4-7 KB/cell); no flush", "parallelism": "replicas"}
 
 
 # ---------------------------------------------------------------------------
@@ -172,7 +186,7 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs * 1e3 / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": workload_config(args, args.n),
+            "config": dict(workload_config(args, args.n), form="reference CPU path (oracle port, FP64)"),
             "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -212,58 +226,96 @@ def load_selector(device):
     return sel, "trained at startup (quick)"
 
 
-def time_form(m, args, precision, U0, W0, device, U_ref, selector=None):
-    """Rate of another precision form on the same mesh and state, and its
-    error against the headline form after the same W + K steps."""
-    import numpy as np
-    import torch
+def selector_summary(selector, stats):
+    return {"weights": selector[1], "central_threshold": SEL_THRESHOLD,
+            "directional_predictions": "not trusted (full TENO)",
+            "predict": "once per step, from the step's initial state; trusted where the face neighbours are confident too",
+            "confident_cells": stats["confident_cells"] / stats["cells"],
+            "confident_variables": stats["confident_variables"] / (4 * stats["cells"]),
+            "stencils_evaluated_frac": stats["stencils_evaluated"] / stats["stencils_full"],
+            "error_flag": stats["error"]}
 
+
+FORMS = {
+    # form: (precision, learned selector)
+    "fp64": ("fp64", False),
+    "fp64_fast": ("fp64_fast", False),
+    "fp32": ("fp32", False),
+    "fp32_learned": ("fp32", True),
+}
+
+
+def make_solver(m, args, form, device, selector):
     import mallard_gb300 as mg
+    prec, learned = FORMS[form]
     s = mg.Solver(m, face_reconstruction="TENO", basis_type="legendre", basis_order=3, riemann_solver="HLLC",
                   boundaries=[{"name": z, "type": "extrapolation"} for z in ("right", "top", "left", "bottom")],
-                  teno_variant=args.variant, reorder=True, device=device, precision=precision)
-    if selector is not None:
+                  teno_variant=args.variant, reorder=True, device=device, precision=prec)
+    if learned:
         s.attach_selector(selector[0], threshold=SEL_THRESHOLD)
+    return s
+
+
+def errors_vs(m, U, U_ref):
+    import numpy as np
+    vol = m.cell_volume
+    if not (np.isfinite(U).all() and np.isfinite(U_ref).all()):
+        return {"finite": bool(np.isfinite(U).all())}
+    d = np.abs(U[:, 0] - U_ref[:, 0])
+    return {"density_l1_rel_err": float(np.sum(vol * d) / np.sum(vol * np.abs(U_ref[:, 0]))),
+            "density_linf_rel_err": float(d.max() / np.abs(U_ref[:, 0]).max()),
+            "mass_rel_diff": float(abs(np.sum(vol * U[:, 0]) - np.sum(vol * U_ref[:, 0])) / np.sum(vol * U_ref[:, 0])),
+            "energy_rel_diff": float(abs(np.sum(vol * U[:, 3]) - np.sum(vol * U_ref[:, 3])) /
+                                     np.sum(vol * U_ref[:, 3]))}
+
+
+def time_form(m, args, form, U0, W0, device, selector, barrier=None, clocks=None):
+    """One form on the workload: device-timed rate over K graph-replayed steps
+    after W warm-up steps (CUDA events on the solver's stream), the final
+    state, per-kernel times from a second pass with events around every
+    launch, and the selector's statistics."""
+    import torch
+    s = make_solver(m, args, form, device, selector)
     stream = torch.cuda.Stream()
     s.set_stream(stream.cuda_stream)
     s.set_state(U0, W0)
     s.launch(CFL, args.warmup)
     s.synchronize()
+    if clocks:
+        clocks.start()
+        time.sleep(0.3)
+    if barrier:
+        barrier()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     s.launch(CFL, args.steps)
     e1.record(stream)
     e1.synchronize()
+    if barrier:
+        barrier()
     ms = e0.elapsed_time(e1)
+    clk = clocks.stop() if clocks else None
+    flags = s.status()
     U, _ = s.get_state()
-    stats = s.selector_stats() if selector is not None else None
+    stats = s.selector_stats() if FORMS[form][1] else None
     s.set_state(U0, W0)
     s.launch(CFL, args.warmup)
     s.kernel_timing(True)
     s.launch(CFL, args.steps)
     kt = s.kernel_times()
-    s.close()
-    vol = m.cell_volume
-    out = {"value": m.n_cells * args.steps / (ms * 1e-3) / 1e6, "ms_per_step": ms / args.steps,
-           "finite": bool(np.isfinite(U).all()),
-           "kernel_ms_per_launch": {k: v[0] / max(v[1], 1) for k, v in kt.items() if v[1]}}
-    if stats is not None:
-        out["selector"] = {"weights": selector[1], "central_threshold": SEL_THRESHOLD,
-                           "directional_predictions": "not trusted (full TENO)",
-                           "predict": "once per step, from the step's initial state",
-                           "confident_cells": stats["confident_cells"] / stats["cells"],
-                           "confident_variables": stats["confident_variables"] / (4 * stats["cells"]),
-                           "stencils_evaluated_frac": stats["stencils_evaluated"] / stats["stencils_full"],
-                           "error_flag": stats["error"]}
-    if np.isfinite(U_ref).all() and out["finite"]:
-        d = np.abs(U[:, 0] - U_ref[:, 0])
-        out["density_l1_rel_err"] = float(np.sum(vol * d) / np.sum(vol * np.abs(U_ref[:, 0])))
-        out["density_linf_rel_err"] = float(d.max() / np.abs(U_ref[:, 0]).max())
-        out["mass_rel_diff"] = float(abs(np.sum(vol * U[:, 0]) - np.sum(vol * U_ref[:, 0])) / np.sum(vol * U_ref[:, 0]))
-        out["energy_rel_diff"] = float(abs(np.sum(vol * U[:, 3]) - np.sum(vol * U_ref[:, 3])) /
-                                       np.sum(vol * U_ref[:, 3]))
-    return out
+    s.kernel_timing(False)
+    return s, {"ms": ms, "U": U, "flags": flags, "stats": stats, "kt": kt, "clocks": clk}
+
+
+def recon_bytes_selected(solver, stats, cells):
+    """Compulsory bytes of one selector-driven reconstruction launch: the
+    tables of the stencils actually evaluated plus the per-cell constants
+    (shapes, face slots, stencil mask, prediction, state, face states)."""
+    full_bytes, _ = solver.traffic_model()
+    per_stencil = 19 * (4 + 4 * 9)
+    fixed = full_bytes - stats["stencils_full"] * per_stencil
+    return stats["stencils_evaluated"] * per_stencil + fixed + cells * 4
 
 
 def run_ours(args):
@@ -294,45 +346,32 @@ def run_ours(args):
 
     t_setup = time.perf_counter()
     m = case_mesh(args.n)
-    solver = mg.Solver(m, face_reconstruction="TENO", basis_type="legendre", basis_order=3, riemann_solver="HLLC",
-                       boundaries=[{"name": z, "type": "extrapolation"} for z in ("right", "top", "left", "bottom")],
-                       teno_variant=args.variant, reorder=True, device=local, precision=args.precision)
-    setup_s = time.perf_counter() - t_setup
-    stream = torch.cuda.Stream()
-    solver.set_stream(stream.cuda_stream)
     U0, W0 = four_quadrant(m)
     cells = m.n_cells
+    head = args.form
+    selector = load_selector(local) if FORMS[head][1] or "fp32_learned" in args.forms.split(",") else None
+    setup_s = time.perf_counter() - t_setup
 
-    # ---- timed region: K steps of the device-resident loop (CUDA graph)
-    solver.set_state(U0, W0)
-    solver.launch(CFL, args.warmup)
-    solver.synchronize()
+    # ---- the other forms (the plain FP64 path's final state is the error reference)
+    forms, finals = {}, {}
+    for form in [f for f in args.forms.split(",") if f and f != head]:
+        s, r = time_form(m, args, form, U0, W0, local, selector)
+        s.close()
+        finals[form] = r["U"]
+        kt = r["kt"]
+        forms[form] = {"value": cells * args.steps / (r["ms"] * 1e-3) / 1e6, "ms_per_step": r["ms"] / args.steps,
+                       "finite": bool(np.isfinite(r["U"]).all()) and r["flags"] == 0,
+                       "kernel_ms_per_launch": {k: v[0] / max(v[1], 1) for k, v in kt.items() if v[1]}}
+        if r["stats"]:
+            forms[form]["selector"] = selector_summary(selector, r["stats"])
+    # ---- the headline form
     clocks = ClockSampler(local)
-    clocks.start()
-    time.sleep(0.3)
-    barrier()
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    ev0.record(stream)
-    solver.launch(CFL, args.steps)
-    ev1.record(stream)
-    ev1.synchronize()
-    barrier()
-    ms = ev0.elapsed_time(ev1)
-    clk = clocks.stop()
-    flags = solver.status()
-    Uend, _ = solver.get_state()
-    finite = bool(np.isfinite(Uend).all()) and flags == 0
-    ms_max = max_over_ranks(ms)
+    solver, r = time_form(m, args, head, U0, W0, local, selector, barrier=barrier, clocks=clocks)
+    ms_max = max_over_ranks(r["ms"])
     value = cells * args.steps * world / (ms_max * 1e-3) / 1e6
-
-    # ---- per-kernel times (same steps from the same state, events around each launch)
-    solver.set_state(U0, W0)
-    solver.launch(CFL, args.warmup)
-    solver.kernel_timing(True)
-    solver.launch(CFL, args.steps)
-    kt = solver.kernel_times()
-    solver.kernel_timing(False)
+    Uend, flags, kt, clk, stats = r["U"], r["flags"], r["kt"], r["clocks"], r["stats"]
+    finite = bool(np.isfinite(Uend).all()) and flags == 0
+    finals[head] = Uend
 
     # ---- end to end through the public API with host buffers
     Uh = torch.empty((cells, 4), dtype=torch.float64, pin_memory=True).numpy()
@@ -351,65 +390,95 @@ def run_ours(args):
     h2d = cells * (4 + 5) * 8
     d2h = cells * (4 + 5) * 8
 
-    # ---- roofline of the dominant kernel (reconstruction)
+    # ---- roofline of the dominant kernel
     recon_bytes, stage_bytes = solver.traffic_model()
     peaks = {}
     pk = ROOT / "MEASURED_PEAKS.json"
     if pk.exists():
         peaks = json.loads(pk.read_text())
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    recon_ms, recon_n = kt["recon"]
-    recon_avg_s = recon_ms / max(recon_n, 1) * 1e-3
-    achieved = recon_bytes / recon_avg_s / 1e9
+    total_ms = sum(x[0] for x in kt.values())
+    kshare = {k: {"ms_per_launch": v[0] / max(v[1], 1), "launches": v[1], "share": v[0] / max(total_ms, 1e-30)}
+              for k, v in kt.items() if v[1]}
+    dom = max(kshare, key=lambda k: kshare[k]["share"])
+    learned = FORMS[head][1]
+    kernel_names = {"recon": ("teno32_kernel<10,20,2,SEL>" if learned else
+                              ("teno32_kernel<10,20,2>" if FORMS[head][0] == "fp32" else "teno_kernel<10,20,2>")),
+                    "selector": "mlp_kernel<1> (tcgen05)", "flux": "flux kernel", "update": "update_kernel",
+                    "cfl": "spectral_kernel"}
+    dom_ms, dom_n = kt[dom]
+    dom_s = dom_ms / max(dom_n, 1) * 1e-3
+    if dom == "recon":
+        algo = recon_bytes_selected(solver, stats, cells) if learned else recon_bytes
+    elif dom == "selector":
+        # nb4 indices of all stencils, the state gathered once per cell, predictions, weight image per CTA
+        algo = (stats["stencils_full"] * 19 * 4 + cells * (32 + 4) + (cells + 127) // 128 * 25216) if stats else 0
+    else:
+        algo = 0
+    achieved = algo / dom_s / 1e9 if algo else None
     traffic = None
     tf = ROOT / "profiles" / "teno_recon_traffic.json"
-    if tf.exists():
+    if tf.exists() and dom == "recon":
         t = json.loads(tf.read_text())
-        traffic = t.get("dram_bytes_per_cell", 0) * cells or None
-    kshare = {k: {"ms_per_launch": v[0] / max(v[1], 1), "launches": v[1], "share": v[0] / max(sum(x[0] for x in kt.values()), 1e-30)}
-              for k, v in kt.items()}
-    # FP64 arithmetic roof of the reconstruction (FP64 is the binding unit on GB300)
-    flops_cell = teno_flops_per_cell(args.precision)
-    fp64_peak = mg.fp64_peak_gflops(local)
-    fp64_achieved = flops_cell * cells / recon_avg_s / 1e9
-    gpu_launches = args.steps * 11
-
-    # ---- other forms on the same workload: rate and error against the FP64 state
-    forms = {}
-    for prec in [p for p in args.forms.split(",") if p and p != args.precision]:
-        if prec == "fp32_learned":
-            forms[prec] = time_form(m, args, "fp32", U0, W0, local, Uend, selector=load_selector(local))
-        else:
-            forms[prec] = time_form(m, args, prec, U0, W0, local, Uend)
-    forms[args.precision] = {"value": value, "ms_per_step": ms_max / args.steps, "finite": finite}
+        key = "fp32_learned" if learned else FORMS[head][0]
+        per_cell = t.get("dram_bytes_per_cell_by_form", {}).get(key)
+        traffic = per_cell * cells if per_cell else None
+    roofline = {"bound": "hbm", "kernel": kernel_names.get(dom, dom), "achieved": achieved, "peak": hbm_peak,
+                "unit": "GB/s", "frac": achieved / hbm_peak if achieved else None,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if pk.exists() else "fallback 6800 GB/s",
+                "traffic": traffic, "algorithmic_bytes_per_launch": algo}
+    launches_per_step = 11 + (2 if learned else 0)  # + selector inference and neighbour check
+    gpu_launches = args.steps * launches_per_step
+    forms[head] = {"value": value, "ms_per_step": ms_max / args.steps, "finite": finite,
+                   "kernel_ms_per_launch": {k: v[0] / max(v[1], 1) for k, v in kt.items() if v[1]}}
+    if stats:
+        forms[head]["selector"] = selector_summary(selector, stats)
+    solver.close()
+    # errors of every form against the plain FP64 path after the same W + K steps
+    accuracy = None
+    if "fp64" in finals:
+        for form, U in finals.items():
+            if form != "fp64":
+                forms[form].update(errors_vs(m, U, finals["fp64"]))
+        if head != "fp64":
+            accuracy = {k: forms[head].get(k) for k in ("density_l1_rel_err", "density_linf_rel_err",
+                                                        "mass_rel_diff", "energy_rel_diff")}
+            accuracy["against"] = "plain FP64 GPU path (bit-faithful to the reference's arithmetic), same steps"
+            accuracy["bar"] = "density L1 <= 1e-3"
+    fp64_roof = None
+    if FORMS[head][0].startswith("fp64"):
+        flops_cell = teno_flops_per_cell(FORMS[head][0])
+        fp64_peak = mg.fp64_peak_gflops(local)
+        rs = kt["recon"][0] / max(kt["recon"][1], 1) * 1e-3
+        fp64_roof = {"achieved_gflops": flops_cell * cells / rs / 1e9, "peak_gflops": fp64_peak,
+                     "frac": flops_cell * cells / rs / 1e9 / fp64_peak, "flops_per_cell": flops_cell,
+                     "peak_source": "measured FMA-chain probe on this GPU"}
 
     cpu = None
-    if rank == 0 and world >= 1 and not args.no_cpu_baseline:
+    if rank == 0 and not args.no_cpu_baseline:
         rate, threads, secs, ccells = cpu_oracle_rate(args.cpu_sample_n, 2, 1, args.variant)
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"cartesian_tri {args.cpu_sample_n}x{args.cpu_sample_n} ({ccells} cells) of the same "
-                         f"workload, 2 steps after 1 warm-up, {threads} OpenMP threads, {secs:.1f} s"}
+                         f"workload, FP64 plain, 2 steps after 1 warm-up, {threads} OpenMP threads, {secs:.1f} s"}
 
     if rank == 0:
+        cfg = workload_config(args, args.n)
+        cfg["form"] = head
+        cfg["precision"] = FORMS[head][0] + (" + learned stencil selector" if learned else "")
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": workload_config(args, args.n),
+                "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32 (reconstruction, flux) + f64 (state, accumulation)" if FORMS[head][0] == "fp32" else "f64",
+                "data": "synthetic", "config": cfg,
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-                "gpu_launches": gpu_launches,
-                "clocks": clk,
-                "roofline": {"bound": "hbm", "kernel": "teno_kernel<10,20,2>", "achieved": achieved,
-                             "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
-                             "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if pk.exists() else "fallback",
-                             "traffic": traffic, "algorithmic_bytes_per_launch": recon_bytes},
-                "fp64_roof": {"achieved_gflops": fp64_achieved, "peak_gflops": fp64_peak,
-                              "frac": fp64_achieved / fp64_peak, "flops_per_cell": flops_cell,
-                              "peak_source": "measured FMA-chain probe on this GPU"},
+                "gpu_launches": gpu_launches, "clocks": clk, "roofline": roofline,
                 "kernels": kshare, "stage_bytes": stage_bytes, "finite": finite, "status_flags": flags,
-                "forms": forms,
-                "setup_s": setup_s, "cpu_baseline": cpu}
+                "forms": forms, "setup_s": setup_s, "cpu_baseline": cpu}
+        if fp64_roof:
+            line["fp64_roof"] = fp64_roof
+        if accuracy:
+            line["accuracy_vs_fp64"] = accuracy
         print(json.dumps(line), flush=True)
-    solver.close()
     if dist:
         dist.destroy_process_group()
 

@@ -232,8 +232,9 @@ int mgpu_calc_dt_noalloc(mgpu_ctx* ctx, double cfl, double* dt_device, double* s
  * Adam); inference runs on the tcgen05 tensor cores in BF16 with FP32
  * accumulation.  Attached to an FP32-form context (p = 3) it replaces the
  * smoothness indicators of every variable whose predicted class reaches
- * the probability threshold, and the cell evaluates only the stencils its
- * variables need; a variable below the threshold runs full TENO. */
+ * the probability threshold in the cell and in all its face neighbours, and
+ * the cell evaluates only the stencils its variables need; any other
+ * variable runs full TENO. */
 #define MGPU_SEL_INPUTS 96
 #define MGPU_SEL_OUTPUTS 32
 #define MGPU_SEL_CLASSES 8

@@ -92,7 +92,7 @@ struct mgpu_ctx {
     bool sel_on = false;
     float sel_thr_central = 0.0f, sel_thr_directional = 0.0f;
     bool sel_every_stage = false;
-    DevArray<uint8_t> sel_wimg, pred;
+    DevArray<uint8_t> sel_wimg, pred, trusted;  // raw predictions, after the neighbour check
     DevArray<unsigned> sel_err;
     DevArray<unsigned> flags;
     DevArray<unsigned long long> rmax;
@@ -164,11 +164,16 @@ struct mgpu_ctx {
     // predict: run the selector on Uin (otherwise reuse its last predictions)
     void reconstruct(const double* Uin, uint8_t* mask_out, bool predict = true) {
         if (single() && sel_on) {
-            if (predict) timed(4, [&] {
-                return sel::launch_mlp_cells(sel_wimg.p, teno, Uin, sel_thr_central, sel_thr_directional, pred.p,
-                                             sel_err.p, stream);
+            if (predict) {
+                timed(4, [&] {
+                    return sel::launch_mlp_cells(sel_wimg.p, teno, Uin, sel_thr_central, sel_thr_directional, pred.p,
+                                                 sel_err.p, stream);
+                });
+                timed(4, [&] { return sel::launch_trust((int)N, cfaces.p, lr.p, pred.p, trusted.p, stream); });
+            }
+            timed(0, [&] {
+                return f32::launch_teno_selected(teno, K, M, nq, Uin, trusted.p, fv32.p, mask_out, stream);
             });
-            timed(0, [&] { return f32::launch_teno_selected(teno, K, M, nq, Uin, pred.p, fv32.p, mask_out, stream); });
         } else if (single()) {
             timed(0, [&] { return f32::launch_teno(teno, K, M, nq, Uin, fv32.p, mask_out, stream); });
         } else if (cfg.recon == MGPU_RECON_TENO) {

@@ -467,6 +467,7 @@ int mgpu_set_selector(mgpu_ctx* ctx, mgpu_selector* s, float thr_central, float 
         ck(sel::mlp_prepare(), "cudaFuncSetAttribute");
         if (!ctx->sel_wimg.p) ctx->sel_wimg.alloc(sel::WEIGHT_IMAGE_BYTES);
         if (!ctx->pred.p) ctx->pred.alloc((size_t)ctx->N * 4);
+        if (!ctx->trusted.p) ctx->trusted.alloc((size_t)ctx->N * 4);
         if (!ctx->sel_err.p) ctx->sel_err.alloc(1);
         ck(cudaMemcpy(ctx->sel_wimg.p, s->d_wimg.p, sel::WEIGHT_IMAGE_BYTES, cudaMemcpyDeviceToDevice), "D2D");
         ctx->sel_thr_central = thr_central;
@@ -498,7 +499,7 @@ int mgpu_selector_stats(mgpu_ctx* ctx, uint64_t* counts) {
         if (!counts) throw ArgFail("null argument");
         if (!ctx->pred.p) throw ArgFail("no selector attached");
         std::vector<uint8_t> pr((size_t)ctx->N * 4), sm(ctx->N);
-        ck(cudaMemcpyAsync(pr.data(), ctx->pred.p, pr.size(), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+        ck(cudaMemcpyAsync(pr.data(), ctx->trusted.p, pr.size(), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
         ck(cudaMemcpyAsync(sm.data(), ctx->smask.p, sm.size(), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
         unsigned e = 0;
         ck(cudaMemcpyAsync(&e, ctx->sel_err.p, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream), "D2H");

@@ -50,6 +50,31 @@ __device__ __forceinline__ uint32_t stencil_cell(const TenoArgs& a, int tile, in
     return __ldg(a.nb + (((size_t)tile * S + s) * MR + j) * TILE + lane);
 }
 
+// The 19 stencil values of variable v minus uc, for stencil s of a cell.
+// NB4: 16-byte index loads from the FP32 form's grouped layout.
+template <bool NB4, class ToF>
+__device__ __forceinline__ void stencil_diffs(const TenoArgs& a, const double* __restrict__ U, int tile, int lane,
+                                              int s, int v, float uc, ToF to_f, float* d) {
+    if (NB4) {
+        constexpr int GJ = (MR + 3) / 4;
+        const uint4* p = reinterpret_cast<const uint4*>(a.nb4) + (((size_t)tile * S + s) * GJ) * TILE + lane;
+        uint32_t id[GJ * 4];
+#pragma unroll
+        for (int g = 0; g < GJ; ++g) {
+            const uint4 q = __ldg(p + g * TILE);
+            id[4 * g] = q.x;
+            id[4 * g + 1] = q.y;
+            id[4 * g + 2] = q.z;
+            id[4 * g + 3] = q.w;
+        }
+#pragma unroll
+        for (int j = 0; j < MR; ++j) d[j] = to_f(__ldg(U + (size_t)id[j] * 4 + v)) - uc;
+    } else {
+#pragma unroll
+        for (int j = 0; j < MR; ++j) d[j] = to_f(__ldg(U + (size_t)stencil_cell<false>(a, tile, lane, s, j) * 4 + v)) - uc;
+    }
+}
+
 // Features of variable v of one cell, from the FP64 state (values rounded
 // to FP32 first, as the FP32 form reads them).  Writes PER_VAR floats.
 // to_f converts an FP64 state value to FP32.
@@ -58,14 +83,12 @@ __device__ __forceinline__ void features(const TenoArgs& a, const double* __rest
                                          unsigned smask, ToF to_f, float* x) {
     const int tile = cell >> 3, lane = cell & 7;
     const float uc = to_f(__ldg(U + (size_t)cell * 4 + v));
+    stencil_diffs<NB4>(a, U, tile, lane, 0, v, uc, to_f, x);
     float lo = 0.0f, hi = 0.0f;
 #pragma unroll
     for (int j = 0; j < MR; ++j) {
-        const uint32_t n = stencil_cell<NB4>(a, tile, lane, 0, j);
-        const float d = to_f(__ldg(U + (size_t)n * 4 + v)) - uc;
-        x[j] = d;
-        lo = fminf(lo, d);
-        hi = fmaxf(hi, d);
+        lo = fminf(lo, x[j]);
+        hi = fmaxf(hi, x[j]);
     }
     // ranges below 1e-30 count as zero (their reciprocal would overflow)
     const float r0 = hi - lo > 1.0e-30f ? hi - lo : 0.0f;
@@ -77,13 +100,13 @@ __device__ __forceinline__ void features(const TenoArgs& a, const double* __rest
     for (int s = 1; s < S; ++s) {
         float f = -1.0f;
         if ((smask >> s) & 1u) {
+            float d[MR];
+            stencil_diffs<NB4>(a, U, tile, lane, s, v, uc, to_f, d);
             float l = 0.0f, h = 0.0f;
-#pragma unroll 4
+#pragma unroll
             for (int j = 0; j < MR; ++j) {
-                const uint32_t n = stencil_cell<NB4>(a, tile, lane, s, j);
-                const float d = to_f(__ldg(U + (size_t)n * 4 + v)) - uc;
-                l = fminf(l, d);
-                h = fmaxf(h, d);
+                l = fminf(l, d[j]);
+                h = fmaxf(h, d[j]);
             }
             const float rs = h - l;
             f = r0 > 0.0f ? fminf(rs * inv, 4.0f) * 0.25f : (rs > 0.0f ? 1.0f : 0.0f);

@@ -44,6 +44,10 @@ int mlp_smem_bytes();
 cudaError_t mlp_prepare();
 cudaError_t launch_mlp_rows(const uint8_t* wimg, int n, const float* X, float* logits, uint8_t* pred,
                             float thr_central, float thr_directional, unsigned* err, cudaStream_t s);
+// trusted = pred with the confident bit kept only where every face
+// neighbour's same variable is confident too (both [n][4] bytes)
+cudaError_t launch_trust(int n, const int4* cfaces, const int2* lr, const uint8_t* pred, uint8_t* trusted,
+                         cudaStream_t s);
 cudaError_t launch_mlp_cells(const uint8_t* wimg, const TenoArgs& a, const double* U, float thr_central,
                              float thr_directional, uint8_t* pred, unsigned* err, cudaStream_t s);
 

@@ -287,9 +287,38 @@ __global__ void __launch_bounds__(THREADS, 2) mlp_kernel(const uint8_t* __restri
     if (warp == 0) tmem_dealloc(tbase);
 }
 
+// Trust a confident prediction only where the same variable is confident in
+// every face neighbour too: predictions made once per step then keep a
+// one-cell margin to any discontinuity, more than it moves within a step.
+__global__ void __launch_bounds__(256) trust_kernel(int n, const int4* __restrict__ cfaces,
+                                                   const int2* __restrict__ lr, const uint32_t* __restrict__ pred,
+                                                   uint32_t* __restrict__ trusted) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    uint32_t keep = pred[c] & 0x80808080u;
+    const int4 cf = cfaces[c];
+    const int fs[4] = {cf.x, cf.y, cf.z, cf.w};
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        if (fs[e] < 0) break;
+        const int2 o = lr[fs[e]];
+        const int other = o.x == c ? o.y : o.x;
+        if (other >= 0) keep &= pred[other];
+    }
+    trusted[c] = (pred[c] & 0x7f7f7f7fu) | keep;
+}
+
 }  // namespace
 
 int mlp_smem_bytes() { return SM_TOTAL; }
+
+cudaError_t launch_trust(int n, const int4* cfaces, const int2* lr, const uint8_t* pred, uint8_t* trusted,
+                         cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    trust_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, cfaces, lr, reinterpret_cast<const uint32_t*>(pred),
+                                                   reinterpret_cast<uint32_t*>(trusted));
+    return cudaGetLastError();
+}
 
 cudaError_t mlp_prepare() {
     cudaError_t e = cudaFuncSetAttribute(mlp_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM_TOTAL);
