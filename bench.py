@@ -29,6 +29,10 @@ learned form, all on the GPU, replayed as a CUDA graph.  Inputs (tables
 Metric: Mcell-updates/s = cells x steps / seconds / 1e6 (one cell-update =
 one cell advanced one full SSPRK3 step).
 
+A second section, "wedge", times the benchmark spec's 4M-cell configuration:
+the supersonic ramp channel (Delaunay mesh, inviscid), plain FP64 against
+FP32 + learned selector, with the learned form's density error.
+
 --impl reference times the CPU oracle (the restatement of the reference's
 algorithm, FP64, all host threads) on a 256 x 256 sample of the same
 workload.
@@ -54,6 +58,7 @@ SEED = 20261203
 CFL = 0.5
 CPU_SAMPLE_N = 256
 SEL_THRESHOLD = 0.98
+WEDGE_CFL = 0.4
 
 
 def parse():
@@ -70,6 +75,8 @@ def parse():
     ap.add_argument("--forms", default="fp64,fp64_fast,fp32",
                     help="other forms timed on the same workload (comma list, '' for none); fp64 is also the "
                          "error reference")
+    ap.add_argument("--wedge-n", type=int, default=816,
+                    help="rows of the ramp-channel lattice (3n+1 columns; 816 -> 4.0M triangles); 0 skips it")
     ap.add_argument("--cpu-sample-n", type=int, default=CPU_SAMPLE_N)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -279,6 +286,12 @@ def time_form(m, args, form, U0, W0, device, selector, barrier=None, clocks=None
     stream = torch.cuda.Stream()
     s.set_stream(stream.cuda_stream)
     s.set_state(U0, W0)
+    tune = None
+    if FORMS[form][0] == "fp32":
+        shape, tms = s.autotune()
+        tune = {"chosen_shape": shape, "ms_per_shape": [round(x, 4) for x in tms],
+                "shapes": "0: 128 thr/<=128 regs, 1: 128/<=80, 2: 128/<=64, 3: 256/<=64"}
+        s.set_state(U0, W0)
     s.launch(CFL, args.warmup)
     s.synchronize()
     if clocks:
@@ -305,7 +318,59 @@ def time_form(m, args, form, U0, W0, device, selector, barrier=None, clocks=None
     s.launch(CFL, args.steps)
     kt = s.kernel_times()
     s.kernel_timing(False)
-    return s, {"ms": ms, "U": U, "flags": flags, "stats": stats, "kt": kt, "clocks": clk}
+    return s, {"ms": ms, "U": U, "flags": flags, "stats": stats, "kt": kt, "clocks": clk, "tune": tune}
+
+
+def run_wedge(args, device, selector):
+    """The supersonic ramp channel (15 degree ramp at x = 0.5 in a 3 x 1
+    channel, jittered-lattice Delaunay mesh of 2 nx ny triangles, Mach 2.5
+    upt inflow, p_out outflow, slip walls, TENO + Rusanov, CFL 0.4): plain
+    FP64 against FP32 + learned selector, same steps, density error of the
+    learned form against the plain one."""
+    import numpy as np
+    import torch
+
+    import mallard_gb300 as mg
+    from mallard_gb300.train_selector import wedge_setup
+    ny = args.wedge_n
+    nx = 3 * ny + 1
+    t0 = time.perf_counter()
+    mesh = mg.Mesh.ramp_channel(nx, ny, 3.0, 1.0, 0.5, 15.0, 0.2, seed=SEED)
+    out = {"workload": f"ramp channel {nx}x{ny} lattice -> {mesh.n_cells} Delaunay triangles, 15 deg ramp, "
+                       f"Mach 2.5, TENO p3 + Rusanov, SSPRK3 CFL {WEDGE_CFL}, inviscid (slip walls)",
+           "cells": mesh.n_cells, "mesh_s": time.perf_counter() - t0}
+    finals = {}
+    for form, prec in (("fp64", "fp64"), ("fp32_learned", "fp32")):
+        t1 = time.perf_counter()
+        s, U0, W0 = wedge_setup(mesh, precision=prec)
+        if form == "fp32_learned":
+            s.attach_selector(selector[0], threshold=SEL_THRESHOLD)
+        setup = time.perf_counter() - t1
+        stream = torch.cuda.Stream()
+        s.set_stream(stream.cuda_stream)
+        s.set_state(U0, W0)
+        if prec == "fp32":
+            s.autotune()
+            s.set_state(U0, W0)
+        s.launch(WEDGE_CFL, args.warmup)
+        s.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        s.launch(WEDGE_CFL, args.steps)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        U, _ = s.get_state()
+        finals[form] = U
+        out[form] = {"value": mesh.n_cells * args.steps / (ms * 1e-3) / 1e6, "ms_per_step": ms / args.steps,
+                     "finite": bool(np.isfinite(U).all()) and s.status() == 0, "setup_s": setup}
+        if form == "fp32_learned":
+            out[form]["selector"] = selector_summary(selector, s.selector_stats())
+        s.close()
+    out["fp32_learned"].update(errors_vs(mesh, finals["fp32_learned"], finals["fp64"]))
+    out["speedup_learned_vs_fp64"] = out["fp32_learned"]["value"] / out["fp64"]["value"]
+    return out
 
 
 def recon_bytes_selected(solver, stats, cells):
@@ -364,6 +429,8 @@ def run_ours(args):
                        "kernel_ms_per_launch": {k: v[0] / max(v[1], 1) for k, v in kt.items() if v[1]}}
         if r["stats"]:
             forms[form]["selector"] = selector_summary(selector, r["stats"])
+        if r["tune"]:
+            forms[form]["autotune"] = r["tune"]
     # ---- the headline form
     clocks = ClockSampler(local)
     solver, r = time_form(m, args, head, U0, W0, local, selector, barrier=barrier, clocks=clocks)
@@ -433,6 +500,8 @@ def run_ours(args):
                    "kernel_ms_per_launch": {k: v[0] / max(v[1], 1) for k, v in kt.items() if v[1]}}
     if stats:
         forms[head]["selector"] = selector_summary(selector, stats)
+    if r["tune"]:
+        forms[head]["autotune"] = r["tune"]
     solver.close()
     # errors of every form against the plain FP64 path after the same W + K steps
     accuracy = None
@@ -453,6 +522,8 @@ def run_ours(args):
         fp64_roof = {"achieved_gflops": flops_cell * cells / rs / 1e9, "peak_gflops": fp64_peak,
                      "frac": flops_cell * cells / rs / 1e9 / fp64_peak, "flops_per_cell": flops_cell,
                      "peak_source": "measured FMA-chain probe on this GPU"}
+
+    wedge = run_wedge(args, local, selector or load_selector(local)) if args.wedge_n > 0 else None
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -478,6 +549,8 @@ def run_ours(args):
             line["fp64_roof"] = fp64_roof
         if accuracy:
             line["accuracy_vs_fp64"] = accuracy
+        if wedge:
+            line["wedge"] = wedge
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

@@ -116,6 +116,16 @@ typedef struct mgpu_mesh_buf mgpu_mesh_buf; /* an owning host mesh */
 
 /* Generate one of the reference's meshes (same numbering and geometry). */
 int mgpu_mesh_generate(int mesh_type, uint32_t nx, uint32_t ny, double Lx, double Ly, mgpu_mesh_buf** out);
+/* A channel [0, Lx] x [yb(x), Ly] whose lower wall rises as a ramp of
+ * ramp_deg degrees from x = x0 (no reference counterpart): an
+ * (nx+1) x (ny+1) node lattice mapped onto the channel, interior nodes
+ * jittered by up to +-jitter (< 0.5) of the local spacing (seeded),
+ * triangulated by Delaunay (quad diagonals, then Lawson edge flips):
+ * 2 nx ny triangles.  Zones:
+ * 0 interior, 1 inflow (x = 0), 2 outflow (x = Lx), 3 lower wall, 4 upper
+ * wall. */
+int mgpu_mesh_generate_ramp(uint32_t nx, uint32_t ny, double Lx, double Ly, double x0, double ramp_deg, double jitter,
+                            uint64_t seed, mgpu_mesh_buf** out);
 /* Build a mesh from connectivity (the reference's unimplemented FILE type):
  * geometry is derived with the reference's formulas. */
 int mgpu_mesh_from_connectivity(uint32_t n_nodes, const double* node_coords, uint32_t n_cells,
@@ -292,6 +302,14 @@ int mgpu_selector_stats(mgpu_ctx* ctx, uint64_t* counts);
  * and launch counts since the last reset (arrays of 5). */
 int mgpu_enable_kernel_timing(mgpu_ctx* ctx, int enable);
 int mgpu_kernel_times(mgpu_ctx* ctx, double* ms, uint32_t* launches);
+/* Autotuner: times each launch shape of the reconstruction kernel (FP32
+ * form at p = 3: 128-thread blocks with at most 128, 80 or 64 registers per
+ * thread, or 256-thread blocks with 64)
+ * on the current state, three launches each after a warm-up, and keeps the
+ * fastest for later launches.  ms[4] receives the average time per shape
+ * (0 where not applicable), best the chosen shape.  Both may be NULL.  Other
+ * forms have a single shape. */
+int mgpu_autotune(mgpu_ctx* ctx, double* ms, int* best);
 /* Algorithmic (compulsory) bytes one reconstruction launch and one full
  * stage move, from the actual table sizes. */
 int mgpu_traffic_model(mgpu_ctx* ctx, double* recon_bytes, double* stage_bytes);

@@ -84,6 +84,7 @@ def lib():
         "mgpu_last_error": (C.c_char_p, []),
         "mgpu_version": (i32, []),
         "mgpu_mesh_generate": (i32, [i32, u32, u32, f64, f64, P(vp)]),
+        "mgpu_mesh_generate_ramp": (i32, [u32, u32, f64, f64, f64, f64, f64, u64, P(vp)]),
         "mgpu_mesh_from_connectivity": (i32, [u32, vp, u32, vp, vp, vp, vp, u32, vp, vp, vp, u32, vp, vp, P(vp)]),
         "mgpu_mesh_permute_cells": (i32, [vp, u64, vp]),
         "mgpu_mesh_view": (i32, [vp, P(MeshView)]),
@@ -111,6 +112,7 @@ def lib():
         "mgpu_enable_kernel_timing": (i32, [vp, i32]),
         "mgpu_kernel_times": (i32, [vp, vp, vp]),
         "mgpu_traffic_model": (i32, [vp, P(f64), P(f64)]),
+        "mgpu_autotune": (i32, [vp, vp, P(i32)]),
         "mgpu_n_cells": (u32, [vp]),
         "mgpu_riemann_flux_batch": (i32, [i32, u32] + [vp] * 12),
         "mgpu_primitives_batch": (i32, [f64, f64, f64, f64, f64, f64, u32, vp, vp]),

@@ -120,11 +120,15 @@ MGPU_DECLARE_TENO_FLUX
 #undef MGPU_DECLARE_TENO_FLUX
 // FP32-bulk form (fp32_fast.cu): face states in FP32, flux written in FP64.
 namespace f32 {
+// shape: launch shape 0..3 (128-thread blocks with at most 128, 80 or 64
+// registers, or 256-thread blocks with 64; p = 3 only, other orders use
+// shape 0), chosen by the autotuner
+constexpr int TENO32_SHAPES = 4;
 cudaError_t launch_teno(const TenoArgs& a, int K, int M, int nq, const double* U, float* fv, uint8_t* masks,
-                        cudaStream_t s);
+                        int shape, cudaStream_t s);
 // with the learned selector's predictions (p = 3 only)
 cudaError_t launch_teno_selected(const TenoArgs& a, int K, int M, int nq, const double* U, const uint8_t* pred,
-                                 float* fv, uint8_t* masks, cudaStream_t s);
+                                 float* fv, uint8_t* masks, int shape, cudaStream_t s);
 cudaError_t launch_flux(const FluxArgs& a, const float* fv, const GasParams& g, const BcTable& bct, int rsolver,
                         int nq, cudaStream_t s);
 }  // namespace f32

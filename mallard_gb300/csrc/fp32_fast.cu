@@ -14,36 +14,24 @@
 // not.  Only the corrected weighting is built in this form.
 #include <cstdint>
 
+#include "fp_convert.cuh"
 #include "physics.cuh"
 
 namespace mgpu {
 namespace f32 {
 namespace {
 
-// FP64 -> FP32 on the integer pipe, for the state gathered from the FP64
-// stage arrays.  On GB300 the conversion instruction (F2F) issues on the
-// FP64 unit at FP64 rate (~2 per clock per SM); a funnel shift, a rebias and
-// two range guards do the same on the integer pipe.  Rounds toward zero
-// (relative error < 2^-23); magnitudes below FP32's normal range become a
-// signed zero, those above become infinity, NaN stays NaN.
-__device__ __forceinline__ float f(double x) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
-    const unsigned e = hi & 0x7ff00000u, sign = hi & 0x80000000u;
-    unsigned r = (__funnelshift_l(lo, hi, 3) & 0x7fffffffu) - 0x40000000u;
-    r = (r & 0x7fffffffu) | sign;
-    if (e <= (896u << 20)) r = sign;
-    if (e > (1150u << 20)) r = sign | 0x7f800000u | ((lo | (hi & 0xfffffu)) ? 0x400000u : 0u);
-    return __uint_as_float(r);
-}
+// FP64 -> FP32 of the state gathered from the FP64 stage arrays and of the
+// FP64 constants: round to nearest on the integer pipe (fp_convert.cuh).
+__device__ __forceinline__ float f(double x) { return f32_rn(x); }
 
 // SEL: per (cell, variable) predictions of the learned selector (pred:
 // predicted mask, bit 7 = confident).  A confident variable takes the
 // predicted stencils with equal weights and computes no smoothness
 // indicator; a cell evaluates only the stencils that one of its variables
 // needs, all of them as soon as one variable is not confident.
-template <int K, int M, int NQ, bool SEL>
-__global__ void __launch_bounds__(128) teno32_kernel(const TenoArgs a, const double* __restrict__ U,
+template <int K, int M, int NQ, bool SEL, int BS, int MINB>
+__global__ void __launch_bounds__(BS, MINB) teno32_kernel(const TenoArgs a, const double* __restrict__ U,
                                                      float* __restrict__ fv, uint8_t* __restrict__ masks,
                                                      const uint8_t* __restrict__ pred) {
     constexpr int KR = K - 1, MR = M - 1, NF = 3, S = 4;
@@ -310,28 +298,42 @@ cudaError_t flux_nq(const FluxArgs& a, const float* fv, const GasParams& g, cons
     return cudaErrorInvalidValue;
 }
 
-template <int K, int M, int NQ, bool SEL>
-cudaError_t teno_go(const TenoArgs& a, const double* U, float* fv, uint8_t* masks, const uint8_t* pred,
-                    cudaStream_t s) {
+template <int K, int M, int NQ, bool SEL, int BS, int MINB>
+cudaError_t teno_go1(const TenoArgs& a, const double* U, float* fv, uint8_t* masks, const uint8_t* pred,
+                     cudaStream_t s) {
     const long long threads = (long long)a.n_cells * 4;
-    const unsigned blocks = (unsigned)((threads + 127) / 128);
-    if (blocks) teno32_kernel<K, M, NQ, SEL><<<blocks, 128, 0, s>>>(a, U, fv, masks, pred);
+    const unsigned blocks = (unsigned)((threads + BS - 1) / BS);
+    if (blocks) teno32_kernel<K, M, NQ, SEL, BS, MINB><<<blocks, BS, 0, s>>>(a, U, fv, masks, pred);
     return cudaGetLastError();
+}
+
+// Launch shapes the autotuner chooses from: (block size, minimum resident
+// blocks per SM), i.e. register caps of 128, 80 and 64 per thread.
+template <int K, int M, int NQ, bool SEL>
+cudaError_t teno_go(const TenoArgs& a, const double* U, float* fv, uint8_t* masks, const uint8_t* pred, int shape,
+                    cudaStream_t s) {
+    switch (shape) {
+        case 0: return teno_go1<K, M, NQ, SEL, 128, 4>(a, U, fv, masks, pred, s);
+        case 1: return teno_go1<K, M, NQ, SEL, 128, 6>(a, U, fv, masks, pred, s);
+        case 2: return teno_go1<K, M, NQ, SEL, 128, 8>(a, U, fv, masks, pred, s);
+        case 3: return teno_go1<K, M, NQ, SEL, 256, 4>(a, U, fv, masks, pred, s);
+    }
+    return cudaErrorInvalidValue;
 }
 
 }  // namespace
 
 cudaError_t launch_teno(const TenoArgs& a, int K, int M, int nq, const double* U, float* fv, uint8_t* masks,
-                        cudaStream_t s) {
-    if (K == 10 && M == 20 && nq == 2) return teno_go<10, 20, 2, false>(a, U, fv, masks, nullptr, s);
-    if (K == 6 && M == 12 && nq == 1) return teno_go<6, 12, 1, false>(a, U, fv, masks, nullptr, s);
-    if (K == 3 && M == 6 && nq == 1) return teno_go<3, 6, 1, false>(a, U, fv, masks, nullptr, s);
+                        int shape, cudaStream_t s) {
+    if (K == 10 && M == 20 && nq == 2) return teno_go<10, 20, 2, false>(a, U, fv, masks, nullptr, shape, s);
+    if (K == 6 && M == 12 && nq == 1) return teno_go1<6, 12, 1, false, 128, 4>(a, U, fv, masks, nullptr, s);
+    if (K == 3 && M == 6 && nq == 1) return teno_go1<3, 6, 1, false, 128, 4>(a, U, fv, masks, nullptr, s);
     return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_teno_selected(const TenoArgs& a, int K, int M, int nq, const double* U, const uint8_t* pred,
-                                 float* fv, uint8_t* masks, cudaStream_t s) {
-    if (K == 10 && M == 20 && nq == 2) return teno_go<10, 20, 2, true>(a, U, fv, masks, pred, s);
+                                 float* fv, uint8_t* masks, int shape, cudaStream_t s) {
+    if (K == 10 && M == 20 && nq == 2) return teno_go<10, 20, 2, true>(a, U, fv, masks, pred, shape, s);
     return cudaErrorInvalidValue;
 }
 

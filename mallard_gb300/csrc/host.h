@@ -33,6 +33,8 @@ void derive_geometry(HostMesh& m);
 HostMesh make_cartesian(uint32_t nx, uint32_t ny, double Lx, double Ly);
 HostMesh make_cartesian_tri(uint32_t nx, uint32_t ny, double Lx, double Ly);
 HostMesh make_wedge(uint32_t nx, uint32_t ny, double Lx, double Ly);
+HostMesh make_ramp_channel(uint32_t nx, uint32_t ny, double Lx, double Ly, double x0, double ramp_deg, double jitter,
+                           uint64_t seed);
 
 // Quadrature rules (quadrature.cpp:23-273): points [n][dim], weights [n].
 struct QuadRule {

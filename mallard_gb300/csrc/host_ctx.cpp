@@ -781,6 +781,55 @@ int mgpu_kernel_times(mgpu_ctx* ctx, double* ms, uint32_t* launches) {
     });
 }
 
+int mgpu_autotune(mgpu_ctx* ctx, double* ms, int* best) {
+    if (int rc = need_ready(ctx)) return rc;
+    return guarded([&] {
+        const int n = ctx->single() && ctx->K == 10 ? f32::TENO32_SHAPES : 1;
+        std::vector<double> t(f32::TENO32_SHAPES, 0.0);
+        cudaEvent_t a, b;
+        ck(cudaEventCreate(&a), "cudaEventCreate");
+        ck(cudaEventCreate(&b), "cudaEventCreate");
+        const bool timing = ctx->timing;
+        ctx->timing = false;
+        int choice = 0;
+        double tbest = 1e300;
+        try {
+            for (int sh = 0; sh < n; ++sh) {
+                ctx->teno_shape = sh;
+                ctx->reconstruct(ctx->U.p, nullptr, true);  // warm-up (and the selector's predictions)
+                ck(cudaEventRecord(a, ctx->stream), "cudaEventRecord");
+                for (int r = 0; r < 3; ++r) ctx->reconstruct(ctx->U.p, nullptr, false);
+                ck(cudaEventRecord(b, ctx->stream), "cudaEventRecord");
+                ck(cudaEventSynchronize(b), "cudaEventSynchronize");
+                float f = 0.f;
+                ck(cudaEventElapsedTime(&f, a, b), "cudaEventElapsedTime");
+                t[sh] = f / 3.0;
+                if (t[sh] < tbest) {
+                    tbest = t[sh];
+                    choice = sh;
+                }
+            }
+        } catch (...) {
+            ctx->timing = timing;
+            cudaEventDestroy(a);
+            cudaEventDestroy(b);
+            throw;
+        }
+        ctx->timing = timing;
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        ctx->teno_shape = choice;
+        if (ctx->step_exec) {  // recapture with the chosen shape
+            cudaGraphExecDestroy(ctx->step_exec);
+            ctx->step_exec = nullptr;
+        }
+        if (ms)
+            for (int i = 0; i < f32::TENO32_SHAPES; ++i) ms[i] = t[i];
+        if (best) *best = choice;
+        return MGPU_OK;
+    });
+}
+
 int mgpu_traffic_model(mgpu_ctx* ctx, double* recon_bytes, double* stage_bytes) {
     if (int rc = need_ready(ctx)) return rc;
     if (recon_bytes) *recon_bytes = ctx->recon_bytes;

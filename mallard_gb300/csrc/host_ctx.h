@@ -92,6 +92,7 @@ struct mgpu_ctx {
     bool sel_on = false;
     float sel_thr_central = 0.0f, sel_thr_directional = 0.0f;
     bool sel_every_stage = false;
+    int teno_shape = 0;  // FP32 reconstruction launch shape (mgpu_autotune)
     DevArray<uint8_t> sel_wimg, pred, trusted;  // raw predictions, after the neighbour check
     DevArray<unsigned> sel_err;
     DevArray<unsigned> flags;
@@ -172,10 +173,11 @@ struct mgpu_ctx {
                 timed(4, [&] { return sel::launch_trust((int)N, cfaces.p, lr.p, pred.p, trusted.p, stream); });
             }
             timed(0, [&] {
-                return f32::launch_teno_selected(teno, K, M, nq, Uin, trusted.p, fv32.p, mask_out, stream);
+                return f32::launch_teno_selected(teno, K, M, nq, Uin, trusted.p, fv32.p, mask_out, teno_shape,
+                                                 stream);
             });
         } else if (single()) {
-            timed(0, [&] { return f32::launch_teno(teno, K, M, nq, Uin, fv32.p, mask_out, stream); });
+            timed(0, [&] { return f32::launch_teno(teno, K, M, nq, Uin, fv32.p, mask_out, teno_shape, stream); });
         } else if (cfg.recon == MGPU_RECON_TENO) {
             timed(0, [&] {
                 return fast() ? fast::launch_teno(teno, K, M, nq, cfg.teno_variant, Uin, fv.p, mask_out, stream)

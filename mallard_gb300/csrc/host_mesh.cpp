@@ -9,6 +9,7 @@
 // part of the algorithm's input.
 #include <algorithm>
 #include <cmath>
+#include <numeric>
 #include <random>
 #include <stdexcept>
 
@@ -272,11 +273,218 @@ HostMesh make_wedge(uint32_t nx, uint32_t ny, double Lx, double Ly) {
     return m;
 }
 
+// Triangulated channel [0, Lx] x [yb(x), Ly] whose lower wall rises as a
+// ramp of angle ramp_deg from x = x0 (no reference counterpart).  Nodes form
+// an (nx+1) x (ny+1) lattice mapped onto the channel; interior nodes move by
+// a seeded uniform jitter of up to +-jitter of the local spacing in x and y.
+// Each lattice quad is split along its Delaunay diagonal, then edges are
+// flipped until the triangulation is Delaunay.
+// Zones: 0 interior, 1 inflow (x = 0), 2 outflow (x = Lx), 3 lower wall,
+// 4 upper wall.
+HostMesh make_ramp_channel(uint32_t nx, uint32_t ny, double Lx, double Ly, double x0, double ramp_deg, double jitter,
+                           uint64_t seed) {
+    if (jitter < 0 || jitter >= 0.5) throw std::runtime_error("ramp channel: jitter must be in [0, 0.5)");
+    const double tn = std::tan(ramp_deg * 3.14159265358979323846 / 180.0);
+    if (!(Ly > (Lx - x0) * tn)) throw std::runtime_error("ramp channel: the ramp reaches the upper wall");
+    HostMesh m;
+    const uint32_t W = nx + 1;
+    m.n_nodes = W * (ny + 1);
+    m.node_coords.resize(2 * (size_t)m.n_nodes);
+    std::mt19937_64 rng(seed);
+    auto unit = [&]() { return (double)(rng() >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0; };  // [-1, 1)
+    const double hx = Lx / nx;
+    for (uint32_t j = 0; j <= ny; ++j)
+        for (uint32_t i = 0; i <= nx; ++i) {
+            double x = i * hx;
+            const bool inner = i > 0 && i < nx && j > 0 && j < ny;
+            const double jx = inner ? unit() * jitter : 0.0, jy = inner ? unit() * jitter : 0.0;
+            x += jx * hx;
+            const double yb = x > x0 ? (x - x0) * tn : 0.0;
+            const double hy = (Ly - yb) / ny;
+            const double y = yb + (j + jy) * hy;
+            m.node_coords[2 * ((size_t)j * W + i)] = x;
+            m.node_coords[2 * ((size_t)j * W + i) + 1] = y;
+        }
+    const double* X = m.node_coords.data();
+    // in-circle determinant of d against the counter-clockwise triangle (a, b, c)
+    auto incircle = [&](uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
+        const double adx = X[2 * a] - X[2 * d], ady = X[2 * a + 1] - X[2 * d + 1];
+        const double bdx = X[2 * b] - X[2 * d], bdy = X[2 * b + 1] - X[2 * d + 1];
+        const double cdx = X[2 * c] - X[2 * d], cdy = X[2 * c + 1] - X[2 * d + 1];
+        return (adx * adx + ady * ady) * (bdx * cdy - cdx * bdy) - (bdx * bdx + bdy * bdy) * (adx * cdy - cdx * ady) +
+               (cdx * cdx + cdy * cdy) * (adx * bdy - bdx * ady);
+    };
+    m.n_cells = 2 * nx * ny;
+    m.off_noc.resize(m.n_cells + 1);
+    m.noc.resize(3 * (size_t)m.n_cells);
+    for (uint32_t j = 0; j < ny; ++j)
+        for (uint32_t i = 0; i < nx; ++i) {
+            const uint32_t a = j * W + i, b = a + 1, c = a + W + 1, d = a + W;
+            const size_t t = 2 * ((size_t)j * nx + i);
+            uint32_t* q = &m.noc[3 * t];
+            if (incircle(a, b, c, d) > 0) {  // d inside: split along b-d
+                q[0] = a; q[1] = b; q[2] = d;
+                q[3] = b; q[4] = c; q[5] = d;
+            } else {
+                q[0] = a; q[1] = b; q[2] = c;
+                q[3] = a; q[4] = c; q[5] = d;
+            }
+        }
+    for (uint32_t c = 0; c <= m.n_cells; ++c) m.off_noc[c] = 3 * c;
+    // Lawson flips: where the lattice is sheared or compressed (over the
+    // ramp) a quad's diagonal is not enough; flip every interior edge whose
+    // opposite vertex lies inside the neighbour's circumcircle until none
+    // does.  The channel is convex, so the result is the Delaunay
+    // triangulation of the nodes (up to co-circular ties).
+    {
+        const uint32_t T = m.n_cells;
+        std::vector<int64_t> nbr(3 * (size_t)T, -1);  // neighbour triangle*3 + edge across edge k (v_k, v_k+1)
+        {
+            std::vector<std::pair<uint64_t, uint32_t>> es(3 * (size_t)T);
+            for (uint32_t t = 0; t < T; ++t)
+                for (int k = 0; k < 3; ++k) {
+                    const uint32_t p = m.noc[3 * (size_t)t + k], r = m.noc[3 * (size_t)t + (k + 1) % 3];
+                    es[3 * (size_t)t + k] = {((uint64_t)std::min(p, r) << 32) | std::max(p, r), 3 * t + (uint32_t)k};
+                }
+            std::sort(es.begin(), es.end());
+            for (size_t e = 0; e + 1 < es.size(); ++e)
+                if (es[e].first == es[e + 1].first) {
+                    nbr[es[e].second] = es[e + 1].second;
+                    nbr[es[e + 1].second] = es[e].second;
+                }
+        }
+        std::vector<uint32_t> stack(3 * (size_t)T);
+        std::iota(stack.begin(), stack.end(), 0u);
+        size_t flips = 0;
+        const size_t max_flips = 100 * (size_t)T;
+        while (!stack.empty()) {
+            const uint32_t te = stack.back();
+            stack.pop_back();
+            const int64_t ue = nbr[te];
+            if (ue < 0) continue;
+            const uint32_t t = te / 3, k = te % 3, u = (uint32_t)ue / 3, l = (uint32_t)ue % 3;
+            uint32_t* A = &m.noc[3 * (size_t)t];
+            uint32_t* B = &m.noc[3 * (size_t)u];
+            const uint32_t a = A[k], b = A[(k + 1) % 3], c = A[(k + 2) % 3];  // edge a-b, t = (a, b, c) ccw
+            const uint32_t d = B[(l + 2) % 3];                              // u = (b, a, d) ccw
+            if (!(incircle(a, b, c, d) > 0)) continue;
+            if (++flips > max_flips) throw std::runtime_error("ramp channel: edge flips did not converge");
+            // neighbours of the outer edges before the flip
+            const int64_t n_bc = nbr[3 * (size_t)t + (k + 1) % 3], n_ca = nbr[3 * (size_t)t + (k + 2) % 3];
+            const int64_t n_ad = nbr[3 * (size_t)u + (l + 1) % 3], n_db = nbr[3 * (size_t)u + (l + 2) % 3];
+            // new t = (c, a, d), new u = (d, b, c); edges: t0 c-a, t1 a-d, t2 d-c; u0 d-b, u1 b-c, u2 c-d
+            A[0] = c; A[1] = a; A[2] = d;
+            B[0] = d; B[1] = b; B[2] = c;
+            auto link = [&](uint32_t x, int64_t y) {
+                nbr[x] = y;
+                if (y >= 0) nbr[(size_t)y] = x;
+            };
+            link(3 * t + 0, n_ca);
+            link(3 * t + 1, n_ad);
+            link(3 * t + 2, 3 * (int64_t)u + 2);
+            link(3 * u + 0, n_db);
+            link(3 * u + 1, n_bc);
+            for (uint32_t x : {3 * t + 0, 3 * t + 1, 3 * u + 0, 3 * u + 1}) stack.push_back(x);
+        }
+    }
+    // faces: unique edges, numbered in order of first appearance
+    std::vector<std::pair<uint64_t, uint32_t>> edges(3 * (size_t)m.n_cells);  // (key, cell*3 + k)
+    for (uint32_t c = 0; c < m.n_cells; ++c)
+        for (int k = 0; k < 3; ++k) {
+            const uint32_t p = m.noc[3 * (size_t)c + k], r = m.noc[3 * (size_t)c + (k + 1) % 3];
+            const uint64_t key = ((uint64_t)std::min(p, r) << 32) | std::max(p, r);
+            edges[3 * (size_t)c + k] = {key, 3 * c + (uint32_t)k};
+        }
+    std::sort(edges.begin(), edges.end());
+    m.foc.assign(3 * (size_t)m.n_cells, 0);
+    std::vector<uint32_t> first;  // face -> first (cell*3+k) slot
+    std::vector<int32_t> second;
+    for (size_t e = 0; e < edges.size();) {
+        size_t g = e + 1;
+        while (g < edges.size() && edges[g].first == edges[e].first) ++g;
+        if (g - e > 2) throw std::runtime_error("ramp channel: an edge is shared by more than two triangles");
+        first.push_back(std::min(edges[e].second, g - e == 2 ? edges[e + 1].second : edges[e].second));
+        second.push_back(g - e == 2 ? (int32_t)std::max(edges[e].second, edges[e + 1].second) : -1);
+        e = g;
+    }
+    // renumber faces by first appearance
+    std::vector<uint32_t> order(first.size());
+    std::iota(order.begin(), order.end(), 0u);
+    std::sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return first[a] < first[b]; });
+    m.n_faces = (uint32_t)order.size();
+    m.cof.assign(2 * (size_t)m.n_faces, -1);
+    m.off_nof.resize(m.n_faces + 1);
+    m.nof.resize(2 * (size_t)m.n_faces);
+    for (uint32_t f = 0; f < m.n_faces; ++f) {
+        const uint32_t o = order[f];
+        const uint32_t s0 = first[o];
+        const uint32_t c0 = s0 / 3, k0 = s0 % 3;
+        m.cof[2 * (size_t)f] = (int32_t)c0;
+        m.foc[s0] = f;
+        m.nof[2 * (size_t)f] = m.noc[3 * (size_t)c0 + k0];
+        m.nof[2 * (size_t)f + 1] = m.noc[3 * (size_t)c0 + (k0 + 1) % 3];
+        if (second[o] >= 0) {
+            m.cof[2 * (size_t)f + 1] = second[o] / 3;
+            m.foc[(size_t)second[o]] = f;
+        }
+        m.off_nof[f] = 2 * f;
+    }
+    m.off_nof[m.n_faces] = 2 * m.n_faces;
+    m.off_foc.resize(m.n_cells + 1);
+    for (uint32_t c = 0; c <= m.n_cells; ++c) m.off_foc[c] = 3 * c;
+    // zones
+    std::vector<std::vector<uint32_t>> zones(5);
+    for (uint32_t f = 0; f < m.n_faces; ++f) {
+        if (m.cof[2 * (size_t)f + 1] >= 0) {
+            zones[0].push_back(f);
+            continue;
+        }
+        const uint32_t p = m.nof[2 * (size_t)f], r = m.nof[2 * (size_t)f + 1];
+        const uint32_t ip = p % W, jp = p / W, ir = r % W, jr = r / W;
+        if (ip == 0 && ir == 0) zones[1].push_back(f);
+        else if (ip == nx && ir == nx) zones[2].push_back(f);
+        else if (jp == 0 && jr == 0) zones[3].push_back(f);
+        else if (jp == ny && jr == ny) zones[4].push_back(f);
+        else throw std::runtime_error("ramp channel: boundary face off the boundary");
+    }
+    m.zone_off.assign(1, 0);
+    for (auto& z : zones) {
+        m.zone_faces.insert(m.zone_faces.end(), z.begin(), z.end());
+        m.zone_off.push_back((uint32_t)m.zone_faces.size());
+    }
+    derive_geometry(m);
+    for (uint32_t c = 0; c < m.n_cells; ++c)
+        if (!(m.cell_volume[c] > 0)) throw std::runtime_error("ramp channel: degenerate triangle");
+    return m;
+}
+
 }  // namespace mgpu
 
 using mgpu::HostMesh;
 
 extern "C" {
+
+int mgpu_mesh_generate_ramp(uint32_t nx, uint32_t ny, double Lx, double Ly, double x0, double ramp_deg, double jitter,
+                            uint64_t seed, mgpu_mesh_buf** out) {
+    if (!out || nx == 0 || ny == 0 || !(Lx > 0) || !(Ly > 0) || !(x0 >= 0) || !(x0 < Lx)) {
+        mgpu::set_error("mgpu_mesh_generate_ramp: invalid arguments");
+        return MGPU_ERR_ARG;
+    }
+    try {
+        auto* b = new mgpu_mesh_buf();
+        try {
+            b->m = mgpu::make_ramp_channel(nx, ny, Lx, Ly, x0, ramp_deg, jitter, seed);
+        } catch (...) {
+            delete b;
+            throw;
+        }
+        *out = b;
+        return MGPU_OK;
+    } catch (const std::exception& e) {
+        mgpu::set_error(e.what());
+        return MGPU_ERR_ARG;
+    }
+}
 
 int mgpu_mesh_generate(int mesh_type, uint32_t nx, uint32_t ny, double Lx, double Ly, mgpu_mesh_buf** out) {
     if (!out || nx == 0 || ny == 0 || !(Lx > 0) || !(Ly > 0)) {

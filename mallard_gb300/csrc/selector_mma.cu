@@ -21,6 +21,7 @@
 
 #include <cuda_bf16.h>
 
+#include "fp_convert.cuh"
 #include "selector.cuh"
 #include "selector_launch.h"
 
@@ -141,9 +142,10 @@ __device__ __forceinline__ uint4 pack8(const float* x) {
     return u;
 }
 
-// FP64 -> FP32 of a state value, round to nearest
+// FP64 -> FP32 of a state value, round to nearest, on the integer pipe
+// (the conversion instruction would make this kernel FP64-bound)
 struct ToFloatRN {
-    __device__ float operator()(double x) const { return __double2float_rn(x); }
+    __device__ float operator()(double x) const { return f32_rn(x); }
 };
 
 // SRC 0: feature rows from X [n][IN]; SRC 1: features of cells 0..n-1 of a

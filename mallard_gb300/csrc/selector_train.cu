@@ -7,6 +7,7 @@
 // sums in row order), so a training run is deterministic for a given seed.
 #include <cstdint>
 
+#include "fp_convert.cuh"
 #include "selector.cuh"
 #include "selector_launch.h"
 
@@ -14,9 +15,9 @@ namespace mgpu {
 namespace sel {
 namespace {
 
-// FP64 -> FP32, round to nearest (the harvest path is not throughput bound)
+// FP64 -> FP32, round to nearest, on the integer pipe
 struct ToFloatRN {
-    __device__ float operator()(double x) const { return __double2float_rn(x); }
+    __device__ float operator()(double x) const { return f32_rn(x); }
 };
 
 // One thread per (selected cell, variable): feature row and class label.

@@ -66,6 +66,15 @@ class Mesh:
         return cls(h)
 
     @classmethod
+    def ramp_channel(cls, nx, ny, Lx=3.0, Ly=1.0, x0=0.5, ramp_deg=15.0, jitter=0.2, seed=0):
+        """Jittered-lattice Delaunay triangulation of a channel with a ramp
+        (2 nx ny triangles); zones interior, inflow, outflow, wall, top."""
+        h = C.c_void_p()
+        N.check(N.lib().mgpu_mesh_generate_ramp(nx, ny, float(Lx), float(Ly), float(x0), float(ramp_deg),
+                                                float(jitter), int(seed), C.byref(h)))
+        return cls(h, ["interior", "inflow", "outflow", "wall", "top"])
+
+    @classmethod
     def from_connectivity(cls, node_coords, offsets_nodes_of_cell, nodes_of_cell, offsets_faces_of_cell,
                           faces_of_cell, offsets_nodes_of_face, nodes_of_face, cells_of_face, zone_offsets,
                           zone_faces, zone_names=None):

@@ -255,6 +255,14 @@ class Solver:
         keys = ("cells", "confident_cells", "confident_variables", "stencils_evaluated", "stencils_full", "error")
         return {k: int(c[i]) for i, k in enumerate(keys)}
 
+    def autotune(self):
+        """Pick the fastest launch shape of the reconstruction kernel on the
+        current state; returns (chosen shape, ms per shape)."""
+        ms = np.zeros(4)
+        best = C.c_int()
+        N.check(self._lib.mgpu_autotune(self._h, N.ptr(ms), C.byref(best)))
+        return best.value, ms
+
     def traffic_model(self):
         r, s = C.c_double(), C.c_double()
         N.check(self._lib.mgpu_traffic_model(self._h, C.byref(r), C.byref(s)))

@@ -4,13 +4,15 @@
 
 Training pairs are harvested from the FP64 solver's own runs (corrected
 TENO, p = 3, HLLC, SSPRK3, CFL 0.5) at seeded random initial states of
-three problem families:
+four problem families:
   * Sod-type shock tubes on a 1000 x 8 strip of triangles (symmetry
     boundaries), random left/right states and diaphragm position;
   * two-dimensional four-quadrant Riemann problems on the unit square
     (transmissive boundaries), random quadrant states and split point,
     harvested over the first steps;
-  * cylindrical explosions (random centre, radius and states).
+  * cylindrical explosions (random centre, radius and states);
+  * supersonic flow through a ramp channel (Delaunay mesh, random ramp
+    angle and Mach number, Rusanov flux), harvested every 100 steps.
 Each harvest keeps every cell where some variable leaves the central
 stencil and a fraction of the all-central cells.  The network is then
 trained with minibatch Adam by the library's own kernels.
@@ -94,6 +96,41 @@ def harvest_all(sel, seed=0, quick=False, log=print):
         U, W = state_from_primitives(rho, 0 * rho, 0 * rho, p, **GAS)
         rows += _run_and_harvest(sel, sq, "extrapolation", U, W, 120 if quick else 240, 30, 0.05, 200 + i)
     log(f"  + explosions: {rows} rows")
+    # supersonic ramp channels (Rusanov flux, inflow / outflow / slip walls)
+    for i in range(1 if quick else 4):
+        rows += _run_wedge(sel, r, quick, 300 + i)
+    log(f"  + wedges: {rows} rows")
+    return rows
+
+
+def wedge_setup(mesh, mach=2.5, rho=1.4, p=1.0, riemann="Rusanov", precision="fp64_fast"):
+    """Solver and initial state of the supersonic ramp channel: uniform inflow
+    state everywhere, "upt" inflow, "p_out" outflow, slip walls."""
+    R = GAS["p_ref"] / (GAS["T_ref"] * GAS["rho_ref"])
+    u = mach * float(np.sqrt(GAS["gamma"] * p / rho))
+    T = p / (rho * R)
+    blist = [{"name": "inflow", "type": "upt", "u": [u, 0.0], "p": p, "T": T},
+             {"name": "outflow", "type": "p_out", "p": p},
+             {"name": "wall", "type": "wall_adiabatic"}, {"name": "top", "type": "wall_adiabatic"}]
+    s = Solver(mesh, face_reconstruction="TENO", basis_type="legendre", basis_order=3, riemann_solver=riemann,
+               boundaries=blist, teno_variant="corrected", precision=precision, **GAS)
+    n = mesh.n_cells
+    U, W = state_from_primitives(np.full(n, rho), np.full(n, u), np.zeros(n), np.full(n, p), **GAS)
+    return s, U, W
+
+
+def _run_wedge(sel, r, quick, seed):
+    mesh = Mesh.ramp_channel(150 if quick else 240, 50 if quick else 80, 3.0, 1.0, 0.5, r.uniform(8.0, 20.0), 0.2,
+                             seed=seed)
+    s, U, W = wedge_setup(mesh, mach=r.uniform(1.8, 3.5))
+    rows = 0
+    with s:
+        s.set_state(U, W)
+        for k in range(4):
+            s.run(0.4, 50 if quick else 100)
+            if s.status() != 0:
+                break
+            rows += sel.harvest(s, keep_central=0.05, seed=seed * 1000 + k)
     return rows
 
 

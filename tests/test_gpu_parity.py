@@ -239,3 +239,36 @@ def test_nan_state_is_flagged():
     s.set_state(U, W)
     s.take_step(1e-4)
     assert s.status() & 1
+
+
+def test_ramp_channel_wedge_parity():
+    """The supersonic ramp channel (Delaunay mesh from the library's
+    generator; upt inflow, p_out outflow, slip walls; TENO + Rusanov): one
+    residual and 20 steps against the oracle."""
+    from mallard_gb300.train_selector import wedge_setup
+    from cases import GAS
+    from oracle import OracleCase, OracleMesh
+    m = mg.Mesh.ramp_channel(36, 12, 3.0, 1.0, 0.5, 15.0, 0.2, seed=11)
+    m.permute_cells(3)
+    s, U, W = wedge_setup(m, mach=2.5, precision="fp64")
+    oc = OracleCase(OracleMesh.from_arrays(m), recon="TENO", basis="legendre", poly_order=3, riemann="Rusanov",
+                    **GAS)
+    oc.set_teno_variant(1)
+    R = GAS["p_ref"] / (GAS["T_ref"] * GAS["rho_ref"])
+    u = 2.5 * np.sqrt(GAS["gamma"] * 1.0 / 1.4)
+    oc.add_boundary(m.zone_index("inflow"), "upt", (u, 0.0, 1.0, 1.0 / (1.4 * R)))
+    oc.add_boundary(m.zone_index("outflow"), "p_out", (1.0,))
+    oc.add_boundary(m.zone_index("wall"), "wall_adiabatic")
+    oc.add_boundary(m.zone_index("top"), "wall_adiabatic")
+    # a perturbed state so that every stencil decision is exercised
+    r = np.random.default_rng(4)
+    Up = U * (1 + 0.02 * r.standard_normal(U.shape))
+    assert_close(s.calc_rhs(Up), oc.calc_rhs(Up), STAGE_TOL, what="ramp channel residual")
+    s.set_state(U, W)
+    oc.set_state(U, W)
+    s.run(0.4, 20)
+    oc.run(0.4, 20)
+    Ug, _ = s.get_state()
+    Uo, _ = oc.get_state()
+    assert_close(Ug, Uo, RUN_TOL, what="ramp channel 20 steps")
+    s.close()
