@@ -295,6 +295,39 @@ int mgpu_set_selector_every_stage(mgpu_ctx* ctx, int every_stage);
  * [3] stencils evaluated, [4] stencils full TENO evaluates, [5] error flag. */
 int mgpu_selector_stats(mgpu_ctx* ctx, uint64_t* counts);
 
+/* ---- batched form -------------------------------------------------------
+ * No counterpart in the reference.  Many independent cases on a few meshes
+ * (n_groups <= 8; group g holds cases_per_group[g] cases on meshes[g]),
+ * stepped together: one launch per kernel covers every case, each mesh's
+ * TENO tables and face geometry exist once and are shared by its cases, and
+ * every case has its own time step (its own CFL reduction), time and status
+ * flags.  The FP32 form of corrected TENO at p = 3 only (cfg->precision =
+ * MGPU_PREC_FP32); the boundary list applies to every case's zones.
+ * Cases are addressed as (group, index within the group); states are in
+ * the caller's cell order of the group's mesh. */
+typedef struct mgpu_batch mgpu_batch;
+int mgpu_batch_create(uint32_t n_groups, const mgpu_mesh* const* meshes, const uint32_t* cases_per_group,
+                      const mgpu_config* cfg, mgpu_batch** out);
+int mgpu_batch_add_boundary(mgpu_batch* b, uint32_t zone, int type, const double* data, int n_data);
+int mgpu_batch_finalize(mgpu_batch* b);
+void mgpu_batch_destroy(mgpu_batch* b);
+uint32_t mgpu_batch_n_cases(const mgpu_batch* b);
+/* Also resets the case's time and status flags; prim may be NULL. */
+int mgpu_batch_set_state(mgpu_batch* b, uint32_t group, uint32_t index, const double* U, const double* prim);
+int mgpu_batch_get_state(mgpu_batch* b, uint32_t group, uint32_t index, double* U, double* prim);
+/* n_steps CFL steps of every case, each a replay of one captured CUDA graph
+ * (spectral radius and dt per case, three SSPRK3 stages); asynchronous. */
+int mgpu_batch_run(mgpu_batch* b, double cfl, uint32_t n_steps);
+int mgpu_batch_synchronize(mgpu_batch* b);
+/* Per case (global order: group 0's cases first): status flags (bit 0
+ * non-finite state, bit 1 invalid dt) and time; either may be NULL. */
+int mgpu_batch_status(mgpu_batch* b, uint32_t* flags, double* times);
+/* Autotuner of the batched reconstruction: times the 4 launch shapes x 4
+ * grid sizes (one thread per item, or a persistent grid of 2, 4, 8 CTAs per
+ * SM) on the current states and keeps the fastest.  ms[16] receives the
+ * times (shape-major); any output may be NULL. */
+int mgpu_batch_autotune(mgpu_batch* b, double* ms, int* shape, int* blocks_per_sm);
+
 /* Diagnostics for measurement.  Kernel timing brackets every launch of the
  * reconstruction, flux, update, CFL and selector kernels with CUDA events on
  * the launching stream; mgpu_kernel_times returns, per kernel class

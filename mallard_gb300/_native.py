@@ -113,6 +113,17 @@ def lib():
         "mgpu_kernel_times": (i32, [vp, vp, vp]),
         "mgpu_traffic_model": (i32, [vp, P(f64), P(f64)]),
         "mgpu_autotune": (i32, [vp, vp, P(i32)]),
+        "mgpu_batch_create": (i32, [u32, vp, vp, P(Config), P(vp)]),
+        "mgpu_batch_add_boundary": (i32, [vp, u32, i32, vp, i32]),
+        "mgpu_batch_finalize": (i32, [vp]),
+        "mgpu_batch_destroy": (None, [vp]),
+        "mgpu_batch_n_cases": (u32, [vp]),
+        "mgpu_batch_set_state": (i32, [vp, u32, u32, vp, vp]),
+        "mgpu_batch_get_state": (i32, [vp, u32, u32, vp, vp]),
+        "mgpu_batch_run": (i32, [vp, f64, u32]),
+        "mgpu_batch_synchronize": (i32, [vp]),
+        "mgpu_batch_status": (i32, [vp, vp, vp]),
+        "mgpu_batch_autotune": (i32, [vp, vp, P(i32), P(i32)]),
         "mgpu_n_cells": (u32, [vp]),
         "mgpu_riemann_flux_batch": (i32, [i32, u32] + [vp] * 12),
         "mgpu_primitives_batch": (i32, [f64, f64, f64, f64, f64, f64, u32, vp, vp]),

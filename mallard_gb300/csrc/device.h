@@ -132,6 +132,52 @@ cudaError_t launch_teno_selected(const TenoArgs& a, int K, int M, int nq, const 
 cudaError_t launch_flux(const FluxArgs& a, const float* fv, const GasParams& g, const BcTable& bct, int rsolver,
                         int nq, cudaStream_t s);
 }  // namespace f32
+// ---------------------------------------------------------------------------
+// Batched form: many cases on a few meshes in one launch per kernel.
+// The cases of group g share one mesh (its tables and geometry, in the
+// per-group argument blocks below); their state and face rows are
+// interleaved per 8-row tile: row(c) = ubase + ((c / 8) C + case) 8 + c % 8.
+// A kernel's threads run over all groups in order; group g starts at the
+// thread index in the *0 arrays.  The kernels are persistent: any grid
+// size works, each thread strides over the whole range.
+// ---------------------------------------------------------------------------
+constexpr int MAX_GROUPS = 8;
+struct BatchLaunch {
+    int n_groups;
+    unsigned C[MAX_GROUPS];          // cases in the group
+    unsigned case0[MAX_GROUPS];      // global index of its first case
+    int n_cells[MAX_GROUPS], n_faces[MAX_GROUPS];  // cells, flux faces
+    unsigned long long ubase[MAX_GROUPS], fbase[MAX_GROUPS];
+    long long cell0[MAX_GROUPS + 1];  // thread ranges: (case, cell)
+    long long teno0[MAX_GROUPS + 1];  //                (case, cell, variable)
+    long long face0[MAX_GROUPS + 1];  //                (case, flux face)
+    // per-group argument blocks in device memory (tables, geometry)
+    const TenoArgs* teno;
+    const FluxArgs* flux;
+    const UpdateArgs* upd;
+    const SpecArgs* spec;
+    // state of all cases
+    double *U, *Ut, *W, *prim, *snd, *G;
+    float* fv;
+    double *dt, *t;                  // per case
+    unsigned long long* rmax;        // per case
+    unsigned* flags;                 // per case
+};
+
+namespace f32 {
+cudaError_t launch_teno_batch(const BatchLaunch& b, const double* U, int shape, int blocks_per_sm, cudaStream_t s);
+cudaError_t launch_flux_batch(const BatchLaunch& b, const GasParams& g, const BcTable& bct, int rsolver, int nq,
+                              const double* U, cudaStream_t s);
+}  // namespace f32
+cudaError_t launch_update_batch(const BatchLaunch& b, const GasParams& g, int stage, cudaStream_t s);
+cudaError_t launch_spectral_batch(const BatchLaunch& b, cudaStream_t s);
+cudaError_t launch_dt_batch(const BatchLaunch& b, int n_cases, double cfl, cudaStream_t s);
+// caller-order rows of one case <-> its interleaved internal rows
+cudaError_t launch_batch_rows(int n, int width, const uint32_t* perm_old, const double* src, double* dst,
+                              unsigned long long ubase, unsigned C, unsigned cs, bool to_batch, cudaStream_t s);
+cudaError_t launch_batch_prims(int n, const GasParams& g, double* U, double* prim, double* snd,
+                               unsigned long long ubase, unsigned C, unsigned cs, cudaStream_t s);
+
 // kernels.cu
 cudaError_t launch_first_order(int n_faces, const int2* lr, const double* U, double* fv, cudaStream_t s);
 cudaError_t launch_update(const UpdateArgs& a, const GasParams& g, int stage, bool fast, cudaStream_t s);

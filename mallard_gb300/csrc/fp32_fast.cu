@@ -30,24 +30,35 @@ __device__ __forceinline__ float f(double x) { return f32_rn(x); }
 // predicted stencils with equal weights and computes no smoothness
 // indicator; a cell evaluates only the stencils that one of its variables
 // needs, all of them as soon as one variable is not confident.
-template <int K, int M, int NQ, bool SEL, int BS, int MINB>
-__global__ void __launch_bounds__(BS, MINB) teno32_kernel(const TenoArgs a, const double* __restrict__ U,
-                                                     float* __restrict__ fv, uint8_t* __restrict__ masks,
-                                                     const uint8_t* __restrict__ pred) {
+// Row indices of state and face arrays.  Ix1: one case, rows in the mesh's
+// own order.  IxB: case cs of a batch group of C cases sharing one mesh,
+// rows interleaved per 8-row tile: row(c) = base + ((c / 8) C + cs) 8 + c % 8.
+struct Ix1 {
+    __device__ __forceinline__ size_t u(size_t c) const { return c; }
+    __device__ __forceinline__ size_t f(size_t fi) const { return fi; }
+};
+struct IxB {
+    size_t ubase, fbase;
+    unsigned C, cs;
+    __device__ __forceinline__ size_t u(size_t c) const { return ubase + (((c >> 3) * C + cs) << 3) + (c & 7); }
+    __device__ __forceinline__ size_t f(size_t fi) const { return fbase + (((fi >> 3) * C + cs) << 3) + (fi & 7); }
+};
+
+// Reconstruction of variable v of one cell.  live: lanes of the warp whose
+// cells exist (the four lanes of a cell share its fate).
+template <int K, int M, int NQ, bool SEL, class IX>
+__device__ __forceinline__ void teno32_cell(const TenoArgs& a, const double* __restrict__ U, float* __restrict__ fv,
+                                            uint8_t* __restrict__ masks, const uint8_t* __restrict__ pred, int cell,
+                                            int v, unsigned live, const IX& ix) {
     constexpr int KR = K - 1, MR = M - 1, NF = 3, S = 4;
     constexpr int GJ = (MR + 3) / 4, GP = (MR * KR + 3) / 4, GF = (NF * NQ * KR + 3) / 4;
-    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
-    const int cell = gt >> 2, v = gt & 3;
-    // lanes of cells that exist (the four lanes of a cell share its fate)
-    const unsigned live = __ballot_sync(0xffffffffu, cell < a.n_cells);
-    if (cell >= a.n_cells) return;
     const int tile = cell >> 3, lane = cell & 7;
-    const float uc = f(U[(size_t)cell * NC + v]);
+    const float uc = f(U[ix.u(cell) * NC + v]);
     const unsigned sm = a.smask[cell];
     unsigned need = sm, pm = 0;
     bool conf = false;
     if (SEL) {
-        const unsigned p = pred[(size_t)cell * NC + v];
+        const unsigned p = pred[ix.u(cell) * NC + v];
         pm = p & sm & 0xFu;
         conf = (p & 0x80u) && pm;
         unsigned my = conf ? pm : sm;
@@ -73,7 +84,7 @@ __global__ void __launch_bounds__(BS, MINB) teno32_kernel(const TenoArgs a, cons
             const uint32_t id[4] = {n.x, n.y, n.z, n.w};
 #pragma unroll
             for (int e = 0; e < 4; ++e)
-                if (g * 4 + e < MR) d[g * 4 + e] = f(__ldg(U + (size_t)id[e] * NC + v)) - uc;
+                if (g * 4 + e < MR) d[g * 4 + e] = f(__ldg(U + ix.u(id[e]) * NC + v)) - uc;
         }
         // coefficients = (P x areas) . d, accumulated over the stencil in order
         const float4* Pp = reinterpret_cast<const float4*>(a.P4) + ((size_t)(tile * S + s) * GP) * TILE + lane;
@@ -145,7 +156,7 @@ __global__ void __launch_bounds__(BS, MINB) teno32_kernel(const TenoArgs a, cons
         for (int s = 1; s < S; ++s) w[s] = ((mask >> s) & 1u) ? share : 0.0f;
     }
     }
-    if (masks) masks[(size_t)cell * NC + v] = (uint8_t)mask;
+    if (masks) masks[ix.u(cell) * NC + v] = (uint8_t)mask;
     // blended coefficients
     float c[KR];
 #pragma unroll
@@ -177,9 +188,20 @@ __global__ void __launch_bounds__(BS, MINB) teno32_kernel(const TenoArgs a, cons
             float out = uc;
 #pragma unroll
             for (int k = 0; k < KR; ++k) out = fmaf(c[k], phi[(fl * NQ + q) * KR + k], out);
-            fv[((fi * NQ + q) * 2 + side) * NC + v] = out;
+            fv[((ix.f(fi) * NQ + q) * 2 + side) * NC + v] = out;
         }
     }
+}
+
+template <int K, int M, int NQ, bool SEL, int BS, int MINB>
+__global__ void __launch_bounds__(BS, MINB) teno32_kernel(const TenoArgs a, const double* __restrict__ U,
+                                                          float* __restrict__ fv, uint8_t* __restrict__ masks,
+                                                          const uint8_t* __restrict__ pred) {
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const int cell = gt >> 2, v = gt & 3;
+    const unsigned live = __ballot_sync(0xffffffffu, cell < a.n_cells);
+    if (cell >= a.n_cells) return;
+    teno32_cell<K, M, NQ, SEL>(a, U, fv, masks, pred, cell, v, live, Ix1{});
 }
 
 // Primitive recovery of a face state: FP32, or FP64 when the internal energy
@@ -198,11 +220,10 @@ __device__ __forceinline__ void primitives_guarded(const GasParams& g, const flo
     }
 }
 
-template <int RS, int NQ>
-__global__ void __launch_bounds__(128) flux32_kernel(const FluxArgs a, const float* __restrict__ fv,
-                                                     const GasParams g, const BcTable bct) {
-    const int fi = blockIdx.x * blockDim.x + threadIdx.x;
-    if (fi >= a.n_faces) return;
+// Flux of one face (local index fi) into G.
+template <int RS, int NQ, class IX>
+__device__ __forceinline__ void flux32_face(const FluxArgs& a, const float* __restrict__ fv, const GasParams& g,
+                                            const BcTable& bct, int fi, const IX& ix) {
     const int2 lr = a.lr[fi];
     const double2 nn = a.nrm[fi];
     const float n[2] = {f(nn.x), f(nn.y)};
@@ -212,7 +233,7 @@ __global__ void __launch_bounds__(128) flux32_kernel(const FluxArgs a, const flo
     float F[4] = {0.0f, 0.0f, 0.0f, 0.0f};
 #pragma unroll
     for (int q = 0; q < NQ; ++q) {
-        const float4* fq = reinterpret_cast<const float4*>(fv + ((size_t)fi * NQ + q) * 8);
+        const float4* fq = reinterpret_cast<const float4*>(fv + (ix.f(fi) * NQ + q) * 8);
         float cl[4], cr[4], pl[5], pr[5], Ft[4];
         {
             const float4 x = fq[0];
@@ -224,10 +245,10 @@ __global__ void __launch_bounds__(128) flux32_kernel(const FluxArgs a, const flo
         }
         if (!admissible(g, cl))
 #pragma unroll
-            for (int i = 0; i < 4; i++) cl[i] = f(a.U[(size_t)lr.x * NC + i]);
+            for (int i = 0; i < 4; i++) cl[i] = f(a.U[ix.u(lr.x) * NC + i]);
         if (type < 0 && !admissible(g, cr))
 #pragma unroll
-            for (int i = 0; i < 4; i++) cr[i] = f(a.U[(size_t)lr.y * NC + i]);
+            for (int i = 0; i < 4; i++) cr[i] = f(a.U[ix.u(lr.y) * NC + i]);
         primitives_guarded(g, cl, pl);
         if (type == MGPU_BC_WALL_ADIABATIC) {
             Ft[0] = 0.0f;
@@ -276,9 +297,17 @@ __global__ void __launch_bounds__(128) flux32_kernel(const FluxArgs a, const flo
         for (int i = 0; i < 4; i++) F[i] = fmaf(f(a.qw[q]), Ft[i], F[i]);
     }
     const double area = a.area[fi];
-    double2* Gf = reinterpret_cast<double2*>(a.G + (size_t)fi * 4);
+    double2* Gf = reinterpret_cast<double2*>(a.G + ix.f(fi) * 4);
     Gf[0] = make_double2(area * (double)(F[0] * 0.5f), area * (double)(F[1] * 0.5f));
     Gf[1] = make_double2(area * (double)(F[2] * 0.5f), area * (double)(F[3] * 0.5f));
+}
+
+template <int RS, int NQ>
+__global__ void __launch_bounds__(128) flux32_kernel(const FluxArgs a, const float* __restrict__ fv,
+                                                     const GasParams g, const BcTable bct) {
+    const int fi = blockIdx.x * blockDim.x + threadIdx.x;
+    if (fi >= a.n_faces) return;
+    flux32_face<RS, NQ>(a, fv, g, bct, fi, Ix1{});
 }
 
 template <int RS, int NQ>
@@ -321,7 +350,94 @@ cudaError_t teno_go(const TenoArgs& a, const double* U, float* fv, uint8_t* mask
     return cudaErrorInvalidValue;
 }
 
+// group of a batch thread index
+__device__ __forceinline__ int batch_group(const long long* start, int n, long long gt) {
+    int g = 0;
+    while (g + 1 < n && gt >= start[g + 1]) ++g;
+    return g;
+}
+
+// Batched reconstruction: thread (case, cell, variable), 32 consecutive
+// threads = one 8-cell tile of one case, consecutive tiles = the same mesh
+// tile of consecutive cases (so a table tile is reused from cache).
+template <int K, int M, int NQ, int BS, int MINB>
+__global__ void __launch_bounds__(BS, MINB) teno32_batch_kernel(const BatchLaunch b, const double* __restrict__ U) {
+    const long long total = b.teno0[b.n_groups];
+    for (long long gt = (long long)blockIdx.x * BS + threadIdx.x; gt < total; gt += (long long)gridDim.x * BS) {
+        const int gi = batch_group(b.teno0, b.n_groups, gt);
+        const long long t = gt - b.teno0[gi];
+        const int v = (int)(t & 3), lane8 = (int)((t >> 2) & 7);
+        const long long tc = t >> 5;
+        const unsigned C = b.C[gi];
+        const IxB ix{b.ubase[gi], b.fbase[gi], C, (unsigned)(tc % C)};
+        const int cell = (int)(tc / C) * 8 + lane8;
+        const unsigned live = __ballot_sync(0xffffffffu, cell < b.n_cells[gi]);
+        if (cell >= b.n_cells[gi]) continue;
+        teno32_cell<K, M, NQ, false>(b.teno[gi], U, b.fv, nullptr, nullptr, cell, v, live, ix);
+    }
+}
+
+// Batched face flux: thread (case, flux face).
+template <int RS, int NQ>
+__global__ void __launch_bounds__(128) flux32_batch_kernel(const BatchLaunch b, const GasParams g, const BcTable bct,
+                                                           const double* __restrict__ U) {
+    const long long total = b.face0[b.n_groups];
+    for (long long gt = (long long)blockIdx.x * 128 + threadIdx.x; gt < total; gt += (long long)gridDim.x * 128) {
+        const int gi = batch_group(b.face0, b.n_groups, gt);
+        const long long t = gt - b.face0[gi];
+        const long long tc = t >> 3;
+        const unsigned C = b.C[gi];
+        const int fi = (int)(tc / C) * 8 + (int)(t & 7);
+        if (fi >= b.n_faces[gi]) continue;
+        const IxB ix{b.ubase[gi], b.fbase[gi], C, (unsigned)(tc % C)};
+        FluxArgs a = b.flux[gi];
+        a.U = U;
+        a.G = b.G;
+        flux32_face<RS, NQ>(a, b.fv, g, bct, fi, ix);
+    }
+}
+
+template <int K, int M, int NQ, int BS, int MINB>
+cudaError_t teno_batch_go(const BatchLaunch& b, const double* U, int blocks_per_sm, cudaStream_t s) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long need = (b.teno0[b.n_groups] + BS - 1) / BS;
+    long long blocks = blocks_per_sm > 0 ? (long long)sms * blocks_per_sm : need;
+    if (blocks > need) blocks = need;
+    if (blocks > 0) teno32_batch_kernel<K, M, NQ, BS, MINB><<<(unsigned)blocks, BS, 0, s>>>(b, U);
+    return cudaGetLastError();
+}
+
 }  // namespace
+
+cudaError_t launch_teno_batch(const BatchLaunch& b, const double* U, int shape, int blocks_per_sm, cudaStream_t s) {
+    switch (shape) {
+        case 0: return teno_batch_go<10, 20, 2, 128, 4>(b, U, blocks_per_sm, s);
+        case 1: return teno_batch_go<10, 20, 2, 128, 6>(b, U, blocks_per_sm, s);
+        case 2: return teno_batch_go<10, 20, 2, 128, 8>(b, U, blocks_per_sm, s);
+        case 3: return teno_batch_go<10, 20, 2, 256, 4>(b, U, blocks_per_sm, s);
+    }
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_flux_batch(const BatchLaunch& b, const GasParams& g, const BcTable& bct, int rsolver, int nq,
+                              const double* U, cudaStream_t s) {
+    if (nq != 2) return cudaErrorInvalidValue;
+    const long long blocks = (b.face0[b.n_groups] + 127) / 128;
+    if (blocks == 0) return cudaSuccess;
+    switch (rsolver) {
+        case MGPU_RIEMANN_RUSANOV:
+            flux32_batch_kernel<MGPU_RIEMANN_RUSANOV, 2><<<(unsigned)blocks, 128, 0, s>>>(b, g, bct, U);
+            break;
+        case MGPU_RIEMANN_HLL: flux32_batch_kernel<MGPU_RIEMANN_HLL, 2><<<(unsigned)blocks, 128, 0, s>>>(b, g, bct, U); break;
+        case MGPU_RIEMANN_HLLC:
+            flux32_batch_kernel<MGPU_RIEMANN_HLLC, 2><<<(unsigned)blocks, 128, 0, s>>>(b, g, bct, U);
+            break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
 
 cudaError_t launch_teno(const TenoArgs& a, int K, int M, int nq, const double* U, float* fv, uint8_t* masks,
                         int shape, cudaStream_t s) {

@@ -58,19 +58,33 @@ __device__ __forceinline__ double sound_speed(double gamma, double rho, const do
     return sqrt(gamma * W[2] / rho);
 }
 
+// Row indices (see fp32_fast.cu): one case, or case cs of a batch group
+// whose rows are interleaved per 8-row tile.
+struct Ix1 {
+    __device__ __forceinline__ size_t u(size_t c) const { return c; }
+    __device__ __forceinline__ size_t f(size_t fi) const { return fi; }
+};
+struct IxB {
+    size_t ubase, fbase;
+    unsigned C, cs;
+    __device__ __forceinline__ size_t u(size_t c) const { return ubase + (((c >> 3) * C + cs) << 3) + (c & 7); }
+    __device__ __forceinline__ size_t f(size_t fi) const { return fbase + (((fi >> 3) * C + cs) << 3) + (fi & 7); }
+};
+
 // FAST: residual times a precomputed 1/volume and primitives_rcp (the
 // FP64-fast and FP32 forms); otherwise the reference's divisions.
-template <int STAGE, bool FAST>
-__global__ void __launch_bounds__(256) update_kernel(const UpdateArgs a, const GasParams g) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= a.n_cells) return;
+// Cell c (local index) of one case; dt and the NaN flag are the case's.
+template <int STAGE, bool FAST, class IX>
+__device__ __forceinline__ void update_cell(const UpdateArgs& a, const GasParams& g, int c, const IX& ix,
+                                            const double* dtp, unsigned* flag) {
+    const size_t row = ix.u(c);
     const int4 gl = a.gat[c];
     const int ent[4] = {gl.x, gl.y, gl.z, gl.w};
     double r[4] = {0.0, 0.0, 0.0, 0.0};
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
         if (ent[e] < 0) break;
-        const double2* Gf = reinterpret_cast<const double2*>(a.G + (size_t)(ent[e] >> 1) * 4);
+        const double2* Gf = reinterpret_cast<const double2*>(a.G + ix.f((size_t)(ent[e] >> 1)) * 4);
         const double2 g0 = Gf[0], g1 = Gf[1];
         const double x[4] = {g0.x, g0.y, g1.x, g1.y};
         if (ent[e] & 1) {
@@ -92,16 +106,16 @@ __global__ void __launch_bounds__(256) update_kernel(const UpdateArgs a, const G
     }
     double2* out2;
     if (STAGE == 0) {
-        out2 = reinterpret_cast<double2*>(a.rhs + (size_t)c * 4);
+        out2 = reinterpret_cast<double2*>(a.rhs + row * 4);
         out2[0] = make_double2(r[0], r[1]);
         out2[1] = make_double2(r[2], r[3]);
         return;
     }
-    const double dt = *a.dt;
-    const double2* U2 = reinterpret_cast<const double2*>(a.U + (size_t)c * 4);
-    const double2* W2 = reinterpret_cast<const double2*>(a.W + (size_t)c * 4);
-    double2* Ut2 = reinterpret_cast<double2*>(a.Ut + (size_t)c * 4);
-    double2* Wo2 = reinterpret_cast<double2*>(a.W + (size_t)c * 4);
+    const double dt = *dtp;
+    const double2* U2 = reinterpret_cast<const double2*>(a.U + row * 4);
+    const double2* W2 = reinterpret_cast<const double2*>(a.W + row * 4);
+    double2* Ut2 = reinterpret_cast<double2*>(a.Ut + row * 4);
+    double2* Wo2 = reinterpret_cast<double2*>(a.W + row * 4);
     if (STAGE == 1) {
         const double2 u0 = U2[0], u1 = U2[1];
         const double u[4] = {u0.x, u0.y, u1.x, u1.y};
@@ -140,21 +154,28 @@ __global__ void __launch_bounds__(256) update_kernel(const UpdateArgs a, const G
         double u[4];
 #pragma unroll
         for (int i = 0; i < 4; i++) u[i] = w[i] + c3 * r[i];
-        double2* Uo2 = reinterpret_cast<double2*>(a.U + (size_t)c * 4);
+        double2* Uo2 = reinterpret_cast<double2*>(a.U + row * 4);
         Uo2[0] = make_double2(u[0], u[1]);
         Uo2[1] = make_double2(u[2], u[3]);
         double p[5];
         if (FAST) primitives_rcp(g, u, p);
         else primitives(g, u, p);
-        double* po = a.prim + (size_t)c * NPR;
+        double* po = a.prim + row * NPR;
 #pragma unroll
         for (int i = 0; i < NPR; i++) po[i] = p[i];
-        a.snd[c] = sound_speed(g.gamma, u[0], p);
+        a.snd[row] = sound_speed(g.gamma, u[0], p);
         bool ok = true;
 #pragma unroll
         for (int i = 0; i < 4; i++) ok = ok && isfinite(u[i]);
-        if (!ok) atomicOr(a.flags, 1u);
+        if (!ok) atomicOr(flag, 1u);
     }
+}
+
+template <int STAGE, bool FAST>
+__global__ void __launch_bounds__(256) update_kernel(const UpdateArgs a, const GasParams g) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= a.n_cells) return;
+    update_cell<STAGE, FAST>(a, g, c, Ix1{}, a.dt, a.flags);
 }
 
 // ---------------------------------------------------------------------------
@@ -171,11 +192,10 @@ __global__ void __launch_bounds__(256) sound_kernel(int n, double gamma, const d
 
 // The sound speeds come from the per-cell array written with the
 // primitives.  FAST multiplies by precomputed 1/dxn instead of dividing.
-template <bool FAST>
-__global__ void __launch_bounds__(256) spectral_kernel(const SpecArgs a) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    double tot = 0.0;
-    if (c < a.n_cells) {
+template <bool FAST, class IX>
+__device__ __forceinline__ double spectral_cell(const SpecArgs& a, int c, const IX& ix) {
+    double tot;
+    {
         const int4 cf = a.cfaces[c];
         const int ent[4] = {cf.x, cf.y, cf.z, cf.w};
         double conv = 0.0, acou = 0.0;
@@ -188,9 +208,9 @@ __global__ void __launch_bounds__(256) spectral_kernel(const SpecArgs a) {
             const int2 lr = a.lr[f];
             const int L = lr.x, R = lr.y < 0 ? lr.x : lr.y;
             const double2 n = a.nrm[f];
-            const double* wl = a.prim + (size_t)L * NPR;
-            const double* wr = a.prim + (size_t)R * NPR;
-            const double al = a.snd[L], ar = a.snd[R];
+            const double* wl = a.prim + ix.u(L) * NPR;
+            const double* wr = a.prim + ix.u(R) * NPR;
+            const double al = a.snd[ix.u(L)], ar = a.snd[ix.u(R)];
             const double af = 0.5 * (al + ar);
             const double uf0 = 0.5 * (wl[0] + wr[0]), uf1 = 0.5 * (wl[1] + wr[1]);
             const double un = fabs(uf0 * n.x + uf1 * n.y);
@@ -210,6 +230,16 @@ __global__ void __launch_bounds__(256) spectral_kernel(const SpecArgs a) {
         conv *= 1.37 * geom;
         acou = 1.37 * sqrt(geom * acou);
         tot = conv + acou;
+    }
+    return tot;
+}
+
+template <bool FAST>
+__global__ void __launch_bounds__(256) spectral_kernel(const SpecArgs a) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    double tot = 0.0;
+    if (c < a.n_cells) {
+        tot = spectral_cell<FAST>(a, c, Ix1{});
         a.rho_cell[c] = tot;
     }
     // block max of positive doubles via their bit patterns
@@ -231,6 +261,106 @@ __global__ void __launch_bounds__(256) spectral_kernel(const SpecArgs a) {
         }
         if (threadIdx.x == 0) atomicMax(a.rmax_bits, bits);
     }
+}
+
+// ---------------------------------------------------------------------------
+// Batched form (see BatchLaunch): thread (case, cell); 8 consecutive threads
+// are one 8-cell tile of one case.
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ int batch_group(const long long* start, int n, long long gt) {
+    int g = 0;
+    while (g + 1 < n && gt >= start[g + 1]) ++g;
+    return g;
+}
+
+template <int STAGE>
+__global__ void __launch_bounds__(256) update_batch_kernel(const BatchLaunch b, const GasParams g) {
+    const long long total = b.cell0[b.n_groups];
+    for (long long gt = (long long)blockIdx.x * 256 + threadIdx.x; gt < total; gt += (long long)gridDim.x * 256) {
+        const int gi = batch_group(b.cell0, b.n_groups, gt);
+        const long long t = gt - b.cell0[gi];
+        const long long tc = t >> 3;
+        const unsigned C = b.C[gi];
+        const int c = (int)(tc / C) * 8 + (int)(t & 7);
+        if (c >= b.n_cells[gi]) continue;
+        const unsigned cs = (unsigned)(tc % C);
+        UpdateArgs a = b.upd[gi];
+        a.G = b.G;
+        a.U = b.U;
+        a.Ut = b.Ut;
+        a.W = b.W;
+        a.prim = b.prim;
+        a.snd = b.snd;
+        const unsigned gc = b.case0[gi] + cs;
+        update_cell<STAGE, true>(a, g, c, IxB{b.ubase[gi], b.fbase[gi], C, cs}, b.dt + gc, b.flags + gc);
+    }
+}
+
+// Spectral radius per cell, maximum per case (8 lanes of one case-tile
+// reduce, then one atomic per tile).
+__global__ void __launch_bounds__(256) spectral_batch_kernel(const BatchLaunch b) {
+    const long long total = b.cell0[b.n_groups];
+    for (long long gt = (long long)blockIdx.x * 256 + threadIdx.x; gt < total; gt += (long long)gridDim.x * 256) {
+        const int gi = batch_group(b.cell0, b.n_groups, gt);
+        const long long t = gt - b.cell0[gi];
+        const long long tc = t >> 3;
+        const unsigned C = b.C[gi];
+        const int c = (int)(tc / C) * 8 + (int)(t & 7);
+        const unsigned cs = (unsigned)(tc % C);
+        double tot = 0.0;
+        if (c < b.n_cells[gi]) {
+            SpecArgs a = b.spec[gi];
+            a.prim = b.prim;
+            a.snd = b.snd;
+            tot = spectral_cell<true>(a, c, IxB{b.ubase[gi], b.fbase[gi], C, cs});
+        }
+        unsigned long long bits = (unsigned long long)__double_as_longlong(tot);
+#pragma unroll
+        for (int o = 4; o > 0; o >>= 1) {
+            const unsigned long long other = __shfl_xor_sync(0xffffffffu, bits, o);
+            bits = other > bits ? other : bits;
+        }
+        if ((t & 7) == 0) atomicMax(b.rmax + b.case0[gi] + cs, bits);
+    }
+}
+
+__global__ void dt_batch_kernel(const BatchLaunch b, int n_cases, double cfl) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n_cases) return;
+    const double rmax = __longlong_as_double((long long)b.rmax[c]);
+    const double d = cfl / rmax;
+    b.dt[c] = d;
+    if (!(d >= 0.0) || !isfinite(d)) atomicOr(b.flags + c, 2u);
+    b.t[c] = b.t[c] + d;
+}
+
+// caller-order rows (src, perm_old[internal] = caller) <-> interleaved rows
+__global__ void batch_rows_kernel(int n, int width, const uint32_t* __restrict__ perm_old,
+                                  const double* __restrict__ src, double* __restrict__ dst,
+                                  unsigned long long ubase, unsigned C, unsigned cs, int to_batch) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)n * width) return;
+    const int c = (int)(t / width), k = (int)(t % width);
+    const size_t row = ubase + (((size_t)(c >> 3) * C + cs) << 3) + (c & 7);
+    const size_t old = perm_old[c];
+    if (to_batch) dst[row * width + k] = src[old * width + k];
+    else dst[old * width + k] = src[row * width + k];
+}
+
+// primitives (the reference's arithmetic) and sound speed of one case's rows
+__global__ void batch_prims_kernel(int n, const GasParams g, const double* __restrict__ U, double* __restrict__ prim,
+                                   double* __restrict__ snd, unsigned long long ubase, unsigned C, unsigned cs) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    const size_t row = ubase + (((size_t)(c >> 3) * C + cs) << 3) + (c & 7);
+    double u[4], w[5];
+#pragma unroll
+    for (int k = 0; k < 4; k++) u[k] = U[row * 4 + k];
+    primitives(g, u, w);
+#pragma unroll
+    for (int k = 0; k < 5; k++) prim[row * 5 + k] = w[k];
+    snd[row] = sound_speed(g.gamma, u[0], w);
 }
 
 __global__ void dt_kernel(const unsigned long long* rmax_bits, double cfl, double* dt, double* t, unsigned* flags) {
@@ -339,6 +469,43 @@ cudaError_t launch_sound(int n, double gamma, const double* U, const double* pri
     const unsigned blocks = (unsigned)((n + 255) / 256);
     if (blocks == 0) return cudaSuccess;
     sound_kernel<<<blocks, 256, 0, s>>>(n, gamma, U, prim, snd);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_update_batch(const BatchLaunch& b, const GasParams& g, int stage, cudaStream_t s) {
+    const long long blocks = (b.cell0[b.n_groups] + 255) / 256;
+    if (blocks == 0) return cudaSuccess;
+    switch (stage) {
+        case 1: update_batch_kernel<1><<<(unsigned)blocks, 256, 0, s>>>(b, g); break;
+        case 2: update_batch_kernel<2><<<(unsigned)blocks, 256, 0, s>>>(b, g); break;
+        case 3: update_batch_kernel<3><<<(unsigned)blocks, 256, 0, s>>>(b, g); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_spectral_batch(const BatchLaunch& b, cudaStream_t s) {
+    const long long blocks = (b.cell0[b.n_groups] + 255) / 256;
+    if (blocks) spectral_batch_kernel<<<(unsigned)blocks, 256, 0, s>>>(b);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dt_batch(const BatchLaunch& b, int n_cases, double cfl, cudaStream_t s) {
+    if (n_cases > 0) dt_batch_kernel<<<(n_cases + 127) / 128, 128, 0, s>>>(b, n_cases, cfl);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_rows(int n, int width, const uint32_t* perm_old, const double* src, double* dst,
+                              unsigned long long ubase, unsigned C, unsigned cs, bool to_batch, cudaStream_t s) {
+    const long long threads = (long long)n * width;
+    if (threads) batch_rows_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(n, width, perm_old, src, dst, ubase,
+                                                                                      C, cs, to_batch ? 1 : 0);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_prims(int n, const GasParams& g, double* U, double* prim, double* snd,
+                               unsigned long long ubase, unsigned C, unsigned cs, cudaStream_t s) {
+    if (n > 0) batch_prims_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, g, U, prim, snd, ubase, C, cs);
     return cudaGetLastError();
 }
 
