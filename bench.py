@@ -31,7 +31,9 @@ one cell advanced one full SSPRK3 step).
 
 A second section, "wedge", times the benchmark spec's 4M-cell configuration:
 the supersonic ramp channel (Delaunay mesh, inviscid), plain FP64 against
-FP32 + learned selector, with the learned form's density error.
+FP32 + learned selector, with the learned form's density error.  A third,
+"batched", times configuration 4: 256 four-quadrant cases of uneven mesh
+size stepped together by the batched FP32 form.
 
 --impl reference times the CPU oracle (the restatement of the reference's
 algorithm, FP64, all host threads) on a 256 x 256 sample of the same
@@ -77,6 +79,8 @@ def parse():
                          "error reference")
     ap.add_argument("--wedge-n", type=int, default=816,
                     help="rows of the ramp-channel lattice (3n+1 columns; 816 -> 4.0M triangles); 0 skips it")
+    ap.add_argument("--batch-cases", type=int, default=256,
+                    help="cases of the batched section (configuration 4); 0 skips it")
     ap.add_argument("--cpu-sample-n", type=int, default=CPU_SAMPLE_N)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -373,6 +377,79 @@ def run_wedge(args, device, selector):
     return out
 
 
+def run_batched(args, device):
+    """Configuration 4: n_cases independent four-quadrant problems on unit
+    squares, mesh size drawn per case from {64, 128, 256, 512}^2 quads
+    (cartesian_tri, so twice as many triangles), quadrant states drawn per
+    case (rho ~ U[0.1, 2], p ~ U[0.03, 2], u, v ~ U[-1.5, 1.5]); the
+    batched FP32 form with one launch per kernel over all cases, autotuned."""
+    import numpy as np
+    import torch
+
+    import mallard_gb300 as mg
+    from mallard_gb300.batch import Batch
+    r = np.random.default_rng(SEED)
+    sizes = [64, 128, 256, 512]
+    draw = r.integers(0, 4, args.batch_cases)
+    counts = [int((draw == i).sum()) for i in range(4)]
+    used = [i for i in range(4) if counts[i]]
+    t0 = time.perf_counter()
+    meshes = [mg.Mesh.generate("cartesian_tri", sizes[i], sizes[i], 1.0, 1.0) for i in used]
+    b = Batch(meshes, [counts[i] for i in used],
+              boundaries=[{"name": z, "type": "extrapolation"} for z in ("right", "top", "left", "bottom")],
+              riemann_solver="HLLC")
+    cells = 0
+    for g, i in enumerate(used):
+        m = meshes[g]
+        x, y = m.cell_coords[:, 0], m.cell_coords[:, 1]
+        for k in range(counts[i]):
+            q = np.column_stack([r.uniform(0.1, 2.0, 4), r.uniform(-1.5, 1.5, 4), r.uniform(-1.5, 1.5, 4),
+                                 r.uniform(0.03, 2.0, 4)])
+            sx, sy = r.uniform(0.3, 0.7, 2)
+            quad = np.where(x >= sx, np.where(y >= sy, 0, 3), np.where(y >= sy, 1, 2))
+            pr = q[quad]
+            U, W = mg.state_from_primitives(pr[:, 0], pr[:, 1], pr[:, 2], pr[:, 3])
+            b.set_state(g, k, U, W)
+            cells += m.n_cells
+    setup = time.perf_counter() - t0
+    shape, bps, ms = b.autotune()
+    # autotuning ran reconstructions only; the states are unchanged
+    stream = torch.cuda.Stream()
+    b.set_stream(stream.cuda_stream)
+    b.run(CFL, args.warmup)
+    b.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    b.run(CFL, args.steps)
+    e1.record(stream)
+    e1.synchronize()
+    secs = e0.elapsed_time(e1) * 1e-3
+    per_step = []
+    for _ in range(2):  # two more steps one by one, to see whether the step time changes as cases fail
+        e0.record(stream)
+        b.run(CFL, 1)
+        e1.record(stream)
+        e1.synchronize()
+        per_step.append(e0.elapsed_time(e1))
+    flags, times = b.status()
+    b.close()
+    case_cells = np.concatenate([np.full(counts[i], meshes[g].n_cells) for g, i in enumerate(used)])
+    live = int(case_cells[flags == 0].sum())
+    return {"workload": f"{args.batch_cases} four-quadrant cases, cartesian_tri sizes {{64,128,256,512}}^2 quads "
+                        f"drawn per case (seed {SEED}), random quadrant states, TENO p3 + HLLC, SSPRK3 CFL {CFL}, "
+                        f"FP32 form, one launch per kernel over all cases",
+            "cases_per_size": {f"{sizes[i]}x{sizes[i]}": counts[i] for i in range(4)}, "cells": cells,
+            "value": live * args.steps / secs / 1e6, "unit": UNIT, "ms_per_step": secs * 1e3 / args.steps,
+            "value_counts": "cells of the cases still finite after the timed steps (a failed case is frozen and "
+                            "does no further work)",
+            "live_cells": live,
+            "timing": "CUDA events on the batch's stream around the graph replays",
+            "ms_next_steps": per_step,
+            "autotune": {"shape": shape, "ctas_per_sm": bps, "ms": np.round(ms, 4).tolist()},
+            "finite_cases": int((flags == 0).sum()), "setup_s": setup}
+
+
 def recon_bytes_selected(solver, stats, cells):
     """Compulsory bytes of one selector-driven reconstruction launch: the
     tables of the stencils actually evaluated plus the per-cell constants
@@ -524,6 +601,7 @@ def run_ours(args):
                      "peak_source": "measured FMA-chain probe on this GPU"}
 
     wedge = run_wedge(args, local, selector or load_selector(local)) if args.wedge_n > 0 else None
+    batched = run_batched(args, local) if args.batch_cases > 0 else None
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -551,6 +629,8 @@ def run_ours(args):
             line["accuracy_vs_fp64"] = accuracy
         if wedge:
             line["wedge"] = wedge
+        if batched:
+            line["batched"] = batched
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

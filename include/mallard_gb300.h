@@ -319,6 +319,9 @@ int mgpu_batch_get_state(mgpu_batch* b, uint32_t group, uint32_t index, double* 
  * (spectral radius and dt per case, three SSPRK3 stages); asynchronous. */
 int mgpu_batch_run(mgpu_batch* b, double cfl, uint32_t n_steps);
 int mgpu_batch_synchronize(mgpu_batch* b);
+/* Launch on the caller's stream (a cudaStream_t) from now on; NULL returns
+ * to the batch's own stream. */
+int mgpu_batch_set_stream(mgpu_batch* b, void* stream);
 /* Per case (global order: group 0's cases first): status flags (bit 0
  * non-finite state, bit 1 invalid dt) and time; either may be NULL. */
 int mgpu_batch_status(mgpu_batch* b, uint32_t* flags, double* times);

@@ -122,6 +122,7 @@ def lib():
         "mgpu_batch_get_state": (i32, [vp, u32, u32, vp, vp]),
         "mgpu_batch_run": (i32, [vp, f64, u32]),
         "mgpu_batch_synchronize": (i32, [vp]),
+        "mgpu_batch_set_stream": (i32, [vp, vp]),
         "mgpu_batch_status": (i32, [vp, vp, vp]),
         "mgpu_batch_autotune": (i32, [vp, vp, P(i32), P(i32)]),
         "mgpu_n_cells": (u32, [vp]),

@@ -91,6 +91,9 @@ class Batch:
     def run(self, cfl, n_steps):
         N.check(self._lib.mgpu_batch_run(self._h, float(cfl), int(n_steps)))
 
+    def set_stream(self, stream_handle):
+        N.check(self._lib.mgpu_batch_set_stream(self._h, C.c_void_p(stream_handle) if stream_handle else None))
+
     def synchronize(self):
         N.check(self._lib.mgpu_batch_synchronize(self._h))
 

@@ -139,7 +139,9 @@ cudaError_t launch_flux(const FluxArgs& a, const float* fv, const GasParams& g, 
 // interleaved per 8-row tile: row(c) = ubase + ((c / 8) C + case) 8 + c % 8.
 // A kernel's threads run over all groups in order; group g starts at the
 // thread index in the *0 arrays.  The kernels are persistent: any grid
-// size works, each thread strides over the whole range.
+// size works, each thread strides over the whole range.  A case whose
+// status flags are set (non-finite state, invalid dt) is frozen: every
+// kernel skips it from the next step on.
 // ---------------------------------------------------------------------------
 constexpr int MAX_GROUPS = 8;
 struct BatchLaunch {

@@ -223,7 +223,8 @@ __device__ __forceinline__ void primitives_guarded(const GasParams& g, const flo
 // Flux of one face (local index fi) into G.
 template <int RS, int NQ, class IX>
 __device__ __forceinline__ void flux32_face(const FluxArgs& a, const float* __restrict__ fv, const GasParams& g,
-                                            const BcTable& bct, int fi, const IX& ix) {
+                                            const BcTable& bct, int fi, const IX& ix, const double* __restrict__ Ust,
+                                            double* __restrict__ Gout) {
     const int2 lr = a.lr[fi];
     const double2 nn = a.nrm[fi];
     const float n[2] = {f(nn.x), f(nn.y)};
@@ -245,10 +246,10 @@ __device__ __forceinline__ void flux32_face(const FluxArgs& a, const float* __re
         }
         if (!admissible(g, cl))
 #pragma unroll
-            for (int i = 0; i < 4; i++) cl[i] = f(a.U[ix.u(lr.x) * NC + i]);
+            for (int i = 0; i < 4; i++) cl[i] = f(Ust[ix.u(lr.x) * NC + i]);
         if (type < 0 && !admissible(g, cr))
 #pragma unroll
-            for (int i = 0; i < 4; i++) cr[i] = f(a.U[ix.u(lr.y) * NC + i]);
+            for (int i = 0; i < 4; i++) cr[i] = f(Ust[ix.u(lr.y) * NC + i]);
         primitives_guarded(g, cl, pl);
         if (type == MGPU_BC_WALL_ADIABATIC) {
             Ft[0] = 0.0f;
@@ -297,7 +298,7 @@ __device__ __forceinline__ void flux32_face(const FluxArgs& a, const float* __re
         for (int i = 0; i < 4; i++) F[i] = fmaf(f(a.qw[q]), Ft[i], F[i]);
     }
     const double area = a.area[fi];
-    double2* Gf = reinterpret_cast<double2*>(a.G + ix.f(fi) * 4);
+    double2* Gf = reinterpret_cast<double2*>(Gout + ix.f(fi) * 4);
     Gf[0] = make_double2(area * (double)(F[0] * 0.5f), area * (double)(F[1] * 0.5f));
     Gf[1] = make_double2(area * (double)(F[2] * 0.5f), area * (double)(F[3] * 0.5f));
 }
@@ -307,7 +308,7 @@ __global__ void __launch_bounds__(128) flux32_kernel(const FluxArgs a, const flo
                                                      const GasParams g, const BcTable bct) {
     const int fi = blockIdx.x * blockDim.x + threadIdx.x;
     if (fi >= a.n_faces) return;
-    flux32_face<RS, NQ>(a, fv, g, bct, fi, Ix1{});
+    flux32_face<RS, NQ>(a, fv, g, bct, fi, Ix1{}, a.U, a.G);
 }
 
 template <int RS, int NQ>
@@ -365,15 +366,16 @@ __global__ void __launch_bounds__(BS, MINB) teno32_batch_kernel(const BatchLaunc
     const long long total = b.teno0[b.n_groups];
     for (long long gt = (long long)blockIdx.x * BS + threadIdx.x; gt < total; gt += (long long)gridDim.x * BS) {
         const int gi = batch_group(b.teno0, b.n_groups, gt);
-        const long long t = gt - b.teno0[gi];
+        const unsigned t = (unsigned)(gt - b.teno0[gi]);
         const int v = (int)(t & 3), lane8 = (int)((t >> 2) & 7);
-        const long long tc = t >> 5;
-        const unsigned C = b.C[gi];
-        const IxB ix{b.ubase[gi], b.fbase[gi], C, (unsigned)(tc % C)};
+        const unsigned tc = t >> 5, C = b.C[gi], cs = tc % C;
         const int cell = (int)(tc / C) * 8 + lane8;
-        const unsigned live = __ballot_sync(0xffffffffu, cell < b.n_cells[gi]);
-        if (cell >= b.n_cells[gi]) continue;
-        teno32_cell<K, M, NQ, false>(b.teno[gi], U, b.fv, nullptr, nullptr, cell, v, live, ix);
+        // frozen (failed) cases and cells past the mesh do no work; a warp is one case's tile
+        const bool on = cell < b.n_cells[gi] && b.flags[b.case0[gi] + cs] == 0u;
+        const unsigned live = __ballot_sync(0xffffffffu, on);
+        if (!on) continue;
+        teno32_cell<K, M, NQ, false>(b.teno[gi], U, b.fv, nullptr, nullptr, cell, v, live,
+                                     IxB{b.ubase[gi], b.fbase[gi], C, cs});
     }
 }
 
@@ -384,16 +386,11 @@ __global__ void __launch_bounds__(128) flux32_batch_kernel(const BatchLaunch b, 
     const long long total = b.face0[b.n_groups];
     for (long long gt = (long long)blockIdx.x * 128 + threadIdx.x; gt < total; gt += (long long)gridDim.x * 128) {
         const int gi = batch_group(b.face0, b.n_groups, gt);
-        const long long t = gt - b.face0[gi];
-        const long long tc = t >> 3;
-        const unsigned C = b.C[gi];
+        const unsigned t = (unsigned)(gt - b.face0[gi]);
+        const unsigned tc = t >> 3, C = b.C[gi], cs = tc % C;
         const int fi = (int)(tc / C) * 8 + (int)(t & 7);
-        if (fi >= b.n_faces[gi]) continue;
-        const IxB ix{b.ubase[gi], b.fbase[gi], C, (unsigned)(tc % C)};
-        FluxArgs a = b.flux[gi];
-        a.U = U;
-        a.G = b.G;
-        flux32_face<RS, NQ>(a, b.fv, g, bct, fi, ix);
+        if (fi >= b.n_faces[gi] || b.flags[b.case0[gi] + cs] != 0u) continue;
+        flux32_face<RS, NQ>(b.flux[gi], b.fv, g, bct, fi, IxB{b.ubase[gi], b.fbase[gi], C, cs}, U, b.G);
     }
 }
 

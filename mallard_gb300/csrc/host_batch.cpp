@@ -25,7 +25,7 @@ struct mgpu_batch {
     std::vector<std::unique_ptr<mgpu_ctx, void (*)(mgpu_ctx*)>> groups;
     uint32_t n_cases = 0;
     bool finalized = false;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr, stream_owned = nullptr;  // launch stream; the batch's own
     BatchLaunch bl{};
     DevArray<double> U, Ut, W, prim, snd, G, dt, t;
     DevArray<float> fv;
@@ -40,7 +40,8 @@ struct mgpu_batch {
     double exec_cfl = -1.0;
     ~mgpu_batch() {
         if (exec) cudaGraphExecDestroy(exec);
-        if (stream) cudaStreamDestroy(stream);
+        cudaStream_t own = stream_owned ? stream_owned : stream;
+        if (own) cudaStreamDestroy(own);
     }
 };
 
@@ -314,6 +315,25 @@ int mgpu_batch_run(mgpu_batch* b, double cfl, uint32_t n_steps) {
             b->exec_cfl = cfl;
         }
         for (uint32_t s = 0; s < n_steps; ++s) ck(cudaGraphLaunch(b->exec, b->stream), "cudaGraphLaunch");
+        return MGPU_OK;
+    });
+}
+
+int mgpu_batch_set_stream(mgpu_batch* b, void* stream) {
+    if (int rc = need_batch(b)) return rc;
+    return guarded([&] {
+        ck(cudaStreamSynchronize(b->stream), "cudaStreamSynchronize");
+        if (stream) {
+            // the batch launches on the caller's stream from now on
+            b->stream_owned = b->stream_owned ? b->stream_owned : b->stream;
+            b->stream = (cudaStream_t)stream;
+        } else if (b->stream_owned) {
+            b->stream = b->stream_owned;
+        }
+        if (b->exec) {
+            cudaGraphExecDestroy(b->exec);
+            b->exec = nullptr;
+        }
         return MGPU_OK;
     });
 }

@@ -74,9 +74,15 @@ struct IxB {
 // FAST: residual times a precomputed 1/volume and primitives_rcp (the
 // FP64-fast and FP32 forms); otherwise the reference's divisions.
 // Cell c (local index) of one case; dt and the NaN flag are the case's.
+// State arrays an update reads and writes (one case's, or a batch's).
+struct StageState {
+    const double* G;
+    double *U, *Ut, *W, *prim, *snd, *rhs;
+};
+
 template <int STAGE, bool FAST, class IX>
-__device__ __forceinline__ void update_cell(const UpdateArgs& a, const GasParams& g, int c, const IX& ix,
-                                            const double* dtp, unsigned* flag) {
+__device__ __forceinline__ void update_cell(const UpdateArgs& a, const StageState& st, const GasParams& g, int c,
+                                            const IX& ix, const double* dtp, unsigned* flag) {
     const size_t row = ix.u(c);
     const int4 gl = a.gat[c];
     const int ent[4] = {gl.x, gl.y, gl.z, gl.w};
@@ -84,7 +90,7 @@ __device__ __forceinline__ void update_cell(const UpdateArgs& a, const GasParams
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
         if (ent[e] < 0) break;
-        const double2* Gf = reinterpret_cast<const double2*>(a.G + ix.f((size_t)(ent[e] >> 1)) * 4);
+        const double2* Gf = reinterpret_cast<const double2*>(st.G + ix.f((size_t)(ent[e] >> 1)) * 4);
         const double2 g0 = Gf[0], g1 = Gf[1];
         const double x[4] = {g0.x, g0.y, g1.x, g1.y};
         if (ent[e] & 1) {
@@ -106,16 +112,16 @@ __device__ __forceinline__ void update_cell(const UpdateArgs& a, const GasParams
     }
     double2* out2;
     if (STAGE == 0) {
-        out2 = reinterpret_cast<double2*>(a.rhs + row * 4);
+        out2 = reinterpret_cast<double2*>(st.rhs + row * 4);
         out2[0] = make_double2(r[0], r[1]);
         out2[1] = make_double2(r[2], r[3]);
         return;
     }
     const double dt = *dtp;
-    const double2* U2 = reinterpret_cast<const double2*>(a.U + row * 4);
-    const double2* W2 = reinterpret_cast<const double2*>(a.W + row * 4);
-    double2* Ut2 = reinterpret_cast<double2*>(a.Ut + row * 4);
-    double2* Wo2 = reinterpret_cast<double2*>(a.W + row * 4);
+    const double2* U2 = reinterpret_cast<const double2*>(st.U + row * 4);
+    const double2* W2 = reinterpret_cast<const double2*>(st.W + row * 4);
+    double2* Ut2 = reinterpret_cast<double2*>(st.Ut + row * 4);
+    double2* Wo2 = reinterpret_cast<double2*>(st.W + row * 4);
     if (STAGE == 1) {
         const double2 u0 = U2[0], u1 = U2[1];
         const double u[4] = {u0.x, u0.y, u1.x, u1.y};
@@ -154,16 +160,16 @@ __device__ __forceinline__ void update_cell(const UpdateArgs& a, const GasParams
         double u[4];
 #pragma unroll
         for (int i = 0; i < 4; i++) u[i] = w[i] + c3 * r[i];
-        double2* Uo2 = reinterpret_cast<double2*>(a.U + row * 4);
+        double2* Uo2 = reinterpret_cast<double2*>(st.U + row * 4);
         Uo2[0] = make_double2(u[0], u[1]);
         Uo2[1] = make_double2(u[2], u[3]);
         double p[5];
         if (FAST) primitives_rcp(g, u, p);
         else primitives(g, u, p);
-        double* po = a.prim + row * NPR;
+        double* po = st.prim + row * NPR;
 #pragma unroll
         for (int i = 0; i < NPR; i++) po[i] = p[i];
-        a.snd[row] = sound_speed(g.gamma, u[0], p);
+        st.snd[row] = sound_speed(g.gamma, u[0], p);
         bool ok = true;
 #pragma unroll
         for (int i = 0; i < 4; i++) ok = ok && isfinite(u[i]);
@@ -175,7 +181,8 @@ template <int STAGE, bool FAST>
 __global__ void __launch_bounds__(256) update_kernel(const UpdateArgs a, const GasParams g) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= a.n_cells) return;
-    update_cell<STAGE, FAST>(a, g, c, Ix1{}, a.dt, a.flags);
+    const StageState st{a.G, a.U, a.Ut, a.W, a.prim, a.snd, a.rhs};
+    update_cell<STAGE, FAST>(a, st, g, c, Ix1{}, a.dt, a.flags);
 }
 
 // ---------------------------------------------------------------------------
@@ -193,7 +200,8 @@ __global__ void __launch_bounds__(256) sound_kernel(int n, double gamma, const d
 // The sound speeds come from the per-cell array written with the
 // primitives.  FAST multiplies by precomputed 1/dxn instead of dividing.
 template <bool FAST, class IX>
-__device__ __forceinline__ double spectral_cell(const SpecArgs& a, int c, const IX& ix) {
+__device__ __forceinline__ double spectral_cell(const SpecArgs& a, const double* __restrict__ prim,
+                                                const double* __restrict__ snd, int c, const IX& ix) {
     double tot;
     {
         const int4 cf = a.cfaces[c];
@@ -208,9 +216,9 @@ __device__ __forceinline__ double spectral_cell(const SpecArgs& a, int c, const 
             const int2 lr = a.lr[f];
             const int L = lr.x, R = lr.y < 0 ? lr.x : lr.y;
             const double2 n = a.nrm[f];
-            const double* wl = a.prim + ix.u(L) * NPR;
-            const double* wr = a.prim + ix.u(R) * NPR;
-            const double al = a.snd[ix.u(L)], ar = a.snd[ix.u(R)];
+            const double* wl = prim + ix.u(L) * NPR;
+            const double* wr = prim + ix.u(R) * NPR;
+            const double al = snd[ix.u(L)], ar = snd[ix.u(R)];
             const double af = 0.5 * (al + ar);
             const double uf0 = 0.5 * (wl[0] + wr[0]), uf1 = 0.5 * (wl[1] + wr[1]);
             const double un = fabs(uf0 * n.x + uf1 * n.y);
@@ -239,7 +247,7 @@ __global__ void __launch_bounds__(256) spectral_kernel(const SpecArgs a) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     double tot = 0.0;
     if (c < a.n_cells) {
-        tot = spectral_cell<FAST>(a, c, Ix1{});
+        tot = spectral_cell<FAST>(a, a.prim, a.snd, c, Ix1{});
         a.rho_cell[c] = tot;
     }
     // block max of positive doubles via their bit patterns
@@ -279,21 +287,13 @@ __global__ void __launch_bounds__(256) update_batch_kernel(const BatchLaunch b, 
     const long long total = b.cell0[b.n_groups];
     for (long long gt = (long long)blockIdx.x * 256 + threadIdx.x; gt < total; gt += (long long)gridDim.x * 256) {
         const int gi = batch_group(b.cell0, b.n_groups, gt);
-        const long long t = gt - b.cell0[gi];
-        const long long tc = t >> 3;
-        const unsigned C = b.C[gi];
+        const unsigned t = (unsigned)(gt - b.cell0[gi]);
+        const unsigned tc = t >> 3, C = b.C[gi], cs = tc % C;
         const int c = (int)(tc / C) * 8 + (int)(t & 7);
-        if (c >= b.n_cells[gi]) continue;
-        const unsigned cs = (unsigned)(tc % C);
-        UpdateArgs a = b.upd[gi];
-        a.G = b.G;
-        a.U = b.U;
-        a.Ut = b.Ut;
-        a.W = b.W;
-        a.prim = b.prim;
-        a.snd = b.snd;
         const unsigned gc = b.case0[gi] + cs;
-        update_cell<STAGE, true>(a, g, c, IxB{b.ubase[gi], b.fbase[gi], C, cs}, b.dt + gc, b.flags + gc);
+        if (c >= b.n_cells[gi] || b.flags[gc] != 0u) continue;
+        const StageState st{b.G, b.U, b.Ut, b.W, b.prim, b.snd, nullptr};
+        update_cell<STAGE, true>(b.upd[gi], st, g, c, IxB{b.ubase[gi], b.fbase[gi], C, cs}, b.dt + gc, b.flags + gc);
     }
 }
 
@@ -303,18 +303,12 @@ __global__ void __launch_bounds__(256) spectral_batch_kernel(const BatchLaunch b
     const long long total = b.cell0[b.n_groups];
     for (long long gt = (long long)blockIdx.x * 256 + threadIdx.x; gt < total; gt += (long long)gridDim.x * 256) {
         const int gi = batch_group(b.cell0, b.n_groups, gt);
-        const long long t = gt - b.cell0[gi];
-        const long long tc = t >> 3;
-        const unsigned C = b.C[gi];
+        const unsigned t = (unsigned)(gt - b.cell0[gi]);
+        const unsigned tc = t >> 3, C = b.C[gi], cs = tc % C;
         const int c = (int)(tc / C) * 8 + (int)(t & 7);
-        const unsigned cs = (unsigned)(tc % C);
         double tot = 0.0;
-        if (c < b.n_cells[gi]) {
-            SpecArgs a = b.spec[gi];
-            a.prim = b.prim;
-            a.snd = b.snd;
-            tot = spectral_cell<true>(a, c, IxB{b.ubase[gi], b.fbase[gi], C, cs});
-        }
+        if (c < b.n_cells[gi] && b.flags[b.case0[gi] + cs] == 0u)
+            tot = spectral_cell<true>(b.spec[gi], b.prim, b.snd, c, IxB{b.ubase[gi], b.fbase[gi], C, cs});
         unsigned long long bits = (unsigned long long)__double_as_longlong(tot);
 #pragma unroll
         for (int o = 4; o > 0; o >>= 1) {
@@ -327,7 +321,7 @@ __global__ void __launch_bounds__(256) spectral_batch_kernel(const BatchLaunch b
 
 __global__ void dt_batch_kernel(const BatchLaunch b, int n_cases, double cfl) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= n_cases) return;
+    if (c >= n_cases || b.flags[c] != 0u) return;  // a failed case stays frozen
     const double rmax = __longlong_as_double((long long)b.rmax[c]);
     const double d = cfl / rmax;
     b.dt[c] = d;
