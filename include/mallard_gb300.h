@@ -178,6 +178,16 @@ typedef struct mgpu_config {
     int precision;                  /* MGPU_PREC_*                           */
     int reorder;                    /* 1 = reverse Cuthill-McKee cell order  */
     int device;                     /* CUDA device ordinal                   */
+    /* Viscous (Navier-Stokes) face flux; no counterpart in the reference.
+     * mu(T) = mu_ref (T/T_mu_ref)^1.5 (T_mu_ref + S) / (T + S) (Sutherland)
+     * for sutherland_S > 0, else the constant mu_ref; conductivity
+     * mu cp / prandtl; temperatures in the units of the solver's T = e / cv.
+     * Gradients: Green-Gauss per cell from the cell averages, at a face the
+     * average of its two cells' plus the jump correction along the line
+     * joining their centres.  With viscous != 0 wall_adiabatic walls are
+     * no-slip and adiabatic; other boundaries carry no viscous flux. */
+    int viscous;
+    double mu_ref, T_mu_ref, sutherland_S, prandtl;
 } mgpu_config;
 
 typedef struct mgpu_ctx mgpu_ctx;

@@ -64,6 +64,8 @@ class Config(C.Structure):
         ("time_integrator", C.c_int), ("gamma", C.c_double), ("p_ref", C.c_double), ("T_ref", C.c_double),
         ("rho_ref", C.c_double), ("p_min", C.c_double), ("p_max", C.c_double), ("teno_variant", C.c_int),
         ("precision", C.c_int), ("reorder", C.c_int), ("device", C.c_int),
+        ("viscous", C.c_int), ("mu_ref", C.c_double), ("T_mu_ref", C.c_double), ("sutherland_S", C.c_double),
+        ("prandtl", C.c_double),
     ]
 
 

@@ -88,6 +88,24 @@ struct UpdateArgs {
     unsigned* flags;
 };
 
+// Viscous face flux (no counterpart in the reference): Green-Gauss
+// gradients of (u, v, T) per cell, then per flux face the Navier-Stokes
+// stress and heat flux subtracted from G.
+struct ViscArgs {
+    int n_cells, n_faces;   // cells, flux faces
+    const int4* cfaces;     // faces of each cell, -1 = none
+    const int2* lr;
+    const double2* nrm;     // unit normals
+    const double* area;
+    const double* vol;
+    const int8_t* bc;       // -1 interior, else BcTable index
+    const double2* xc;      // cell centres
+    const double2* xf;      // face midpoints
+    double* grad;           // [n_cells][6]: du/dx, du/dy, dv/dx, dv/dy, dT/dx, dT/dy
+    double* G;
+    double mu_ref, T_ref, S, cp_over_pr;
+};
+
 struct SpecArgs {
     int n_cells;
     const int4* cfaces;     // faces of the cell in the reference's order, -1 = none
@@ -185,6 +203,8 @@ cudaError_t launch_first_order(int n_faces, const int2* lr, const double* U, dou
 cudaError_t launch_update(const UpdateArgs& a, const GasParams& g, int stage, bool fast, cudaStream_t s);
 cudaError_t launch_spectral(const SpecArgs& a, bool fast, cudaStream_t s);
 cudaError_t launch_sound(int n, double gamma, const double* U, const double* prim, double* snd, cudaStream_t s);
+// viscous: gradients of the stage input U, then the face flux into G
+cudaError_t launch_viscous(const ViscArgs& a, const GasParams& g, const BcTable& bct, const double* U, cudaStream_t s);
 cudaError_t launch_dt(const unsigned long long* rmax_bits, double cfl, double* dt, double* t, unsigned* flags,
                       cudaStream_t s);
 cudaError_t launch_set_scalar(double* dst, double value, cudaStream_t s);

@@ -412,6 +412,37 @@ void mgpu_ctx::build() {
     masks.alloc((size_t)N * 4);
     staging.alloc((size_t)N * 5);
     perm_old.upload(cell_old);
+    if (cfg.viscous) {
+        std::vector<double2> h_xc(N), h_xf(F_real);
+        for (uint32_t c = 0; c < N; ++c)
+            h_xc[c] = make_double2(mv.cell_coords[2 * (size_t)cell_old[c]], mv.cell_coords[2 * (size_t)cell_old[c] + 1]);
+        for (uint32_t i = 0; i < F_real; ++i) {
+            const uint32_t f = face_old[i];
+            const double* p0 = mv.node_coords + 2 * (size_t)mv.nodes_of_face[mv.offsets_nodes_of_face[f]];
+            const double* p1 = mv.node_coords + 2 * (size_t)mv.nodes_of_face[mv.offsets_nodes_of_face[f] + 1];
+            h_xf[i] = make_double2(0.5 * (p0[0] + p1[0]), 0.5 * (p0[1] + p1[1]));
+        }
+        xc.upload(h_xc);
+        xf.upload(h_xf);
+        grad.alloc((size_t)N * 6);
+        visc.n_cells = (int)N;
+        visc.n_faces = (int)F_flux;
+        visc.cfaces = cfaces.p;
+        visc.lr = lr.p;
+        visc.nrm = nrm.p;
+        visc.area = area.p;
+        visc.vol = vol.p;
+        visc.bc = bcidx.p;
+        visc.xc = xc.p;
+        visc.xf = xf.p;
+        visc.grad = grad.p;
+        visc.G = G.p;
+        visc.mu_ref = cfg.mu_ref;
+        visc.T_ref = cfg.T_mu_ref;
+        visc.S = cfg.sutherland_S;
+        const double cp = gas.R * cfg.gamma / (cfg.gamma - 1.0);
+        visc.cp_over_pr = cp / cfg.prandtl;
+    }
     // compulsory bytes of one stage: reconstruction + flux (face states in,
     // G out, face geometry) + update (G gathered, state in/out)
     const double flux_b = (double)F_flux * (nq * 64 + 32 + 8 + 16 + 8 + 1);
@@ -448,6 +479,11 @@ void mgpu_config_defaults(mgpu_config* c) {
     c->precision = MGPU_PREC_FP64;
     c->reorder = 1;
     c->device = 0;
+    c->viscous = 0;
+    c->mu_ref = 0.0;
+    c->T_mu_ref = 1.0;
+    c->sutherland_S = 0.0;
+    c->prandtl = 0.72;
 }
 
 int mgpu_create(const mgpu_mesh* mesh, const mgpu_config* cfg, mgpu_ctx** out) {
@@ -459,6 +495,8 @@ int mgpu_create(const mgpu_mesh* mesh, const mgpu_config* cfg, mgpu_ctx** out) {
         if (cfg->precision != MGPU_PREC_FP64 && cfg->precision != MGPU_PREC_FP64_FAST &&
             cfg->precision != MGPU_PREC_FP32)
             throw Unsupported("unknown precision mode");
+        if (cfg->viscous && !(cfg->mu_ref >= 0.0 && cfg->prandtl > 0.0 && (cfg->sutherland_S <= 0.0 || cfg->T_mu_ref > 0.0)))
+            throw ArgFail("viscous flux: mu_ref >= 0, prandtl > 0 and, with Sutherland's law, T_mu_ref > 0");
         if (cfg->precision == MGPU_PREC_FP32 &&
             (cfg->recon != MGPU_RECON_TENO || cfg->teno_variant != MGPU_TENO_CORRECTED))
             throw Unsupported("the FP32 form implements TENO with the corrected weighting");
@@ -663,6 +701,7 @@ int mgpu_calc_rhs(mgpu_ctx* ctx, const double* Uh, double* rhsh) {
         ctx->upload_cells(ctx->Ut.p, Uh, 4);
         ctx->reconstruct(ctx->Ut.p, nullptr);
         ctx->flux(ctx->Ut.p);
+        ctx->viscous(ctx->Ut.p);
         UpdateArgs a = ctx->update_args();
         ck(launch_update(a, ctx->gas, 0, ctx->rcp(), ctx->stream), "update");
         ctx->download_cells(ctx->rhs.p, rhsh, 4);

@@ -100,6 +100,10 @@ struct mgpu_ctx {
     DevArray<int2> lr;
     DevArray<double2> nrm;
     DevArray<double> area, dxn, idxn, ivol, snd;
+    // viscous flux: cell centres, face midpoints, gradients
+    DevArray<double2> xc, xf;
+    DevArray<double> grad;
+    ViscArgs visc{};
     DevArray<int8_t> bcidx;
     DevArray<int4> gat, cfaces;
     DevArray<uint32_t> nb, cface;
@@ -188,6 +192,13 @@ struct mgpu_ctx {
         }
     }
 
+    // viscous face flux into G (after the inviscid flux of the same stage)
+    void viscous(const double* Uin) {
+        if (!cfg.viscous) return;
+        timed(1, [&] { return launch_visc(Uin); });
+    }
+    cudaError_t launch_visc(const double* Uin) { return launch_viscous(visc, gas, bct, Uin, stream); }
+
     void flux(const double* Uin) {
         FluxArgs a{};
         a.n_faces = (int)F_flux;
@@ -234,6 +245,7 @@ struct mgpu_ctx {
         // unless asked to predict at every stage
         reconstruct(in, nullptr, k == 1 || sel_every_stage);
         flux(in);
+        viscous(in);
         UpdateArgs a = update_args();
         timed(2, [&] { return launch_update(a, gas, k, rcp(), stream); });
     }

@@ -272,6 +272,136 @@ __global__ void __launch_bounds__(256) spectral_kernel(const SpecArgs a) {
 }
 
 // ---------------------------------------------------------------------------
+// Viscous face flux (no counterpart in the reference)
+// ---------------------------------------------------------------------------
+
+// (u, v, T) of a conserved state
+__device__ __forceinline__ void uvT(const GasParams& g, const double* U, double* q) {
+    const double rho = U[0];
+    const double u = U[1] / rho, v = U[2] / rho;
+    const double E = U[3] / rho;
+    const double e = E - 0.5 * (u * u + v * v);
+    q[0] = u;
+    q[1] = v;
+    q[2] = e / g.cv;
+}
+
+// Green-Gauss gradient per cell: (1/V) sum over its faces of phi_f n_out A,
+// phi_f the mean of the two cells; on a no-slip wall u = v = 0, T = T_c;
+// on other boundaries phi_f = phi_c.
+__global__ void __launch_bounds__(256) grad_kernel(const ViscArgs a, const GasParams g, const BcTable bct,
+                                                   const double* __restrict__ U) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= a.n_cells) return;
+    double qc[3];
+    uvT(g, U + (size_t)c * NC, qc);
+    double gx[3] = {0.0, 0.0, 0.0}, gy[3] = {0.0, 0.0, 0.0};
+    const int4 cf = a.cfaces[c];
+    const int ent[4] = {cf.x, cf.y, cf.z, cf.w};
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        if (ent[e] < 0) break;
+        const int f = ent[e];
+        const int2 lr = a.lr[f];
+        const double2 n = a.nrm[f];
+        const double A = a.area[f];
+        const double sg = lr.x == c ? 1.0 : -1.0;
+        const double nx = sg * n.x, ny = sg * n.y;
+        double qf[3];
+        if (lr.y >= 0) {
+            double qo[3];
+            uvT(g, U + (size_t)(lr.x == c ? lr.y : lr.x) * NC, qo);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) qf[k] = 0.5 * (qc[k] + qo[k]);
+        } else {
+            const int bi = f < a.n_faces ? a.bc[f] : -1;
+            const bool wall = bi >= 0 && bct.bc[bi].type == MGPU_BC_WALL_ADIABATIC;
+            qf[0] = wall ? 0.0 : qc[0];
+            qf[1] = wall ? 0.0 : qc[1];
+            qf[2] = qc[2];
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            gx[k] = gx[k] + qf[k] * nx * A;
+            gy[k] = gy[k] + qf[k] * ny * A;
+        }
+    }
+    const double vol = a.vol[c];
+    double* go = a.grad + (size_t)c * 6;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        go[2 * k] = gx[k] / vol;
+        go[2 * k + 1] = gy[k] / vol;
+    }
+}
+
+// Navier-Stokes flux through each flux face, subtracted from G = area x F:
+// interior faces from the mean of both cells' gradients corrected by the
+// jump along the centre-to-centre line; no-slip adiabatic walls from the
+// cell's gradient corrected to the wall velocity 0 (no heat flux, no work).
+__global__ void __launch_bounds__(256) viscous_kernel(const ViscArgs a, const GasParams g, const BcTable bct,
+                                                      const double* __restrict__ U) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= a.n_faces) return;
+    const int2 lr = a.lr[f];
+    const int bi = a.bc[f];
+    const bool wall = bi >= 0 && bct.bc[bi].type == MGPU_BC_WALL_ADIABATIC;
+    if (lr.y < 0 && !wall) return;
+    double qL[3], qR[3], gf[6], dx, dy;
+    uvT(g, U + (size_t)lr.x * NC, qL);
+    const double* gL = a.grad + (size_t)lr.x * 6;
+    const double2 xL = a.xc[lr.x];
+    if (lr.y >= 0) {
+        uvT(g, U + (size_t)lr.y * NC, qR);
+        const double* gR = a.grad + (size_t)lr.y * 6;
+#pragma unroll
+        for (int i = 0; i < 6; ++i) gf[i] = 0.5 * (gL[i] + gR[i]);
+        const double2 xR = a.xc[lr.y];
+        dx = xR.x - xL.x;
+        dy = xR.y - xL.y;
+    } else {
+        qR[0] = 0.0;
+        qR[1] = 0.0;
+        qR[2] = qL[2];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) gf[i] = gL[i];
+        const double2 xF = a.xf[f];
+        dx = xF.x - xL.x;
+        dy = xF.y - xL.y;
+    }
+    const double dl = sqrt(dx * dx + dy * dy);
+    const double tx = dx / dl, ty = dy / dl;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const double corr = (qR[k] - qL[k]) / dl - (gf[2 * k] * tx + gf[2 * k + 1] * ty);
+        gf[2 * k] = gf[2 * k] + corr * tx;
+        gf[2 * k + 1] = gf[2 * k + 1] + corr * ty;
+    }
+    const double u = 0.5 * (qL[0] + qR[0]), v = 0.5 * (qL[1] + qR[1]), T = 0.5 * (qL[2] + qR[2]);
+    double mu = a.mu_ref;
+    if (a.S > 0.0) {
+        const double r = T / a.T_ref;
+        mu = a.mu_ref * (r * sqrt(r)) * ((a.T_ref + a.S) / (T + a.S));
+    }
+    const double k = mu * a.cp_over_pr;
+    const double ux = gf[0], uy = gf[1], vx = gf[2], vy = gf[3], Tx = gf[4], Ty = gf[5];
+    const double div = ux + vy;
+    const double txx = mu * (2.0 * ux - 2.0 / 3.0 * div);
+    const double tyy = mu * (2.0 * vy - 2.0 / 3.0 * div);
+    const double txy = mu * (uy + vx);
+    const double2 n = a.nrm[f];
+    double Fv[4];
+    Fv[0] = 0.0;
+    Fv[1] = txx * n.x + txy * n.y;
+    Fv[2] = txy * n.x + tyy * n.y;
+    Fv[3] = wall ? 0.0 : (u * txx + v * txy + k * Tx) * n.x + (u * txy + v * tyy + k * Ty) * n.y;
+    const double A = a.area[f];
+    double* Gf = a.G + (size_t)f * 4;
+#pragma unroll
+    for (int i = 1; i < 4; ++i) Gf[i] = Gf[i] - A * Fv[i];
+}
+
+// ---------------------------------------------------------------------------
 // Batched form (see BatchLaunch): thread (case, cell); 8 consecutive threads
 // are one 8-cell tile of one case.
 // ---------------------------------------------------------------------------
@@ -463,6 +593,14 @@ cudaError_t launch_sound(int n, double gamma, const double* U, const double* pri
     const unsigned blocks = (unsigned)((n + 255) / 256);
     if (blocks == 0) return cudaSuccess;
     sound_kernel<<<blocks, 256, 0, s>>>(n, gamma, U, prim, snd);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_viscous(const ViscArgs& a, const GasParams& g, const BcTable& bct, const double* U, cudaStream_t s) {
+    if (a.n_cells > 0) grad_kernel<<<(a.n_cells + 255) / 256, 256, 0, s>>>(a, g, bct, U);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    if (a.n_faces > 0) viscous_kernel<<<(a.n_faces + 255) / 256, 256, 0, s>>>(a, g, bct, U);
     return cudaGetLastError();
 }
 

@@ -80,7 +80,10 @@ class Solver:
                  max_stencil_size_factor=2.0, quadrature_order_cell=0, quadrature_order_face=0,
                  riemann_solver="HLLC", time_integrator="SSPRK3", gamma=1.4, p_ref=101325.0, T_ref=298.15,
                  rho_ref=1.225, p_min=-1e20, p_max=1e20, boundaries=(), teno_variant="reference", reorder=True,
-                 device=0, precision="fp64"):
+                 device=0, precision="fp64", viscous=None):
+        """viscous: None for the Euler path, or a dict with mu_ref and
+        optionally T_mu_ref, sutherland_S, prandtl (the viscous face flux,
+        no counterpart in the reference; walls become no-slip)."""
         self._lib = N.lib()
         self.mesh = mesh
         self.gas = dict(gamma=gamma, p_ref=p_ref, T_ref=T_ref, rho_ref=rho_ref)
@@ -110,6 +113,12 @@ class Solver:
         self.precision = precision
         cfg.reorder = 1 if reorder else 0
         cfg.device = int(device)
+        if viscous:
+            cfg.viscous = 1
+            cfg.mu_ref = float(viscous["mu_ref"])
+            cfg.T_mu_ref = float(viscous.get("T_mu_ref", 1.0))
+            cfg.sutherland_S = float(viscous.get("sutherland_S", 0.0))
+            cfg.prandtl = float(viscous.get("prandtl", 0.72))
         self.cfg = cfg
         self.nq = 1 if face_reconstruction == "FO" else (
             quadrature_order_face if quadrature_order_face > 0 else (basis_order + 1) // 2)

@@ -103,17 +103,30 @@ def harvest_all(sel, seed=0, quick=False, log=print):
     return rows
 
 
-def wedge_setup(mesh, mach=2.5, rho=1.4, p=1.0, riemann="Rusanov", precision="fp64_fast"):
+def wedge_viscosity(mach=2.5, rho=1.4, p=1.0, reynolds=1e5, length=1.0, prandtl=0.72):
+    """Viscous parameters of the ramp channel: mu at the inflow temperature
+    from the Reynolds number on the ramp length, Sutherland's law with the
+    air ratio S / T_inf = 110.4 / 288.15."""
+    R = GAS["p_ref"] / (GAS["T_ref"] * GAS["rho_ref"])
+    u = mach * float(np.sqrt(GAS["gamma"] * p / rho))
+    T = p / (rho * R)
+    return {"mu_ref": rho * u * length / reynolds, "T_mu_ref": T, "sutherland_S": T * 110.4 / 288.15,
+            "prandtl": prandtl}
+
+
+def wedge_setup(mesh, mach=2.5, rho=1.4, p=1.0, riemann="Rusanov", precision="fp64_fast", reynolds=None):
     """Solver and initial state of the supersonic ramp channel: uniform inflow
-    state everywhere, "upt" inflow, "p_out" outflow, slip walls."""
+    state everywhere, "upt" inflow, "p_out" outflow, walls (slip; no-slip
+    and viscous when a Reynolds number is given)."""
     R = GAS["p_ref"] / (GAS["T_ref"] * GAS["rho_ref"])
     u = mach * float(np.sqrt(GAS["gamma"] * p / rho))
     T = p / (rho * R)
     blist = [{"name": "inflow", "type": "upt", "u": [u, 0.0], "p": p, "T": T},
              {"name": "outflow", "type": "p_out", "p": p},
              {"name": "wall", "type": "wall_adiabatic"}, {"name": "top", "type": "wall_adiabatic"}]
+    visc = wedge_viscosity(mach, rho, p, reynolds) if reynolds else None
     s = Solver(mesh, face_reconstruction="TENO", basis_type="legendre", basis_order=3, riemann_solver=riemann,
-               boundaries=blist, teno_variant="corrected", precision=precision, **GAS)
+               boundaries=blist, teno_variant="corrected", precision=precision, viscous=visc, **GAS)
     n = mesh.n_cells
     U, W = state_from_primitives(np.full(n, rho), np.full(n, u), np.zeros(n), np.full(n, p), **GAS)
     return s, U, W

@@ -969,6 +969,12 @@ struct Case {
     int teno_variant = 0;
     std::vector<Bc> bcs;
     std::vector<double> U, Utmp, prim, face, r1, r2, r3, cfl_local;
+    // viscous face flux (no reference counterpart; restated from the GPU
+    // library's definition): Sutherland viscosity, Green-Gauss gradients
+    bool viscous = false;
+    double mu_ref = 0.0, T_mu_ref = 1.0, sutherland_S = 0.0, cp_over_pr = 0.0;
+    std::vector<double> grad;       // [n_cells][6]
+    std::vector<signed char> wall;  // per face: 1 on a wall_adiabatic zone
     // diagnostics: TENO decision per [cell][var]: bit0 central, bit s = stencil s passed CT2
     std::vector<uint8_t> masks;
 };
@@ -1162,6 +1168,113 @@ inline bool admissible(const Gas& g, const double* W) {
     return (g.gamma - 1.0) * rho * e > 0.0;
 }
 
+// ---------------------------------------------------------------------------
+// Viscous face flux (no counterpart in the reference)
+// ---------------------------------------------------------------------------
+
+inline void uvT(const Gas& g, const double* U, double* q) {
+    double rho = U[0];
+    double u = U[1] / rho, v = U[2] / rho;
+    double E = U[3] / rho;
+    double e = E - 0.5 * (u * u + v * v);
+    q[0] = u;
+    q[1] = v;
+    q[2] = e / g.cv;
+}
+
+// Green-Gauss gradients of (u, v, T) per cell: (1/V) sum_f phi_f n_out A,
+// phi_f the mean of the two cells, u = v = 0 and T = T_c on a wall, phi_c on
+// other boundaries.
+void viscous_gradients(Case& cs, const double* U) {
+    const OMesh& m = *cs.mesh;
+    cs.grad.assign((size_t)m.n_cells * 6, 0.0);
+    for (uint32_t c = 0; c < m.n_cells; ++c) {
+        double qc[3], gx[3] = {0, 0, 0}, gy[3] = {0, 0, 0};
+        uvT(cs.gas, U + (size_t)c * NC, qc);
+        for (uint32_t k = m.off_foc[c]; k < m.off_foc[c + 1]; ++k) {
+            uint32_t f = m.foc[k];
+            int32_t L = m.cof[2 * (size_t)f], R = m.cof[2 * (size_t)f + 1];
+            double n[2];
+            unit2(&m.face_normals[2 * (size_t)f], n);
+            double A = m.face_area[f];
+            double sg = L == (int32_t)c ? 1.0 : -1.0;
+            double nx = sg * n[0], ny = sg * n[1];
+            double qf[3];
+            if (R >= 0) {
+                double qo[3];
+                uvT(cs.gas, U + (size_t)(L == (int32_t)c ? R : L) * NC, qo);
+                for (int i = 0; i < 3; ++i) qf[i] = 0.5 * (qc[i] + qo[i]);
+            } else {
+                bool w = cs.wall[f] != 0;
+                qf[0] = w ? 0.0 : qc[0];
+                qf[1] = w ? 0.0 : qc[1];
+                qf[2] = qc[2];
+            }
+            for (int i = 0; i < 3; ++i) {
+                gx[i] = gx[i] + qf[i] * nx * A;
+                gy[i] = gy[i] + qf[i] * ny * A;
+            }
+        }
+        for (int i = 0; i < 3; ++i) {
+            cs.grad[(size_t)c * 6 + 2 * i] = gx[i] / m.cell_volume[c];
+            cs.grad[(size_t)c * 6 + 2 * i + 1] = gy[i] / m.cell_volume[c];
+        }
+    }
+}
+
+// Navier-Stokes flux through face f (unit normal n out of its first cell):
+// mean gradient corrected by the jump along the centre-to-centre line;
+// on a no-slip adiabatic wall the cell's gradient corrected to velocity 0,
+// with no heat flux and no work.
+void viscous_flux(const Case& cs, uint32_t f, bool wall, const double* U, const double* n, double* Fv) {
+    const OMesh& m = *cs.mesh;
+    int32_t L = m.cof[2 * (size_t)f], R = m.cof[2 * (size_t)f + 1];
+    double qL[3], qR[3], gf[6], dx, dy;
+    uvT(cs.gas, U + (size_t)L * NC, qL);
+    const double* gL = &cs.grad[(size_t)L * 6];
+    const double* xL = m.cc(L);
+    if (R >= 0) {
+        uvT(cs.gas, U + (size_t)R * NC, qR);
+        const double* gR = &cs.grad[(size_t)R * 6];
+        for (int i = 0; i < 6; ++i) gf[i] = 0.5 * (gL[i] + gR[i]);
+        const double* xR = m.cc(R);
+        dx = xR[0] - xL[0];
+        dy = xR[1] - xL[1];
+    } else {
+        qR[0] = 0.0;
+        qR[1] = 0.0;
+        qR[2] = qL[2];
+        for (int i = 0; i < 6; ++i) gf[i] = gL[i];
+        const double* p0 = m.nc(m.node_of_face(f, 0));
+        const double* p1 = m.nc(m.node_of_face(f, 1));
+        dx = 0.5 * (p0[0] + p1[0]) - xL[0];
+        dy = 0.5 * (p0[1] + p1[1]) - xL[1];
+    }
+    double dl = std::sqrt(dx * dx + dy * dy);
+    double tx = dx / dl, ty = dy / dl;
+    for (int k = 0; k < 3; ++k) {
+        double corr = (qR[k] - qL[k]) / dl - (gf[2 * k] * tx + gf[2 * k + 1] * ty);
+        gf[2 * k] = gf[2 * k] + corr * tx;
+        gf[2 * k + 1] = gf[2 * k + 1] + corr * ty;
+    }
+    double u = 0.5 * (qL[0] + qR[0]), v = 0.5 * (qL[1] + qR[1]), T = 0.5 * (qL[2] + qR[2]);
+    double mu = cs.mu_ref;
+    if (cs.sutherland_S > 0.0) {
+        double r = T / cs.T_mu_ref;
+        mu = cs.mu_ref * (r * std::sqrt(r)) * ((cs.T_mu_ref + cs.sutherland_S) / (T + cs.sutherland_S));
+    }
+    double k = mu * cs.cp_over_pr;
+    double ux = gf[0], uy = gf[1], vx = gf[2], vy = gf[3], Tx = gf[4], Ty = gf[5];
+    double div = ux + vy;
+    double txx = mu * (2.0 * ux - 2.0 / 3.0 * div);
+    double tyy = mu * (2.0 * vy - 2.0 / 3.0 * div);
+    double txy = mu * (uy + vx);
+    Fv[0] = 0.0;
+    Fv[1] = txx * n[0] + txy * n[1];
+    Fv[2] = txy * n[0] + tyy * n[1];
+    Fv[3] = wall ? 0.0 : (u * txx + v * txy + k * Tx) * n[0] + (u * txy + v * tyy + k * Ty) * n[1];
+}
+
 void face_flux(Case& cs, uint32_t f, int bc, const Bc* b, const double* U, const double* face, double* rhs) {
     const OMesh& m = *cs.mesh;
     double F[4] = {0, 0, 0, 0}, Ft[4], cl[4], cr[4], pl[5], pr[5], n[2];
@@ -1194,9 +1307,14 @@ void face_flux(Case& cs, uint32_t f, int bc, const Bc* b, const double* U, const
     }
     for (int i = 0; i < NC; i++) F[i] *= 0.5;
     int32_t L = m.cof[2 * (size_t)f], R = m.cof[2 * (size_t)f + 1];
+    double Fv[4] = {0.0, 0.0, 0.0, 0.0};
+    const bool visc = cs.viscous && (bc < 0 || bc == BC_WALL_ADIABATIC);
+    if (visc) viscous_flux(cs, f, bc == BC_WALL_ADIABATIC, U, n, Fv);
     for (int i = 0; i < NC; i++) {
-        scatter_add(&rhs[(size_t)L * NC + i], -m.face_area[f] * F[i]);
-        if (bc < 0 && R >= 0) scatter_add(&rhs[(size_t)R * NC + i], m.face_area[f] * F[i]);
+        double g = m.face_area[f] * F[i];
+        if (visc && i > 0) g = g - m.face_area[f] * Fv[i];
+        scatter_add(&rhs[(size_t)L * NC + i], -g);
+        if (bc < 0 && R >= 0) scatter_add(&rhs[(size_t)R * NC + i], g);
     }
 }
 
@@ -1205,6 +1323,13 @@ void calc_rhs(Case& cs, const double* U, double* face, double* rhs) {
     const OMesh& m = *cs.mesh;
     for (size_t i = 0; i < (size_t)m.n_cells * NC; i++) rhs[i] = 0.0;
     recon(cs, U, face);
+    if (cs.viscous) {
+        cs.wall.assign(m.n_faces, 0);
+        for (const Bc& b : cs.bcs)
+            if (b.type == BC_WALL_ADIABATIC)
+                for (uint32_t k = m.zone_off[b.zone]; k < m.zone_off[b.zone + 1]; ++k) cs.wall[m.zone_faces[k]] = 1;
+        viscous_gradients(cs, U);
+    }
     uint32_t z0 = m.zone_off[0], z1 = m.zone_off[1];
 #pragma omp parallel for if (g_threads > 1) num_threads(g_threads)
     for (int64_t k = z0; k < (int64_t)z1; ++k) face_flux(cs, m.zone_faces[k], -1, nullptr, U, face, rhs);
@@ -1516,6 +1641,17 @@ void orc_case_get_state(void* h, double* U, double* prim) {
 int orc_case_nq(void* h) { return static_cast<Case*>(h)->nq; }
 
 void orc_case_set_teno_variant(void* h, int variant) { static_cast<Case*>(h)->teno_variant = variant; }
+
+// Viscous face flux on (mu_ref > 0 or Sutherland) / off (viscous = 0).
+void orc_case_set_viscous(void* h, int viscous, double mu_ref, double T_mu_ref, double sutherland_S, double prandtl) {
+    Case* cs = static_cast<Case*>(h);
+    cs->viscous = viscous != 0;
+    cs->mu_ref = mu_ref;
+    cs->T_mu_ref = T_mu_ref;
+    cs->sutherland_S = sutherland_S;
+    const double cp = cs->gas.R * cs->gas.gamma / (cs->gas.gamma - 1.0);
+    cs->cp_over_pr = cp / prandtl;
+}
 
 // FaceReconstruction::calc_face_values; face must hold n_faces*nq*2*4 doubles.
 // masks (optional, [n_cells][4]) receives the TENO decision bits.

@@ -79,6 +79,7 @@ def load():
         "orc_case_get_state": (None, [vp, vp, vp]),
         "orc_case_nq": (i32, [vp]),
         "orc_case_set_teno_variant": (None, [vp, i32]),
+        "orc_case_set_viscous": (None, [vp, i32, f64, f64, f64, f64]),
         "orc_case_face_values": (i32, [vp, vp, vp, vp]),
         "orc_case_calc_rhs": (i32, [vp, vp, vp]),
         "orc_case_calc_dt": (i32, [vp, f64, C.POINTER(f64), vp]),
@@ -179,6 +180,11 @@ class OracleCase:
     def set_teno_variant(self, variant):
         """0: the reference's weighting; 1: cut-off weighting (see the C source)."""
         self._lib.orc_case_set_teno_variant(self.h, int(variant))
+
+    def set_viscous(self, mu_ref, T_mu_ref=1.0, sutherland_S=0.0, prandtl=0.72, viscous=True):
+        """The viscous face flux (no reference counterpart; see the C source)."""
+        self._lib.orc_case_set_viscous(self.h, 1 if viscous else 0, float(mu_ref), float(T_mu_ref),
+                                       float(sutherland_S), float(prandtl))
 
     def add_boundary(self, zone, bc_type, data=()):
         d = np.asarray(data, dtype=np.float64)

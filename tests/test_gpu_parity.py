@@ -272,3 +272,54 @@ def test_ramp_channel_wedge_parity():
     Uo, _ = oc.get_state()
     assert_close(Ug, Uo, RUN_TOL, what="ramp channel 20 steps")
     s.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_viscous_ramp_channel_parity(precision):
+    """The viscous face flux (no reference counterpart; the oracle restates
+    the library's definition): Green-Gauss gradients, Sutherland viscosity,
+    no-slip adiabatic walls, at an exaggerated viscosity (Re = 200) so that it
+    matters.  FP64: one residual at 1e-12 and 20 steps at 1e-10 against the
+    oracle; FP32 form: residual at its own tolerance."""
+    from mallard_gb300.train_selector import wedge_setup, wedge_viscosity
+    from cases import GAS
+    from oracle import OracleCase, OracleMesh
+    m = mg.Mesh.ramp_channel(36, 12, 3.0, 1.0, 0.5, 15.0, 0.2, seed=11)
+    m.permute_cells(3)
+    s, U, W = wedge_setup(m, mach=2.5, precision=precision, reynolds=200.0)
+    visc = wedge_viscosity(2.5, reynolds=200.0)
+    oc = OracleCase(OracleMesh.from_arrays(m), recon="TENO", basis="legendre", poly_order=3, riemann="Rusanov",
+                    **GAS)
+    oc.set_teno_variant(1)
+    oc.set_viscous(visc["mu_ref"], visc["T_mu_ref"], visc["sutherland_S"], visc["prandtl"])
+    R = GAS["p_ref"] / (GAS["T_ref"] * GAS["rho_ref"])
+    u = 2.5 * np.sqrt(GAS["gamma"] * 1.0 / 1.4)
+    oc.add_boundary(m.zone_index("inflow"), "upt", (u, 0.0, 1.0, 1.0 / (1.4 * R)))
+    oc.add_boundary(m.zone_index("outflow"), "p_out", (1.0,))
+    oc.add_boundary(m.zone_index("wall"), "wall_adiabatic")
+    oc.add_boundary(m.zone_index("top"), "wall_adiabatic")
+    r = np.random.default_rng(4)
+    Up = U * (1 + 0.02 * r.standard_normal(U.shape))
+    rg, ro = s.calc_rhs(Up), oc.calc_rhs(Up)
+    # the viscous part is not negligible at this Reynolds number
+    oi = OracleCase(OracleMesh.from_arrays(m), recon="TENO", basis="legendre", poly_order=3, riemann="Rusanov",
+                    **GAS)
+    oi.set_teno_variant(1)
+    for zone, typ, data in (("inflow", "upt", (u, 0.0, 1.0, 1.0 / (1.4 * R))), ("outflow", "p_out", (1.0,)),
+                            ("wall", "wall_adiabatic", ()), ("top", "wall_adiabatic", ())):
+        oi.add_boundary(m.zone_index(zone), typ, data)
+    rinv = oi.calc_rhs(Up)
+    assert np.abs(ro - rinv).max() > 1e-3 * np.abs(rinv).max()
+    if precision == "fp64":
+        assert_close(rg, ro, STAGE_TOL, what="viscous residual")
+        s.set_state(U, W)
+        oc.set_state(U, W)
+        s.run(0.4, 20)
+        oc.run(0.4, 20)
+        Ug, _ = s.get_state()
+        Uo, _ = oc.get_state()
+        assert_close(Ug, Uo, RUN_TOL, what="viscous 20 steps")
+    else:
+        err = rel_err(rg, ro)
+        assert np.median(err) < 1e-5 and err.max() < 1e-2, (np.median(err), err.max())
+    s.close()
