@@ -85,6 +85,7 @@ struct UpdateArgs {
     double* prim;
     double* snd;            // sound speed per cell, written with prim
     double* rhs;            // residual output (stage 0 only)
+    float* u32;             // FP32 copy of the stage's output state (FP32 form), or null
     unsigned* flags;
 };
 
@@ -142,10 +143,11 @@ namespace f32 {
 // registers, or 256-thread blocks with 64; p = 3 only, other orders use
 // shape 0), chosen by the autotuner
 constexpr int TENO32_SHAPES = 4;
-cudaError_t launch_teno(const TenoArgs& a, int K, int M, int nq, const double* U, float* fv, uint8_t* masks,
+// U: the FP32 copy of the stage state
+cudaError_t launch_teno(const TenoArgs& a, int K, int M, int nq, const float* U, float* fv, uint8_t* masks,
                         int shape, cudaStream_t s);
 // with the learned selector's predictions (p = 3 only)
-cudaError_t launch_teno_selected(const TenoArgs& a, int K, int M, int nq, const double* U, const uint8_t* pred,
+cudaError_t launch_teno_selected(const TenoArgs& a, int K, int M, int nq, const float* U, const uint8_t* pred,
                                  float* fv, uint8_t* masks, int shape, cudaStream_t s);
 cudaError_t launch_flux(const FluxArgs& a, const float* fv, const GasParams& g, const BcTable& bct, int rsolver,
                         int nq, cudaStream_t s);
@@ -178,6 +180,7 @@ struct BatchLaunch {
     const SpecArgs* spec;
     // state of all cases
     double *U, *Ut, *W, *prim, *snd, *G;
+    float *U32, *Ut32;               // FP32 copies of U and Ut
     float* fv;
     double *dt, *t;                  // per case
     unsigned long long* rmax;        // per case
@@ -185,7 +188,7 @@ struct BatchLaunch {
 };
 
 namespace f32 {
-cudaError_t launch_teno_batch(const BatchLaunch& b, const double* U, int shape, int blocks_per_sm, cudaStream_t s);
+cudaError_t launch_teno_batch(const BatchLaunch& b, const float* U, int shape, int blocks_per_sm, cudaStream_t s);
 cudaError_t launch_flux_batch(const BatchLaunch& b, const GasParams& g, const BcTable& bct, int rsolver, int nq,
                               const double* U, cudaStream_t s);
 }  // namespace f32
@@ -195,8 +198,10 @@ cudaError_t launch_dt_batch(const BatchLaunch& b, int n_cases, double cfl, cudaS
 // caller-order rows of one case <-> its interleaved internal rows
 cudaError_t launch_batch_rows(int n, int width, const uint32_t* perm_old, const double* src, double* dst,
                               unsigned long long ubase, unsigned C, unsigned cs, bool to_batch, cudaStream_t s);
-cudaError_t launch_batch_prims(int n, const GasParams& g, double* U, double* prim, double* snd,
+cudaError_t launch_batch_prims(int n, const GasParams& g, double* U, double* prim, double* snd, float* U32,
                                unsigned long long ubase, unsigned C, unsigned cs, cudaStream_t s);
+// FP32 copy of n doubles (round to nearest)
+cudaError_t launch_to_f32(size_t n, const double* src, float* dst, cudaStream_t s);
 
 // kernels.cu
 cudaError_t launch_first_order(int n_faces, const int2* lr, const double* U, double* fv, cudaStream_t s);

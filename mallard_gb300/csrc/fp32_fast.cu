@@ -6,6 +6,8 @@
 //  * FP64: the table build (least squares, face shapes; the tables are
 //    rounded to FP32 once, on upload), geometry (normals, areas,
 //    volumes), the conserved state and its accumulation across RK stages
+//    (the update kernel also writes an FP32 copy of each stage's state,
+//    which the reconstruction gathers)
 //    (the FP64 update kernel), and primitive recovery near vacuum: when the
 //    internal energy is under 1e-3 of the total the face state is recovered
 //    in FP64.
@@ -47,13 +49,13 @@ struct IxB {
 // Reconstruction of variable v of one cell.  live: lanes of the warp whose
 // cells exist (the four lanes of a cell share its fate).
 template <int K, int M, int NQ, bool SEL, class IX>
-__device__ __forceinline__ void teno32_cell(const TenoArgs& a, const double* __restrict__ U, float* __restrict__ fv,
+__device__ __forceinline__ void teno32_cell(const TenoArgs& a, const float* __restrict__ U, float* __restrict__ fv,
                                             uint8_t* __restrict__ masks, const uint8_t* __restrict__ pred, int cell,
                                             int v, unsigned live, const IX& ix) {
     constexpr int KR = K - 1, MR = M - 1, NF = 3, S = 4;
     constexpr int GJ = (MR + 3) / 4, GP = (MR * KR + 3) / 4, GF = (NF * NQ * KR + 3) / 4;
     const int tile = cell >> 3, lane = cell & 7;
-    const float uc = f(U[ix.u(cell) * NC + v]);
+    const float uc = U[ix.u(cell) * NC + v];
     const unsigned sm = a.smask[cell];
     unsigned need = sm, pm = 0;
     bool conf = false;
@@ -84,7 +86,7 @@ __device__ __forceinline__ void teno32_cell(const TenoArgs& a, const double* __r
             const uint32_t id[4] = {n.x, n.y, n.z, n.w};
 #pragma unroll
             for (int e = 0; e < 4; ++e)
-                if (g * 4 + e < MR) d[g * 4 + e] = f(__ldg(U + ix.u(id[e]) * NC + v)) - uc;
+                if (g * 4 + e < MR) d[g * 4 + e] = __ldg(U + ix.u(id[e]) * NC + v) - uc;
         }
         // coefficients = (P x areas) . d, accumulated over the stencil in order
         const float4* Pp = reinterpret_cast<const float4*>(a.P4) + ((size_t)(tile * S + s) * GP) * TILE + lane;
@@ -194,7 +196,7 @@ __device__ __forceinline__ void teno32_cell(const TenoArgs& a, const double* __r
 }
 
 template <int K, int M, int NQ, bool SEL, int BS, int MINB>
-__global__ void __launch_bounds__(BS, MINB) teno32_kernel(const TenoArgs a, const double* __restrict__ U,
+__global__ void __launch_bounds__(BS, MINB) teno32_kernel(const TenoArgs a, const float* __restrict__ U,
                                                           float* __restrict__ fv, uint8_t* __restrict__ masks,
                                                           const uint8_t* __restrict__ pred) {
     const int gt = blockIdx.x * blockDim.x + threadIdx.x;
@@ -329,7 +331,7 @@ cudaError_t flux_nq(const FluxArgs& a, const float* fv, const GasParams& g, cons
 }
 
 template <int K, int M, int NQ, bool SEL, int BS, int MINB>
-cudaError_t teno_go1(const TenoArgs& a, const double* U, float* fv, uint8_t* masks, const uint8_t* pred,
+cudaError_t teno_go1(const TenoArgs& a, const float* U, float* fv, uint8_t* masks, const uint8_t* pred,
                      cudaStream_t s) {
     const long long threads = (long long)a.n_cells * 4;
     const unsigned blocks = (unsigned)((threads + BS - 1) / BS);
@@ -340,7 +342,7 @@ cudaError_t teno_go1(const TenoArgs& a, const double* U, float* fv, uint8_t* mas
 // Launch shapes the autotuner chooses from: (block size, minimum resident
 // blocks per SM), i.e. register caps of 128, 80 and 64 per thread.
 template <int K, int M, int NQ, bool SEL>
-cudaError_t teno_go(const TenoArgs& a, const double* U, float* fv, uint8_t* masks, const uint8_t* pred, int shape,
+cudaError_t teno_go(const TenoArgs& a, const float* U, float* fv, uint8_t* masks, const uint8_t* pred, int shape,
                     cudaStream_t s) {
     switch (shape) {
         case 0: return teno_go1<K, M, NQ, SEL, 128, 4>(a, U, fv, masks, pred, s);
@@ -362,7 +364,7 @@ __device__ __forceinline__ int batch_group(const long long* start, int n, long l
 // threads = one 8-cell tile of one case, consecutive tiles = the same mesh
 // tile of consecutive cases (so a table tile is reused from cache).
 template <int K, int M, int NQ, int BS, int MINB>
-__global__ void __launch_bounds__(BS, MINB) teno32_batch_kernel(const BatchLaunch b, const double* __restrict__ U) {
+__global__ void __launch_bounds__(BS, MINB) teno32_batch_kernel(const BatchLaunch b, const float* __restrict__ U) {
     const long long total = b.teno0[b.n_groups];
     for (long long gt = (long long)blockIdx.x * BS + threadIdx.x; gt < total; gt += (long long)gridDim.x * BS) {
         const int gi = batch_group(b.teno0, b.n_groups, gt);
@@ -395,7 +397,7 @@ __global__ void __launch_bounds__(128) flux32_batch_kernel(const BatchLaunch b, 
 }
 
 template <int K, int M, int NQ, int BS, int MINB>
-cudaError_t teno_batch_go(const BatchLaunch& b, const double* U, int blocks_per_sm, cudaStream_t s) {
+cudaError_t teno_batch_go(const BatchLaunch& b, const float* U, int blocks_per_sm, cudaStream_t s) {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -408,7 +410,7 @@ cudaError_t teno_batch_go(const BatchLaunch& b, const double* U, int blocks_per_
 
 }  // namespace
 
-cudaError_t launch_teno_batch(const BatchLaunch& b, const double* U, int shape, int blocks_per_sm, cudaStream_t s) {
+cudaError_t launch_teno_batch(const BatchLaunch& b, const float* U, int shape, int blocks_per_sm, cudaStream_t s) {
     switch (shape) {
         case 0: return teno_batch_go<10, 20, 2, 128, 4>(b, U, blocks_per_sm, s);
         case 1: return teno_batch_go<10, 20, 2, 128, 6>(b, U, blocks_per_sm, s);
@@ -436,7 +438,7 @@ cudaError_t launch_flux_batch(const BatchLaunch& b, const GasParams& g, const Bc
     return cudaGetLastError();
 }
 
-cudaError_t launch_teno(const TenoArgs& a, int K, int M, int nq, const double* U, float* fv, uint8_t* masks,
+cudaError_t launch_teno(const TenoArgs& a, int K, int M, int nq, const float* U, float* fv, uint8_t* masks,
                         int shape, cudaStream_t s) {
     if (K == 10 && M == 20 && nq == 2) return teno_go<10, 20, 2, false>(a, U, fv, masks, nullptr, shape, s);
     if (K == 6 && M == 12 && nq == 1) return teno_go1<6, 12, 1, false, 128, 4>(a, U, fv, masks, nullptr, s);
@@ -444,7 +446,7 @@ cudaError_t launch_teno(const TenoArgs& a, int K, int M, int nq, const double* U
     return cudaErrorInvalidValue;
 }
 
-cudaError_t launch_teno_selected(const TenoArgs& a, int K, int M, int nq, const double* U, const uint8_t* pred,
+cudaError_t launch_teno_selected(const TenoArgs& a, int K, int M, int nq, const float* U, const uint8_t* pred,
                                  float* fv, uint8_t* masks, int shape, cudaStream_t s) {
     if (K == 10 && M == 20 && nq == 2) return teno_go<10, 20, 2, true>(a, U, fv, masks, pred, shape, s);
     return cudaErrorInvalidValue;

@@ -28,7 +28,7 @@ struct mgpu_batch {
     cudaStream_t stream = nullptr, stream_owned = nullptr;  // launch stream; the batch's own
     BatchLaunch bl{};
     DevArray<double> U, Ut, W, prim, snd, G, dt, t;
-    DevArray<float> fv;
+    DevArray<float> fv, U32, Ut32;
     DevArray<unsigned long long> rmax;
     DevArray<unsigned> flags;
     DevArray<TenoArgs> d_teno;
@@ -68,7 +68,8 @@ void batch_step(mgpu_batch* b, double cfl) {
     ck(launch_dt_batch(b->bl, (int)b->n_cases, cfl, b->stream), "dt");
     for (int k = 1; k <= 3; ++k) {
         const double* in = k == 1 ? b->U.p : b->Ut.p;
-        ck(f32::launch_teno_batch(b->bl, in, b->teno_shape, b->teno_blocks_per_sm, b->stream), "reconstruction");
+        const float* in32 = k == 1 ? b->U32.p : b->Ut32.p;
+        ck(f32::launch_teno_batch(b->bl, in32, b->teno_shape, b->teno_blocks_per_sm, b->stream), "reconstruction");
         ck(f32::launch_flux_batch(b->bl, g0.gas, g0.bct, b->cfg.riemann_solver, g0.nq, in, b->stream), "flux");
         ck(launch_update_batch(b->bl, g0.gas, k, b->stream), "update");
     }
@@ -200,6 +201,8 @@ int mgpu_batch_finalize(mgpu_batch* b) {
         b->Ut.alloc(rows * 4);
         b->W.alloc(rows * 4);
         b->prim.alloc(rows * 5);
+        b->U32.alloc(rows * 4);
+        b->Ut32.alloc(rows * 4);
         b->snd.alloc(rows);
         b->fv.alloc(frows * nq * 8);
         b->G.alloc(frows * 4);
@@ -219,6 +222,8 @@ int mgpu_batch_finalize(mgpu_batch* b) {
         bl.Ut = b->Ut.p;
         bl.W = b->W.p;
         bl.prim = b->prim.p;
+        bl.U32 = b->U32.p;
+        bl.Ut32 = b->Ut32.p;
         bl.snd = b->snd.p;
         bl.G = b->G.p;
         bl.fv = b->fv.p;
@@ -246,8 +251,8 @@ int mgpu_batch_set_state(mgpu_batch* b, uint32_t group, uint32_t cs, const doubl
         ck(launch_batch_rows((int)c.N, 4, c.perm_old.p, c.staging.p, b->U.p, b->bl.ubase[group], b->C[group], cs,
                              true, b->stream),
            "rows");
-        ck(launch_batch_prims((int)c.N, c.gas, b->U.p, b->prim.p, b->snd.p, b->bl.ubase[group], b->C[group], cs,
-                              b->stream),
+        ck(launch_batch_prims((int)c.N, c.gas, b->U.p, b->prim.p, b->snd.p, b->U32.p, b->bl.ubase[group], b->C[group],
+                              cs, b->stream),
            "primitives");
         if (primh) {
             ck(cudaMemcpyAsync(c.staging.p, primh, (size_t)c.N * 5 * sizeof(double), cudaMemcpyHostToDevice,
@@ -371,10 +376,10 @@ int mgpu_batch_autotune(mgpu_batch* b, double* ms, int* shape, int* blocks_per_s
         int bs = 0, bg = 0;
         for (int sh = 0; sh < f32::TENO32_SHAPES; ++sh)
             for (int gi = 0; gi < 4; ++gi) {
-                ck(f32::launch_teno_batch(b->bl, b->U.p, sh, grids[gi], b->stream), "reconstruction");
+                ck(f32::launch_teno_batch(b->bl, b->U32.p, sh, grids[gi], b->stream), "reconstruction");
                 ck(cudaEventRecord(e0, b->stream), "cudaEventRecord");
                 for (int r = 0; r < 3; ++r)
-                    ck(f32::launch_teno_batch(b->bl, b->U.p, sh, grids[gi], b->stream), "reconstruction");
+                    ck(f32::launch_teno_batch(b->bl, b->U32.p, sh, grids[gi], b->stream), "reconstruction");
                 ck(cudaEventRecord(e1, b->stream), "cudaEventRecord");
                 ck(cudaEventSynchronize(e1), "cudaEventSynchronize");
                 float f = 0.f;

@@ -403,7 +403,11 @@ void mgpu_ctx::build() {
     prim.alloc((size_t)N * 5);
     snd.alloc(N);
     rho_cell.alloc(N);
-    if (cfg.precision == MGPU_PREC_FP32) fv32.alloc((size_t)F_real * nq * 8);
+    if (cfg.precision == MGPU_PREC_FP32) {
+        fv32.alloc((size_t)F_real * nq * 8);
+        U32.alloc((size_t)N * 4);
+        Ut32.alloc((size_t)N * 4);
+    }
     else fv.alloc((size_t)F_real * nq * 8);
     G.alloc((size_t)F_flux * 4);
     scal.alloc(2);
@@ -643,6 +647,7 @@ int mgpu_set_state(mgpu_ctx* ctx, const double* Uh, const double* primh) {
             ck(launch_primitives_batch(ctx->gas, ctx->N, ctx->U.p, ctx->prim.p, ctx->stream), "primitives");
         }
         ck(launch_sound((int)ctx->N, ctx->gas.gamma, ctx->U.p, ctx->prim.p, ctx->snd.p, ctx->stream), "sound speed");
+        if (ctx->single()) ck(launch_to_f32((size_t)ctx->N * 4, ctx->U.p, ctx->U32.p, ctx->stream), "FP32 copy");
         ck(cudaMemsetAsync(ctx->flags.p, 0, sizeof(unsigned), ctx->stream), "cudaMemsetAsync");
         ck(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
         return MGPU_OK;
@@ -666,6 +671,7 @@ int mgpu_calc_face_values(mgpu_ctx* ctx, const double* Uh, double* face, uint8_t
         const bool sgl = ctx->single();
         if (sgl) ck(cudaMemsetAsync(ctx->fv32.p, 0, ctx->fv32.bytes(), ctx->stream), "cudaMemsetAsync");
         else ck(cudaMemsetAsync(ctx->fv.p, 0, ctx->fv.bytes(), ctx->stream), "cudaMemsetAsync");
+        if (ctx->single()) ck(launch_to_f32((size_t)ctx->N * 4, ctx->Ut.p, ctx->Ut32.p, ctx->stream), "FP32 copy");
         ctx->reconstruct(ctx->Ut.p, ctx->masks.p);
         const int nq = ctx->nq;
         std::vector<double> tmp((size_t)ctx->F_real * nq * 8);
@@ -699,6 +705,7 @@ int mgpu_calc_rhs(mgpu_ctx* ctx, const double* Uh, double* rhsh) {
     return guarded([&] {
         if (!Uh || !rhsh) throw ArgFail("null argument");
         ctx->upload_cells(ctx->Ut.p, Uh, 4);
+        if (ctx->single()) ck(launch_to_f32((size_t)ctx->N * 4, ctx->Ut.p, ctx->Ut32.p, ctx->stream), "FP32 copy");
         ctx->reconstruct(ctx->Ut.p, nullptr);
         ctx->flux(ctx->Ut.p);
         ctx->viscous(ctx->Ut.p);

@@ -87,7 +87,8 @@ struct mgpu_ctx {
 
     // device state and work arrays
     DevArray<double> U, Ut, W, prim, vol, fv, G, rho_cell, rhs, scal;  // scal: dt, t
-    DevArray<float> fv32;  // face states of the FP32-bulk form
+    DevArray<float> fv32;        // face states of the FP32-bulk form
+    DevArray<float> U32, Ut32;   // FP32 copies of U and Ut (FP32-bulk form)
     // learned stencil selector (FP32 form): weight image, predictions
     bool sel_on = false;
     float sel_thr_central = 0.0f, sel_thr_directional = 0.0f;
@@ -168,20 +169,21 @@ struct mgpu_ctx {
 
     // predict: run the selector on Uin (otherwise reuse its last predictions)
     void reconstruct(const double* Uin, uint8_t* mask_out, bool predict = true) {
+        const float* u32 = Uin == U.p ? U32.p : Ut32.p;  // the FP32 form reads the FP32 copy
         if (single() && sel_on) {
             if (predict) {
                 timed(4, [&] {
-                    return sel::launch_mlp_cells(sel_wimg.p, teno, Uin, sel_thr_central, sel_thr_directional, pred.p,
+                    return sel::launch_mlp_cells(sel_wimg.p, teno, u32, sel_thr_central, sel_thr_directional, pred.p,
                                                  sel_err.p, stream);
                 });
                 timed(4, [&] { return sel::launch_trust((int)N, cfaces.p, lr.p, pred.p, trusted.p, stream); });
             }
             timed(0, [&] {
-                return f32::launch_teno_selected(teno, K, M, nq, Uin, trusted.p, fv32.p, mask_out, teno_shape,
+                return f32::launch_teno_selected(teno, K, M, nq, u32, trusted.p, fv32.p, mask_out, teno_shape,
                                                  stream);
             });
         } else if (single()) {
-            timed(0, [&] { return f32::launch_teno(teno, K, M, nq, Uin, fv32.p, mask_out, teno_shape, stream); });
+            timed(0, [&] { return f32::launch_teno(teno, K, M, nq, u32, fv32.p, mask_out, teno_shape, stream); });
         } else if (cfg.recon == MGPU_RECON_TENO) {
             timed(0, [&] {
                 return fast() ? fast::launch_teno(teno, K, M, nq, cfg.teno_variant, Uin, fv.p, mask_out, stream)
@@ -247,6 +249,7 @@ struct mgpu_ctx {
         flux(in);
         viscous(in);
         UpdateArgs a = update_args();
+        if (single()) a.u32 = k == 3 ? U32.p : Ut32.p;
         timed(2, [&] { return launch_update(a, gas, k, rcp(), stream); });
     }
 

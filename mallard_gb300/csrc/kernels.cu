@@ -14,6 +14,7 @@
 // residual is deterministic and identical to Kokkos::Serial's.
 #include <cstdint>
 
+#include "fp_convert.cuh"
 #include "physics.cuh"
 
 namespace mgpu {
@@ -78,7 +79,12 @@ struct IxB {
 struct StageState {
     const double* G;
     double *U, *Ut, *W, *prim, *snd, *rhs;
+    float* u32;  // FP32 copy of the stage's output state, or null
 };
+
+__device__ __forceinline__ void store_f32(float* dst, const double* x) {
+    *reinterpret_cast<float4*>(dst) = make_float4(f32_rn(x[0]), f32_rn(x[1]), f32_rn(x[2]), f32_rn(x[3]));
+}
 
 template <int STAGE, bool FAST, class IX>
 __device__ __forceinline__ void update_cell(const UpdateArgs& a, const StageState& st, const GasParams& g, int c,
@@ -136,6 +142,7 @@ __device__ __forceinline__ void update_cell(const UpdateArgs& a, const StageStat
         Ut2[1] = make_double2(t[2], t[3]);
         Wo2[0] = make_double2(w[0], w[1]);
         Wo2[1] = make_double2(w[2], w[3]);
+        if (st.u32) store_f32(st.u32 + row * 4, t);
     } else if (STAGE == 2) {
         const double2 u0 = U2[0], u1 = U2[1], s0 = Ut2[0], s1 = Ut2[1], w0 = W2[0], w1 = W2[1];
         const double u[4] = {u0.x, u0.y, u1.x, u1.y};
@@ -153,6 +160,7 @@ __device__ __forceinline__ void update_cell(const UpdateArgs& a, const StageStat
         Ut2[1] = make_double2(t[2], t[3]);
         Wo2[0] = make_double2(w[0], w[1]);
         Wo2[1] = make_double2(w[2], w[3]);
+        if (st.u32) store_f32(st.u32 + row * 4, t);
     } else {
         const double2 w0 = W2[0], w1 = W2[1];
         const double w[4] = {w0.x, w0.y, w1.x, w1.y};
@@ -163,6 +171,7 @@ __device__ __forceinline__ void update_cell(const UpdateArgs& a, const StageStat
         double2* Uo2 = reinterpret_cast<double2*>(st.U + row * 4);
         Uo2[0] = make_double2(u[0], u[1]);
         Uo2[1] = make_double2(u[2], u[3]);
+        if (st.u32) store_f32(st.u32 + row * 4, u);
         double p[5];
         if (FAST) primitives_rcp(g, u, p);
         else primitives(g, u, p);
@@ -181,7 +190,7 @@ template <int STAGE, bool FAST>
 __global__ void __launch_bounds__(256) update_kernel(const UpdateArgs a, const GasParams g) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= a.n_cells) return;
-    const StageState st{a.G, a.U, a.Ut, a.W, a.prim, a.snd, a.rhs};
+    const StageState st{a.G, a.U, a.Ut, a.W, a.prim, a.snd, a.rhs, a.u32};
     update_cell<STAGE, FAST>(a, st, g, c, Ix1{}, a.dt, a.flags);
 }
 
@@ -422,7 +431,7 @@ __global__ void __launch_bounds__(256) update_batch_kernel(const BatchLaunch b, 
         const int c = (int)(tc / C) * 8 + (int)(t & 7);
         const unsigned gc = b.case0[gi] + cs;
         if (c >= b.n_cells[gi] || b.flags[gc] != 0u) continue;
-        const StageState st{b.G, b.U, b.Ut, b.W, b.prim, b.snd, nullptr};
+        const StageState st{b.G, b.U, b.Ut, b.W, b.prim, b.snd, nullptr, STAGE == 3 ? b.U32 : b.Ut32};
         update_cell<STAGE, true>(b.upd[gi], st, g, c, IxB{b.ubase[gi], b.fbase[gi], C, cs}, b.dt + gc, b.flags + gc);
     }
 }
@@ -474,7 +483,8 @@ __global__ void batch_rows_kernel(int n, int width, const uint32_t* __restrict__
 
 // primitives (the reference's arithmetic) and sound speed of one case's rows
 __global__ void batch_prims_kernel(int n, const GasParams g, const double* __restrict__ U, double* __restrict__ prim,
-                                   double* __restrict__ snd, unsigned long long ubase, unsigned C, unsigned cs) {
+                                   double* __restrict__ snd, float* __restrict__ U32, unsigned long long ubase,
+                                   unsigned C, unsigned cs) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= n) return;
     const size_t row = ubase + (((size_t)(c >> 3) * C + cs) << 3) + (c & 7);
@@ -485,6 +495,12 @@ __global__ void batch_prims_kernel(int n, const GasParams g, const double* __res
 #pragma unroll
     for (int k = 0; k < 5; k++) prim[row * 5 + k] = w[k];
     snd[row] = sound_speed(g.gamma, u[0], w);
+    if (U32) store_f32(U32 + row * 4, u);
+}
+
+__global__ void to_f32_kernel(size_t n, const double* __restrict__ src, float* __restrict__ dst) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = f32_rn(src[i]);
 }
 
 __global__ void dt_kernel(const unsigned long long* rmax_bits, double cfl, double* dt, double* t, unsigned* flags) {
@@ -635,9 +651,14 @@ cudaError_t launch_batch_rows(int n, int width, const uint32_t* perm_old, const 
     return cudaGetLastError();
 }
 
-cudaError_t launch_batch_prims(int n, const GasParams& g, double* U, double* prim, double* snd,
+cudaError_t launch_batch_prims(int n, const GasParams& g, double* U, double* prim, double* snd, float* U32,
                                unsigned long long ubase, unsigned C, unsigned cs, cudaStream_t s) {
-    if (n > 0) batch_prims_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, g, U, prim, snd, ubase, C, cs);
+    if (n > 0) batch_prims_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, g, U, prim, snd, U32, ubase, C, cs);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_to_f32(size_t n, const double* src, float* dst, cudaStream_t s) {
+    if (n) to_f32_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, src, dst);
     return cudaGetLastError();
 }
 

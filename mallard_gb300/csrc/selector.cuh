@@ -52,9 +52,9 @@ __device__ __forceinline__ uint32_t stencil_cell(const TenoArgs& a, int tile, in
 
 // The 19 stencil values of variable v minus uc, for stencil s of a cell.
 // NB4: 16-byte index loads from the FP32 form's grouped layout.
-template <bool NB4, class ToF>
-__device__ __forceinline__ void stencil_diffs(const TenoArgs& a, const double* __restrict__ U, int tile, int lane,
-                                              int s, int v, float uc, ToF to_f, float* d) {
+template <bool NB4, class T, class ToF>
+__device__ __forceinline__ void stencil_diffs(const TenoArgs& a, const T* __restrict__ U, int tile, int lane, int s,
+                                              int v, float uc, ToF to_f, float* d) {
     if (NB4) {
         constexpr int GJ = (MR + 3) / 4;
         const uint4* p = reinterpret_cast<const uint4*>(a.nb4) + (((size_t)tile * S + s) * GJ) * TILE + lane;
@@ -75,12 +75,12 @@ __device__ __forceinline__ void stencil_diffs(const TenoArgs& a, const double* _
     }
 }
 
-// Features of variable v of one cell, from the FP64 state (values rounded
-// to FP32 first, as the FP32 form reads them).  Writes PER_VAR floats.
-// to_f converts an FP64 state value to FP32.
-template <bool NB4, class ToF>
-__device__ __forceinline__ void features(const TenoArgs& a, const double* __restrict__ U, int cell, int v,
-                                         unsigned smask, ToF to_f, float* x) {
+// Features of variable v of one cell, from the state U (FP64, or the FP32
+// form's FP32 copy; to_f gives the FP32 value of an element, rounded to
+// nearest).  Writes PER_VAR floats.
+template <bool NB4, class T, class ToF>
+__device__ __forceinline__ void features(const TenoArgs& a, const T* __restrict__ U, int cell, int v, unsigned smask,
+                                         ToF to_f, float* x) {
     const int tile = cell >> 3, lane = cell & 7;
     const float uc = to_f(__ldg(U + (size_t)cell * 4 + v));
     stencil_diffs<NB4>(a, U, tile, lane, 0, v, uc, to_f, x);

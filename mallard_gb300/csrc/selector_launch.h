@@ -48,7 +48,7 @@ cudaError_t launch_mlp_rows(const uint8_t* wimg, int n, const float* X, float* l
 // neighbour's same variable is confident too (both [n][4] bytes)
 cudaError_t launch_trust(int n, const int4* cfaces, const int2* lr, const uint8_t* pred, uint8_t* trusted,
                          cudaStream_t s);
-cudaError_t launch_mlp_cells(const uint8_t* wimg, const TenoArgs& a, const double* U, float thr_central,
+cudaError_t launch_mlp_cells(const uint8_t* wimg, const TenoArgs& a, const float* U, float thr_central,
                              float thr_directional, uint8_t* pred, unsigned* err, cudaStream_t s);
 
 }  // namespace sel

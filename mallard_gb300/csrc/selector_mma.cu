@@ -142,14 +142,13 @@ __device__ __forceinline__ uint4 pack8(const float* x) {
     return u;
 }
 
-// FP64 -> FP32 of a state value, round to nearest, on the integer pipe
-// (the conversion instruction would make this kernel FP64-bound)
-struct ToFloatRN {
-    __device__ float operator()(double x) const { return f32_rn(x); }
+// the FP32 copy of the state is read as is
+struct AsFloat {
+    __device__ float operator()(float x) const { return x; }
 };
 
 // SRC 0: feature rows from X [n][IN]; SRC 1: features of cells 0..n-1 of a
-// FP32-form context computed from U.  Outputs (each optional): logits
+// FP32-form context computed from U (the FP32 copy of the state).  Outputs (each optional): logits
 // [n][OUT] and per (cell, variable) predictions: the predicted TENO mask,
 // bit 7 set when the class probability reaches the threshold of its kind
 // (central or directional; a probability p passes when sum_c exp(z_c - z_max)
@@ -160,7 +159,7 @@ struct ToFloatRN {
 template <int SRC>
 __global__ void __launch_bounds__(THREADS, 2) mlp_kernel(const uint8_t* __restrict__ wimg, int n,
                                                       const float* __restrict__ X, const TenoArgs a,
-                                                      const double* __restrict__ U, float lim_central,
+                                                      const float* __restrict__ U, float lim_central,
                                                       float lim_directional,
                                                       float* __restrict__ logits, uint8_t* __restrict__ pred,
                                                       unsigned* __restrict__ err) {
@@ -195,7 +194,7 @@ __global__ void __launch_bounds__(THREADS, 2) mlp_kernel(const uint8_t* __restri
 #pragma unroll
                 for (int k = 0; k < PER_VAR; ++k) x[k] = X[(size_t)cell * IN + v * PER_VAR + k];
             } else {
-                features<true>(a, U, cell, v, a.smask[cell], ToFloatRN{}, x);
+                features<true>(a, U, cell, v, a.smask[cell], AsFloat{}, x);
             }
         } else {
 #pragma unroll
@@ -341,7 +340,7 @@ cudaError_t launch_mlp_rows(const uint8_t* wimg, int n, const float* X, float* l
     return cudaGetLastError();
 }
 
-cudaError_t launch_mlp_cells(const uint8_t* wimg, const TenoArgs& a, const double* U, float thr_central,
+cudaError_t launch_mlp_cells(const uint8_t* wimg, const TenoArgs& a, const float* U, float thr_central,
                              float thr_directional, uint8_t* pred, unsigned* err, cudaStream_t s) {
     if (a.n_cells <= 0) return cudaSuccess;
     mlp_kernel<1><<<(a.n_cells + ROWS - 1) / ROWS, THREADS, SM_TOTAL, s>>>(
