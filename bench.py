@@ -30,8 +30,9 @@ Metric: Mcell-updates/s = cells x steps / seconds / 1e6 (one cell-update =
 one cell advanced one full SSPRK3 step).
 
 A second section, "wedge", times the benchmark spec's 4M-cell configuration:
-the supersonic ramp channel (Delaunay mesh, inviscid), plain FP64 against
-FP32 + learned selector, with the learned form's density error.  A third,
+the supersonic ramp channel (Delaunay mesh, viscous at Re 1e5 with no-slip
+walls), plain FP64 against FP32 + learned selector, with the learned
+form's density error.  A third,
 "batched", times configuration 4: 256 four-quadrant cases of uneven mesh
 size stepped together by the batched FP32 form.
 
@@ -79,6 +80,8 @@ def parse():
                          "error reference")
     ap.add_argument("--wedge-n", type=int, default=816,
                     help="rows of the ramp-channel lattice (3n+1 columns; 816 -> 4.0M triangles); 0 skips it")
+    ap.add_argument("--wedge-re", type=float, default=1e5,
+                    help="Reynolds number of the wedge on the ramp length (viscous flux, no-slip walls); 0 = inviscid")
     ap.add_argument("--batch-cases", type=int, default=256,
                     help="cases of the batched section (configuration 4); 0 skips it")
     ap.add_argument("--cpu-sample-n", type=int, default=CPU_SAMPLE_N)
@@ -328,9 +331,10 @@ def time_form(m, args, form, U0, W0, device, selector, barrier=None, clocks=None
 def run_wedge(args, device, selector):
     """The supersonic ramp channel (15 degree ramp at x = 0.5 in a 3 x 1
     channel, jittered-lattice Delaunay mesh of 2 nx ny triangles, Mach 2.5
-    upt inflow, p_out outflow, slip walls, TENO + Rusanov, CFL 0.4): plain
-    FP64 against FP32 + learned selector, same steps, density error of the
-    learned form against the plain one."""
+    upt inflow, p_out outflow, TENO + Rusanov, CFL 0.4; viscous with no-slip
+    walls at Re = --wedge-re, else slip walls): plain FP64 against FP32 +
+    learned selector, same steps, density error of the learned form against
+    the plain one."""
     import numpy as np
     import torch
 
@@ -340,13 +344,16 @@ def run_wedge(args, device, selector):
     nx = 3 * ny + 1
     t0 = time.perf_counter()
     mesh = mg.Mesh.ramp_channel(nx, ny, 3.0, 1.0, 0.5, 15.0, 0.2, seed=SEED)
+    re = args.wedge_re if args.wedge_re > 0 else None
+    flow = (f"viscous Re {re:g} on the ramp length, Pr 0.72, Sutherland, no-slip adiabatic walls" if re
+            else "inviscid (slip walls)")
     out = {"workload": f"ramp channel {nx}x{ny} lattice -> {mesh.n_cells} Delaunay triangles, 15 deg ramp, "
-                       f"Mach 2.5, TENO p3 + Rusanov, SSPRK3 CFL {WEDGE_CFL}, inviscid (slip walls)",
+                       f"Mach 2.5, TENO p3 + Rusanov, SSPRK3 CFL {WEDGE_CFL}, {flow}",
            "cells": mesh.n_cells, "mesh_s": time.perf_counter() - t0}
     finals = {}
     for form, prec in (("fp64", "fp64"), ("fp32_learned", "fp32")):
         t1 = time.perf_counter()
-        s, U0, W0 = wedge_setup(mesh, precision=prec)
+        s, U0, W0 = wedge_setup(mesh, precision=prec, reynolds=re)
         if form == "fp32_learned":
             s.attach_selector(selector[0], threshold=SEL_THRESHOLD)
         setup = time.perf_counter() - t1

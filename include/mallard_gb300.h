@@ -67,7 +67,7 @@ enum { MGPU_MESH_CARTESIAN = 0, MGPU_MESH_CARTESIAN_TRI = 1, MGPU_MESH_WEDGE = 2
 enum { MGPU_RECON_FO = 0, MGPU_RECON_TENO = 1 };
 enum { MGPU_BASIS_MONOMIAL = 0, MGPU_BASIS_LEGENDRE = 1 };
 enum { MGPU_RIEMANN_RUSANOV = 0, MGPU_RIEMANN_HLL = 1, MGPU_RIEMANN_HLLC = 2 };
-enum { MGPU_INTEGRATOR_SSPRK3 = 0 };
+enum { MGPU_INTEGRATOR_SSPRK3 = 0, MGPU_INTEGRATOR_FE = 1, MGPU_INTEGRATOR_RK4 = 2 };
 enum {
     MGPU_BC_SYMMETRY = 0,
     MGPU_BC_EXTRAPOLATION = 1,
@@ -172,7 +172,7 @@ typedef struct mgpu_config {
     int quadrature_order_cell;      /* 0 = reference default p+1             */
     int quadrature_order_face;      /* 0 = reference default (p+1)/2         */
     int riemann_solver;             /* MGPU_RIEMANN_*                        */
-    int time_integrator;            /* MGPU_INTEGRATOR_SSPRK3                */
+    int time_integrator;            /* MGPU_INTEGRATOR_*                     */
     double gamma, p_ref, T_ref, rho_ref, p_min, p_max; /* physics (physics.cpp:27-53) */
     int teno_variant;               /* MGPU_TENO_*                           */
     int precision;                  /* MGPU_PREC_*                           */

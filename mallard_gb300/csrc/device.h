@@ -205,7 +205,7 @@ cudaError_t launch_to_f32(size_t n, const double* src, float* dst, cudaStream_t 
 
 // kernels.cu
 cudaError_t launch_first_order(int n_faces, const int2* lr, const double* U, double* fv, cudaStream_t s);
-cudaError_t launch_update(const UpdateArgs& a, const GasParams& g, int stage, bool fast, cudaStream_t s);
+cudaError_t launch_update(const UpdateArgs& a, const GasParams& g, int stage, int scheme, bool fast, cudaStream_t s);
 cudaError_t launch_spectral(const SpecArgs& a, bool fast, cudaStream_t s);
 cudaError_t launch_sound(int n, double gamma, const double* U, const double* prim, double* snd, cudaStream_t s);
 // viscous: gradients of the stage input U, then the face flux into G

@@ -96,6 +96,7 @@ int mgpu_batch_create(uint32_t n_groups, const mgpu_mesh* const* meshes, const u
         if (cfg->precision != MGPU_PREC_FP32 || cfg->recon != MGPU_RECON_TENO || cfg->poly_order != 3 ||
             cfg->teno_variant != MGPU_TENO_CORRECTED)
             throw Unsupported("the batched form runs the FP32 form of corrected TENO at p = 3");
+        if (cfg->time_integrator != MGPU_INTEGRATOR_SSPRK3) throw Unsupported("the batched form integrates with SSPRK3");
         std::unique_ptr<mgpu_batch> b(new mgpu_batch());
         b->cfg = *cfg;
         for (uint32_t g = 0; g < n_groups; ++g) {

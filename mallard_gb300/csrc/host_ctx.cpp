@@ -495,7 +495,9 @@ int mgpu_create(const mgpu_mesh* mesh, const mgpu_config* cfg, mgpu_ctx** out) {
         if (!mesh || !cfg || !out) throw ArgFail("mgpu_create: null argument");
         if (cfg->recon != MGPU_RECON_FO && cfg->recon != MGPU_RECON_TENO) throw ArgFail("Unknown face reconstruction type.");
         if (cfg->riemann_solver < 0 || cfg->riemann_solver > 2) throw ArgFail("Unknown Riemann solver type.");
-        if (cfg->time_integrator != MGPU_INTEGRATOR_SSPRK3) throw Unsupported("the GPU path implements SSPRK3");
+        if (cfg->time_integrator != MGPU_INTEGRATOR_SSPRK3 && cfg->time_integrator != MGPU_INTEGRATOR_FE &&
+            cfg->time_integrator != MGPU_INTEGRATOR_RK4)
+            throw ArgFail("Unknown time integrator type.");
         if (cfg->precision != MGPU_PREC_FP64 && cfg->precision != MGPU_PREC_FP64_FAST &&
             cfg->precision != MGPU_PREC_FP32)
             throw Unsupported("unknown precision mode");
@@ -710,7 +712,7 @@ int mgpu_calc_rhs(mgpu_ctx* ctx, const double* Uh, double* rhsh) {
         ctx->flux(ctx->Ut.p);
         ctx->viscous(ctx->Ut.p);
         UpdateArgs a = ctx->update_args();
-        ck(launch_update(a, ctx->gas, 0, ctx->rcp(), ctx->stream), "update");
+        ck(launch_update(a, ctx->gas, 0, MGPU_INTEGRATOR_SSPRK3, ctx->rcp(), ctx->stream), "update");
         ctx->download_cells(ctx->rhs.p, rhsh, 4);
         return MGPU_OK;
     });
@@ -741,9 +743,7 @@ int mgpu_take_step(mgpu_ctx* ctx, double dt) {
     if (int rc = need_ready(ctx)) return rc;
     return guarded([&] {
         ck(launch_set_scalar(ctx->dt_ptr(), dt, ctx->stream), "set dt");
-        ctx->stage(1);
-        ctx->stage(2);
-        ctx->stage(3);
+        for (int k = 1; k <= ctx->n_stages(); ++k) ctx->stage(k);
         return MGPU_OK;
     });
 }

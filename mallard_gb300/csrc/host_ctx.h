@@ -241,6 +241,11 @@ struct mgpu_ctx {
         return a;
     }
 
+    // stages of one step: FE 1, SSPRK3 3, RK4 4
+    int n_stages() const {
+        return cfg.time_integrator == MGPU_INTEGRATOR_FE ? 1 : (cfg.time_integrator == MGPU_INTEGRATOR_RK4 ? 4 : 3);
+    }
+
     void stage(int k) {
         const double* in = (k == 1) ? U.p : Ut.p;
         // the selector predicts once per step, from the step's initial state,
@@ -249,8 +254,8 @@ struct mgpu_ctx {
         flux(in);
         viscous(in);
         UpdateArgs a = update_args();
-        if (single()) a.u32 = k == 3 ? U32.p : Ut32.p;
-        timed(2, [&] { return launch_update(a, gas, k, rcp(), stream); });
+        if (single()) a.u32 = k == n_stages() ? U32.p : Ut32.p;
+        timed(2, [&] { return launch_update(a, gas, k, cfg.time_integrator, rcp(), stream); });
     }
 
     void spectral_and_dt(double cfl, bool accumulate_t) {
@@ -274,9 +279,7 @@ struct mgpu_ctx {
 
     void cfl_step(double cfl) {
         spectral_and_dt(cfl, true);
-        stage(1);
-        stage(2);
-        stage(3);
+        for (int k = 1; k <= n_stages(); ++k) stage(k);
     }
 
     // ---- host <-> device in caller numbering ------------------------------

@@ -86,7 +86,9 @@ __device__ __forceinline__ void store_f32(float* dst, const double* x) {
     *reinterpret_cast<float4*>(dst) = make_float4(f32_rn(x[0]), f32_rn(x[1]), f32_rn(x[2]), f32_rn(x[3]));
 }
 
-template <int STAGE, bool FAST, class IX>
+// SCHEME: MGPU_INTEGRATOR_*; STAGE 1.. its stages (the last one writes U,
+// the primitives and the NaN flag), 0 the residual alone.
+template <int STAGE, bool FAST, int SCHEME, class IX>
 __device__ __forceinline__ void update_cell(const UpdateArgs& a, const StageState& st, const GasParams& g, int c,
                                             const IX& ix, const double* dtp, unsigned* flag) {
     const size_t row = ix.u(c);
@@ -128,7 +130,41 @@ __device__ __forceinline__ void update_cell(const UpdateArgs& a, const StageStat
     const double2* W2 = reinterpret_cast<const double2*>(st.W + row * 4);
     double2* Ut2 = reinterpret_cast<double2*>(st.Ut + row * 4);
     double2* Wo2 = reinterpret_cast<double2*>(st.W + row * 4);
-    if (STAGE == 1) {
+    double u[4];  // the new state, on the scheme's last stage
+    if (SCHEME == MGPU_INTEGRATOR_FE) {
+        // FE::take_step (time_integrator.cpp:57-69): U += dt rhs
+        const double2 u0 = U2[0], u1 = U2[1];
+        const double v[4] = {u0.x, u0.y, u1.x, u1.y};
+#pragma unroll
+        for (int i = 0; i < 4; i++) u[i] = v[i] + dt * r[i];
+    } else if (SCHEME == MGPU_INTEGRATOR_RK4) {
+        // RK4::take_step (time_integrator.cpp:85-120), coefficients (:71-79):
+        // U_temp = U + (dt/2) k1,
+        // U + (dt/2) k2, U + dt k3; U += dt/6 k1 + dt/3 k2 + dt/3 k3 + dt/6 k4,
+        // accumulated in W in that order
+        const double cs = STAGE == 1 ? dt * (1.0 / 6.0) : (STAGE == 4 ? dt * (1.0 / 6.0) : dt * (1.0 / 3.0));
+        const double2 w0 = W2[0], w1 = W2[1];
+        if (STAGE < 4) {
+            const double2 u0 = U2[0], u1 = U2[1];
+            const double v[4] = {u0.x, u0.y, u1.x, u1.y};
+            const double h = STAGE == 3 ? dt : dt / 2.0;
+            double t[4], w[4] = {w0.x, w0.y, w1.x, w1.y};
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                t[i] = v[i] + h * r[i];
+                w[i] = (STAGE == 1 ? v[i] : w[i]) + cs * r[i];
+            }
+            Ut2[0] = make_double2(t[0], t[1]);
+            Ut2[1] = make_double2(t[2], t[3]);
+            Wo2[0] = make_double2(w[0], w[1]);
+            Wo2[1] = make_double2(w[2], w[3]);
+            if (st.u32) store_f32(st.u32 + row * 4, t);
+            return;
+        }
+        const double w[4] = {w0.x, w0.y, w1.x, w1.y};
+#pragma unroll
+        for (int i = 0; i < 4; i++) u[i] = w[i] + cs * r[i];
+    } else if (STAGE == 1) {
         const double2 u0 = U2[0], u1 = U2[1];
         const double u[4] = {u0.x, u0.y, u1.x, u1.y};
         const double c1 = dt * (1.0 / 6.0);
@@ -143,6 +179,7 @@ __device__ __forceinline__ void update_cell(const UpdateArgs& a, const StageStat
         Wo2[0] = make_double2(w[0], w[1]);
         Wo2[1] = make_double2(w[2], w[3]);
         if (st.u32) store_f32(st.u32 + row * 4, t);
+        return;
     } else if (STAGE == 2) {
         const double2 u0 = U2[0], u1 = U2[1], s0 = Ut2[0], s1 = Ut2[1], w0 = W2[0], w1 = W2[1];
         const double u[4] = {u0.x, u0.y, u1.x, u1.y};
@@ -161,13 +198,15 @@ __device__ __forceinline__ void update_cell(const UpdateArgs& a, const StageStat
         Wo2[0] = make_double2(w[0], w[1]);
         Wo2[1] = make_double2(w[2], w[3]);
         if (st.u32) store_f32(st.u32 + row * 4, t);
+        return;
     } else {
         const double2 w0 = W2[0], w1 = W2[1];
         const double w[4] = {w0.x, w0.y, w1.x, w1.y};
         const double c3 = dt * (2.0 / 3.0);
-        double u[4];
 #pragma unroll
         for (int i = 0; i < 4; i++) u[i] = w[i] + c3 * r[i];
+    }
+    {
         double2* Uo2 = reinterpret_cast<double2*>(st.U + row * 4);
         Uo2[0] = make_double2(u[0], u[1]);
         Uo2[1] = make_double2(u[2], u[3]);
@@ -186,12 +225,12 @@ __device__ __forceinline__ void update_cell(const UpdateArgs& a, const StageStat
     }
 }
 
-template <int STAGE, bool FAST>
+template <int STAGE, bool FAST, int SCHEME>
 __global__ void __launch_bounds__(256) update_kernel(const UpdateArgs a, const GasParams g) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= a.n_cells) return;
     const StageState st{a.G, a.U, a.Ut, a.W, a.prim, a.snd, a.rhs, a.u32};
-    update_cell<STAGE, FAST>(a, st, g, c, Ix1{}, a.dt, a.flags);
+    update_cell<STAGE, FAST, SCHEME>(a, st, g, c, Ix1{}, a.dt, a.flags);
 }
 
 // ---------------------------------------------------------------------------
@@ -432,7 +471,7 @@ __global__ void __launch_bounds__(256) update_batch_kernel(const BatchLaunch b, 
         const unsigned gc = b.case0[gi] + cs;
         if (c >= b.n_cells[gi] || b.flags[gc] != 0u) continue;
         const StageState st{b.G, b.U, b.Ut, b.W, b.prim, b.snd, nullptr, STAGE == 3 ? b.U32 : b.Ut32};
-        update_cell<STAGE, true>(b.upd[gi], st, g, c, IxB{b.ubase[gi], b.fbase[gi], C, cs}, b.dt + gc, b.flags + gc);
+        update_cell<STAGE, true, MGPU_INTEGRATOR_SSPRK3>(b.upd[gi], st, g, c, IxB{b.ubase[gi], b.fbase[gi], C, cs}, b.dt + gc, b.flags + gc);
     }
 }
 
@@ -580,21 +619,32 @@ cudaError_t launch_first_order(int n_faces, const int2* lr, const double* U, dou
 }
 
 template <bool FAST>
-cudaError_t update_go(const UpdateArgs& a, const GasParams& g, int stage, unsigned blocks, cudaStream_t s) {
-    switch (stage) {
-        case 0: update_kernel<0, FAST><<<blocks, 256, 0, s>>>(a, g); break;
-        case 1: update_kernel<1, FAST><<<blocks, 256, 0, s>>>(a, g); break;
-        case 2: update_kernel<2, FAST><<<blocks, 256, 0, s>>>(a, g); break;
-        case 3: update_kernel<3, FAST><<<blocks, 256, 0, s>>>(a, g); break;
-        default: return cudaErrorInvalidValue;
+cudaError_t update_go(const UpdateArgs& a, const GasParams& g, int stage, int scheme, unsigned blocks,
+                      cudaStream_t s) {
+    constexpr int SS = MGPU_INTEGRATOR_SSPRK3, FE = MGPU_INTEGRATOR_FE, RK = MGPU_INTEGRATOR_RK4;
+    if (stage == 0) {
+        update_kernel<0, FAST, SS><<<blocks, 256, 0, s>>>(a, g);
+    } else if (scheme == SS && stage <= 3) {
+        if (stage == 1) update_kernel<1, FAST, SS><<<blocks, 256, 0, s>>>(a, g);
+        else if (stage == 2) update_kernel<2, FAST, SS><<<blocks, 256, 0, s>>>(a, g);
+        else update_kernel<3, FAST, SS><<<blocks, 256, 0, s>>>(a, g);
+    } else if (scheme == FE && stage == 1) {
+        update_kernel<1, FAST, FE><<<blocks, 256, 0, s>>>(a, g);
+    } else if (scheme == RK && stage <= 4) {
+        if (stage == 1) update_kernel<1, FAST, RK><<<blocks, 256, 0, s>>>(a, g);
+        else if (stage == 2) update_kernel<2, FAST, RK><<<blocks, 256, 0, s>>>(a, g);
+        else if (stage == 3) update_kernel<3, FAST, RK><<<blocks, 256, 0, s>>>(a, g);
+        else update_kernel<4, FAST, RK><<<blocks, 256, 0, s>>>(a, g);
+    } else {
+        return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
 }
 
-cudaError_t launch_update(const UpdateArgs& a, const GasParams& g, int stage, bool fast, cudaStream_t s) {
+cudaError_t launch_update(const UpdateArgs& a, const GasParams& g, int stage, int scheme, bool fast, cudaStream_t s) {
     const unsigned blocks = (unsigned)((a.n_cells + 255) / 256);
     if (blocks == 0) return cudaSuccess;
-    return fast ? update_go<true>(a, g, stage, blocks, s) : update_go<false>(a, g, stage, blocks, s);
+    return fast ? update_go<true>(a, g, stage, scheme, blocks, s) : update_go<false>(a, g, stage, scheme, blocks, s);
 }
 
 cudaError_t launch_spectral(const SpecArgs& a, bool fast, cudaStream_t s) {

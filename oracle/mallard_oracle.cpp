@@ -967,8 +967,9 @@ struct Case {
     //    then replaces a reconstructed face state whose density or pressure
     //    is not positive by the owning cell's average (first-order fallback).
     int teno_variant = 0;
+    int integrator = 0;  // 0 SSPRK3, 1 FE, 2 RK4 (time_integrator.h)
     std::vector<Bc> bcs;
-    std::vector<double> U, Utmp, prim, face, r1, r2, r3, cfl_local;
+    std::vector<double> U, Utmp, prim, face, r1, r2, r3, r4, cfl_local;
     // viscous face flux (no reference counterpart; restated from the GPU
     // library's definition): Sutherland viscosity, Green-Gauss gradients
     bool viscous = false;
@@ -1410,8 +1411,38 @@ void axpby(double a, const std::vector<double>& x, double b, std::vector<double>
     for (int64_t i = 0; i < n; i++) y[i] = a * x[i] + b * y[i];
 }
 
+// FE::take_step (time_integrator.cpp:57-69)
+void take_step_fe(Case& cs, double dt) {
+    calc_rhs(cs, cs.U.data(), cs.face.data(), cs.r1.data());
+    axpy(dt, cs.r1, cs.U);
+    update_prims(cs);
+}
+
+// RK4::take_step (time_integrator.cpp:85-120), coefficients 1/6, 1/3, 1/3, 1/6 (:71-79)
+void take_step_rk4(Case& cs, double dt) {
+    const double c[4] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
+    if (cs.r4.size() != cs.r1.size()) cs.r4.assign(cs.r1.size(), 0.0);
+    calc_rhs(cs, cs.U.data(), cs.face.data(), cs.r1.data());
+    cs.Utmp = cs.U;
+    axpy(dt / 2.0, cs.r1, cs.Utmp);
+    calc_rhs(cs, cs.Utmp.data(), cs.face.data(), cs.r2.data());
+    cs.Utmp = cs.U;
+    axpy(dt / 2.0, cs.r2, cs.Utmp);
+    calc_rhs(cs, cs.Utmp.data(), cs.face.data(), cs.r3.data());
+    cs.Utmp = cs.U;
+    axpy(dt, cs.r3, cs.Utmp);
+    calc_rhs(cs, cs.Utmp.data(), cs.face.data(), cs.r4.data());
+    axpy(dt * c[0], cs.r1, cs.U);
+    axpy(dt * c[1], cs.r2, cs.U);
+    axpy(dt * c[2], cs.r3, cs.U);
+    axpy(dt * c[3], cs.r4, cs.U);
+    update_prims(cs);
+}
+
 // SSPRK3::take_step (time_integrator.cpp:135-163) + Solver::take_step (solver.cpp:521-531)
 void take_step(Case& cs, double dt) {
+    if (cs.integrator == 1) return take_step_fe(cs, dt);
+    if (cs.integrator == 2) return take_step_rk4(cs, dt);
     calc_rhs(cs, cs.U.data(), cs.face.data(), cs.r1.data());
     cs.Utmp = cs.U;
     axpy(dt, cs.r1, cs.Utmp);
@@ -1781,6 +1812,21 @@ void orc_triangle_jac(const double* a, const double* b, const double* c, double*
     inv2(J, Jinv);
 }
 double orc_triangle_area(const double* a, const double* b, const double* c) { return tri_area(a, b, c); }
+
+// FE and RK4 with a U-independent right-hand side (the same stub).
+void orc_fe_const_rhs(double* U, const double* rhs, uint32_t n, double dt) {
+    std::vector<double> u(U, U + (size_t)n * NC), r(rhs, rhs + (size_t)n * NC);
+    axpy(dt, r, u);
+    std::memcpy(U, u.data(), u.size() * sizeof(double));
+}
+void orc_rk4_const_rhs(double* U, const double* rhs, uint32_t n, double dt) {
+    const double c[4] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
+    std::vector<double> u(U, U + (size_t)n * NC), r(rhs, rhs + (size_t)n * NC);
+    for (int k = 0; k < 4; ++k) axpy(dt * c[k], r, u);
+    std::memcpy(U, u.data(), u.size() * sizeof(double));
+}
+
+void orc_case_set_integrator(void* h, int integrator) { static_cast<Case*>(h)->integrator = integrator; }
 
 // SSPRK3 with a caller-supplied right-hand side that does not depend on U
 // (time_integrator_test.cpp:22-28 stub): rhs is [n][4], applied to U [n][4].

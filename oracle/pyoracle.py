@@ -80,6 +80,9 @@ def load():
         "orc_case_nq": (i32, [vp]),
         "orc_case_set_teno_variant": (None, [vp, i32]),
         "orc_case_set_viscous": (None, [vp, i32, f64, f64, f64, f64]),
+        "orc_case_set_integrator": (None, [vp, i32]),
+        "orc_fe_const_rhs": (None, [vp, vp, u32, f64]),
+        "orc_rk4_const_rhs": (None, [vp, vp, u32, f64]),
         "orc_case_face_values": (i32, [vp, vp, vp, vp]),
         "orc_case_calc_rhs": (i32, [vp, vp, vp]),
         "orc_case_calc_dt": (i32, [vp, f64, C.POINTER(f64), vp]),
@@ -180,6 +183,10 @@ class OracleCase:
     def set_teno_variant(self, variant):
         """0: the reference's weighting; 1: cut-off weighting (see the C source)."""
         self._lib.orc_case_set_teno_variant(self.h, int(variant))
+
+    def set_integrator(self, name):
+        """SSPRK3 (default), FE or RK4 (time_integrator.cpp)."""
+        self._lib.orc_case_set_integrator(self.h, {"SSPRK3": 0, "FE": 1, "RK4": 2}[name])
 
     def set_viscous(self, mu_ref, T_mu_ref=1.0, sutherland_S=0.0, prandtl=0.72, viscous=True):
         """The viscous face flux (no reference counterpart; see the C source)."""
@@ -304,9 +311,19 @@ class Oracle:
         return self.lib.orc_triangle_area(_p(a), _p(b), _p(c))
 
     def ssprk3_const_rhs(self, U, rhs, dt):
+        return self._const_rhs(self.lib.orc_ssprk3_const_rhs, U, rhs, dt)
+
+    def fe_const_rhs(self, U, rhs, dt):
+        return self._const_rhs(self.lib.orc_fe_const_rhs, U, rhs, dt)
+
+    def rk4_const_rhs(self, U, rhs, dt):
+        return self._const_rhs(self.lib.orc_rk4_const_rhs, U, rhs, dt)
+
+    @staticmethod
+    def _const_rhs(fn, U, rhs, dt):
         U = np.ascontiguousarray(U, dtype=np.float64).copy()
         R = np.ascontiguousarray(rhs, dtype=np.float64)
-        self.lib.orc_ssprk3_const_rhs(_p(U), _p(R), len(U) // 4 if U.ndim == 1 else len(U), dt)
+        fn(_p(U), _p(R), len(U) // 4 if U.ndim == 1 else len(U), dt)
         return U
 
 

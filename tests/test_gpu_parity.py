@@ -159,6 +159,61 @@ def test_take_step_matches(variant):
     assert_close(Wg, Wo, STAGE_TOL, min_exact=0.95, what="primitives")
 
 
+@pytest.mark.parametrize("integrator", ["FE", "RK4"])
+def test_take_step_other_integrators(integrator):
+    """FE and RK4 (time_integrator.cpp:57-120): one step per stage count at
+    the per-stage bar, then 30 CFL steps of the corrected-weighting pulse at
+    the run bar."""
+    m = tri_mesh(20, seed=6)
+    s, oc = make_pair(m, variant="reference", integrator=integrator)
+    U, W = smooth(m)
+    s.set_state(U, W)
+    oc.set_state(U, W)
+    s.take_step(1e-3)
+    oc.take_step(1e-3)
+    Ug, Wg = s.get_state()
+    Uo, Wo = oc.get_state()
+    assert_close(Ug, Uo, STAGE_TOL, min_exact=0.95, what=f"{integrator} U")
+    assert_close(Wg, Wo, STAGE_TOL, min_exact=0.95, what=f"{integrator} primitives")
+    s.close()
+    m = tri_mesh(16, seed=20261203)
+    bcs = {z: "symmetry" for z in ("left", "right", "top", "bottom")}
+    s, oc = make_pair(m, variant="corrected", bcs=bcs, integrator=integrator)
+    U, W = pulse(m)
+    s.set_state(U, W)
+    oc.set_state(U, W)
+    cfl = 0.2 if integrator == "FE" else 0.5
+    t_gpu = s.run(cfl, 30)
+    t_ora = oc.run(cfl, 30)
+    assert abs(t_gpu - t_ora) <= 1e-12 * t_ora
+    Ug, _ = s.get_state()
+    Uo, _ = oc.get_state()
+    assert np.isfinite(Uo).all()
+    assert_close(Ug, Uo, RUN_TOL, what=f"{integrator} U after 30 steps")
+    assert s.status() == 0
+    s.close()
+
+
+@pytest.mark.parametrize("integrator", ["FE", "RK4"])
+@pytest.mark.parametrize("precision", ["fp64_fast", "fp32"])
+def test_other_integrators_fast_forms(integrator, precision):
+    """FE and RK4 in the FMA and FP32 forms against the FP64 form after 20
+    steps of the explosion (corrected TENO)."""
+    from cases import explosion
+    m = tri_mesh(48, seed=2)
+    out = {}
+    for prec in ("fp64", precision):
+        s, _ = make_pair(m, variant="corrected", integrator=integrator, precision=prec)
+        U, W = explosion(m)
+        s.set_state(U, W)
+        s.run(0.2 if integrator == "FE" else 0.5, 20)
+        assert s.status() == 0
+        out[prec] = s.get_state()[0]
+        s.close()
+    err = rel_err(out[precision], out["fp64"])
+    assert err.max() < (1e-9 if precision == "fp64_fast" else 1e-3), err.max()
+
+
 def test_100_steps_teno_pulse():
     """100 CFL steps of TENO (corrected weighting) on an acoustic pulse in a
     closed box.  The reference's own weighting diverges within the first step

@@ -89,6 +89,18 @@ def test_physics_primitives(golden):
         np.testing.assert_allclose(row, [u[0], u[1], p, T, h], atol=tol, rtol=0)
 
 
+@pytest.mark.parametrize("name", ["FE", "RK4"])
+def test_fe_rk4_consistency(golden, name):
+    """time_integrator_test.cpp FE / RK4: a U-independent RHS advances U0 to 1.1 U0."""
+    t = _tests(golden, "test/time_integrator_test.cpp")[name]
+    assert t is not None
+    n = golden["time_integrator_n_cells"]
+    icpi = np.arange(n * 4, dtype=np.float64).reshape(n, 4)
+    o = Oracle()
+    U = (o.fe_const_rhs if name == "FE" else o.rk4_const_rhs)(icpi, icpi, 0.1)
+    np.testing.assert_allclose(U, 1.1 * icpi, atol=golden["file_tolerances"]["test/time_integrator_test.cpp"])
+
+
 def test_ssprk3_consistency(golden):
     """time_integrator_test.cpp SSPRK3: a U-independent RHS advances U0 to 1.1 U0."""
     t = _tests(golden, "test/time_integrator_test.cpp")["SSPRK3"]
