@@ -107,6 +107,23 @@ struct ViscArgs {
     double mu_ref, T_ref, S, cp_over_pr;
 };
 
+// FP32 form of the viscous flux: (u, v, T) and their Green-Gauss gradients
+// per cell from the FP32 stage state, then the face flux inside the FP32
+// face-flux kernel.  Face geometry rounded to FP32 once, on upload.
+struct Visc32Args {
+    int n_cells;
+    const int4* cfaces;     // faces of each cell, -1 = none
+    const int2* lr;
+    const int8_t* bc;       // -1 interior, else BcTable index
+    const float4* fgeo;     // per flux face: unit normal (x, y), centre-line direction (x, y)
+    const float2* fgeo2;    // per flux face: area, 1 / centre-line length
+    const double* ivol;     // 1 / volume
+    float4* q;              // per cell: u, v, T, 0
+    float4* ga;             // per cell: du/dx, du/dy, dv/dx, dv/dy
+    float2* gb;             // per cell: dT/dx, dT/dy
+    float mu_ref, T_ref, S, cp_over_pr, inv_cv;
+};
+
 struct SpecArgs {
     int n_cells;
     const int4* cfaces;     // faces of the cell in the reference's order, -1 = none
@@ -149,8 +166,11 @@ cudaError_t launch_teno(const TenoArgs& a, int K, int M, int nq, const float* U,
 // with the learned selector's predictions (p = 3 only)
 cudaError_t launch_teno_selected(const TenoArgs& a, int K, int M, int nq, const float* U, const uint8_t* pred,
                                  float* fv, uint8_t* masks, int shape, cudaStream_t s);
+// visc: the viscous flux's arguments (after launch_visc_grad), or null
 cudaError_t launch_flux(const FluxArgs& a, const float* fv, const GasParams& g, const BcTable& bct, int rsolver,
-                        int nq, cudaStream_t s);
+                        int nq, const Visc32Args* visc, cudaStream_t s);
+// per-cell (u, v, T) and gradients of the FP32 stage state U
+cudaError_t launch_visc_grad(const Visc32Args& v, const BcTable& bct, const float* U, cudaStream_t s);
 }  // namespace f32
 // ---------------------------------------------------------------------------
 // Batched form: many cases on a few meshes in one launch per kernel.

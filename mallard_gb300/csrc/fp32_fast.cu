@@ -222,11 +222,117 @@ __device__ __forceinline__ void primitives_guarded(const GasParams& g, const flo
     }
 }
 
-// Flux of one face (local index fi) into G.
-template <int RS, int NQ, class IX>
+// ---------------------------------------------------------------------------
+// Viscous flux, FP32 form (the FP64 kernels in kernels.cu define it; the
+// same operations in FP32 here)
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ float4 uvT32(const float4 x, float inv_cv) {
+    const float ir = __frcp_rn(x.x);
+    const float u = x.y * ir, v = x.z * ir;
+    const float e = x.w * ir - 0.5f * (u * u + v * v);
+    return make_float4(u, v, e * inv_cv, 0.0f);
+}
+
+__global__ void __launch_bounds__(256) visc_grad32_kernel(const Visc32Args a, const BcTable bct,
+                                                          const float* __restrict__ U) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= a.n_cells) return;
+    const float4* U4 = reinterpret_cast<const float4*>(U);
+    const float4 qc = uvT32(U4[c], a.inv_cv);
+    float gx[3] = {0.0f, 0.0f, 0.0f}, gy[3] = {0.0f, 0.0f, 0.0f};
+    const int4 cf = a.cfaces[c];
+    const int ent[4] = {cf.x, cf.y, cf.z, cf.w};
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        if (ent[e] < 0) break;
+        const int fi = ent[e];
+        const int2 lr = a.lr[fi];
+        const float4 gg = a.fgeo[fi];
+        const float A = a.fgeo2[fi].x;
+        const float sA = lr.x == c ? A : -A;
+        float qf[3];
+        if (lr.y >= 0) {
+            const float4 qo = uvT32(U4[lr.x == c ? lr.y : lr.x], a.inv_cv);
+            qf[0] = 0.5f * (qc.x + qo.x);
+            qf[1] = 0.5f * (qc.y + qo.y);
+            qf[2] = 0.5f * (qc.z + qo.z);
+        } else {
+            const int bi = a.bc[fi];
+            const bool wall = bi >= 0 && bct.bc[bi].type == MGPU_BC_WALL_ADIABATIC;
+            qf[0] = wall ? 0.0f : qc.x;
+            qf[1] = wall ? 0.0f : qc.y;
+            qf[2] = qc.z;
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            gx[k] = fmaf(qf[k], gg.x * sA, gx[k]);
+            gy[k] = fmaf(qf[k], gg.y * sA, gy[k]);
+        }
+    }
+    const float iv = f(a.ivol[c]);
+    a.q[c] = qc;
+    a.ga[c] = make_float4(gx[0] * iv, gy[0] * iv, gx[1] * iv, gy[1] * iv);
+    a.gb[c] = make_float2(gx[2] * iv, gy[2] * iv);
+}
+
+// Viscous flux of flux face fi (interior or no-slip adiabatic wall; zero on
+// other boundaries): mean gradient corrected along the centre line, Stokes
+// stresses, Sutherland or constant viscosity, Fourier heat flux.
+__device__ __forceinline__ void visc32_face(const Visc32Args& a, int fi, int2 lr, bool wall, const float n[2],
+                                            float Fv[4]) {
+    const float4 qL = a.q[lr.x];
+    float4 qR;
+    float gf[6];
+    {
+        const float4 l0 = a.ga[lr.x];
+        const float2 l1 = a.gb[lr.x];
+        if (lr.y >= 0) {
+            qR = a.q[lr.y];
+            const float4 r0 = a.ga[lr.y];
+            const float2 r1 = a.gb[lr.y];
+            gf[0] = 0.5f * (l0.x + r0.x);
+            gf[1] = 0.5f * (l0.y + r0.y);
+            gf[2] = 0.5f * (l0.z + r0.z);
+            gf[3] = 0.5f * (l0.w + r0.w);
+            gf[4] = 0.5f * (l1.x + r1.x);
+            gf[5] = 0.5f * (l1.y + r1.y);
+        } else {
+            qR = make_float4(0.0f, 0.0f, qL.z, 0.0f);
+            gf[0] = l0.x; gf[1] = l0.y; gf[2] = l0.z; gf[3] = l0.w; gf[4] = l1.x; gf[5] = l1.y;
+        }
+    }
+    const float4 gg = a.fgeo[fi];
+    const float idl = a.fgeo2[fi].y;
+    const float dq[3] = {qR.x - qL.x, qR.y - qL.y, qR.z - qL.z};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float corr = dq[k] * idl - (gf[2 * k] * gg.z + gf[2 * k + 1] * gg.w);
+        gf[2 * k] = fmaf(corr, gg.z, gf[2 * k]);
+        gf[2 * k + 1] = fmaf(corr, gg.w, gf[2 * k + 1]);
+    }
+    const float u = 0.5f * (qL.x + qR.x), v = 0.5f * (qL.y + qR.y), T = 0.5f * (qL.z + qR.z);
+    float mu = a.mu_ref;
+    if (a.S > 0.0f) {
+        const float r = T / a.T_ref;
+        mu = a.mu_ref * (r * sqrtf(r)) * ((a.T_ref + a.S) / (T + a.S));
+    }
+    const float kc = mu * a.cp_over_pr;
+    const float div = gf[0] + gf[3];
+    const float txx = mu * (2.0f * gf[0] - (2.0f / 3.0f) * div);
+    const float tyy = mu * (2.0f * gf[3] - (2.0f / 3.0f) * div);
+    const float txy = mu * (gf[1] + gf[2]);
+    Fv[0] = 0.0f;
+    Fv[1] = txx * n[0] + txy * n[1];
+    Fv[2] = txy * n[0] + tyy * n[1];
+    Fv[3] = wall ? 0.0f : (u * txx + v * txy + kc * gf[4]) * n[0] + (u * txy + v * tyy + kc * gf[5]) * n[1];
+}
+
+// Flux of one face (local index fi) into G; VISC: minus the viscous flux.
+template <int RS, int NQ, bool VISC, class IX>
 __device__ __forceinline__ void flux32_face(const FluxArgs& a, const float* __restrict__ fv, const GasParams& g,
                                             const BcTable& bct, int fi, const IX& ix, const double* __restrict__ Ust,
-                                            double* __restrict__ Gout) {
+                                            double* __restrict__ Gout, const Visc32Args* va = nullptr) {
     const int2 lr = a.lr[fi];
     const double2 nn = a.nrm[fi];
     const float n[2] = {f(nn.x), f(nn.y)};
@@ -301,31 +407,42 @@ __device__ __forceinline__ void flux32_face(const FluxArgs& a, const float* __re
     }
     const double area = a.area[fi];
     double2* Gf = reinterpret_cast<double2*>(Gout + ix.f(fi) * 4);
+    if (VISC && (type < 0 || type == MGPU_BC_WALL_ADIABATIC)) {
+        float Fv[4];
+        visc32_face(*va, fi, lr, type == MGPU_BC_WALL_ADIABATIC, n, Fv);
+        Gf[0] = make_double2(area * (double)(F[0] * 0.5f), area * (double)(F[1] * 0.5f) - area * (double)Fv[1]);
+        Gf[1] = make_double2(area * (double)(F[2] * 0.5f) - area * (double)Fv[2],
+                             area * (double)(F[3] * 0.5f) - area * (double)Fv[3]);
+        return;
+    }
     Gf[0] = make_double2(area * (double)(F[0] * 0.5f), area * (double)(F[1] * 0.5f));
     Gf[1] = make_double2(area * (double)(F[2] * 0.5f), area * (double)(F[3] * 0.5f));
 }
 
-template <int RS, int NQ>
+template <int RS, int NQ, bool VISC>
 __global__ void __launch_bounds__(128) flux32_kernel(const FluxArgs a, const float* __restrict__ fv,
-                                                     const GasParams g, const BcTable bct) {
+                                                     const GasParams g, const BcTable bct, const Visc32Args v) {
     const int fi = blockIdx.x * blockDim.x + threadIdx.x;
     if (fi >= a.n_faces) return;
-    flux32_face<RS, NQ>(a, fv, g, bct, fi, Ix1{}, a.U, a.G);
+    flux32_face<RS, NQ, VISC>(a, fv, g, bct, fi, Ix1{}, a.U, a.G, &v);
 }
 
 template <int RS, int NQ>
-cudaError_t flux_go(const FluxArgs& a, const float* fv, const GasParams& g, const BcTable& bct, cudaStream_t s) {
+cudaError_t flux_go(const FluxArgs& a, const float* fv, const GasParams& g, const BcTable& bct,
+                    const Visc32Args* v, cudaStream_t s) {
     const unsigned blocks = (unsigned)((a.n_faces + 127) / 128);
-    if (blocks) flux32_kernel<RS, NQ><<<blocks, 128, 0, s>>>(a, fv, g, bct);
+    if (!blocks) return cudaSuccess;
+    if (v) flux32_kernel<RS, NQ, true><<<blocks, 128, 0, s>>>(a, fv, g, bct, *v);
+    else flux32_kernel<RS, NQ, false><<<blocks, 128, 0, s>>>(a, fv, g, bct, Visc32Args{});
     return cudaGetLastError();
 }
 
 template <int RS>
 cudaError_t flux_nq(const FluxArgs& a, const float* fv, const GasParams& g, const BcTable& bct, int nq,
-                    cudaStream_t s) {
+                    const Visc32Args* v, cudaStream_t s) {
     switch (nq) {
-        case 1: return flux_go<RS, 1>(a, fv, g, bct, s);
-        case 2: return flux_go<RS, 2>(a, fv, g, bct, s);
+        case 1: return flux_go<RS, 1>(a, fv, g, bct, v, s);
+        case 2: return flux_go<RS, 2>(a, fv, g, bct, v, s);
     }
     return cudaErrorInvalidValue;
 }
@@ -392,7 +509,7 @@ __global__ void __launch_bounds__(128) flux32_batch_kernel(const BatchLaunch b, 
         const unsigned tc = t >> 3, C = b.C[gi], cs = tc % C;
         const int fi = (int)(tc / C) * 8 + (int)(t & 7);
         if (fi >= b.n_faces[gi] || b.flags[b.case0[gi] + cs] != 0u) continue;
-        flux32_face<RS, NQ>(b.flux[gi], b.fv, g, bct, fi, IxB{b.ubase[gi], b.fbase[gi], C, cs}, U, b.G);
+        flux32_face<RS, NQ, false>(b.flux[gi], b.fv, g, bct, fi, IxB{b.ubase[gi], b.fbase[gi], C, cs}, U, b.G);
     }
 }
 
@@ -453,13 +570,18 @@ cudaError_t launch_teno_selected(const TenoArgs& a, int K, int M, int nq, const 
 }
 
 cudaError_t launch_flux(const FluxArgs& a, const float* fv, const GasParams& g, const BcTable& bct, int rsolver,
-                        int nq, cudaStream_t s) {
+                        int nq, const Visc32Args* visc, cudaStream_t s) {
     switch (rsolver) {
-        case MGPU_RIEMANN_RUSANOV: return flux_nq<MGPU_RIEMANN_RUSANOV>(a, fv, g, bct, nq, s);
-        case MGPU_RIEMANN_HLL: return flux_nq<MGPU_RIEMANN_HLL>(a, fv, g, bct, nq, s);
-        case MGPU_RIEMANN_HLLC: return flux_nq<MGPU_RIEMANN_HLLC>(a, fv, g, bct, nq, s);
+        case MGPU_RIEMANN_RUSANOV: return flux_nq<MGPU_RIEMANN_RUSANOV>(a, fv, g, bct, nq, visc, s);
+        case MGPU_RIEMANN_HLL: return flux_nq<MGPU_RIEMANN_HLL>(a, fv, g, bct, nq, visc, s);
+        case MGPU_RIEMANN_HLLC: return flux_nq<MGPU_RIEMANN_HLLC>(a, fv, g, bct, nq, visc, s);
     }
     return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_visc_grad(const Visc32Args& v, const BcTable& bct, const float* U, cudaStream_t s) {
+    if (v.n_cells > 0) visc_grad32_kernel<<<(v.n_cells + 255) / 256, 256, 0, s>>>(v, bct, U);
+    return cudaGetLastError();
 }
 
 }  // namespace f32

@@ -97,6 +97,7 @@ int mgpu_batch_create(uint32_t n_groups, const mgpu_mesh* const* meshes, const u
             cfg->teno_variant != MGPU_TENO_CORRECTED)
             throw Unsupported("the batched form runs the FP32 form of corrected TENO at p = 3");
         if (cfg->time_integrator != MGPU_INTEGRATOR_SSPRK3) throw Unsupported("the batched form integrates with SSPRK3");
+        if (cfg->viscous) throw Unsupported("the batched form is inviscid");
         std::unique_ptr<mgpu_batch> b(new mgpu_batch());
         b->cfg = *cfg;
         for (uint32_t g = 0; g < n_groups; ++g) {

@@ -446,6 +446,39 @@ void mgpu_ctx::build() {
         visc.S = cfg.sutherland_S;
         const double cp = gas.R * cfg.gamma / (cfg.gamma - 1.0);
         visc.cp_over_pr = cp / cfg.prandtl;
+        if (single()) {
+            // face geometry of the FP32 viscous flux, derived in FP64 and
+            // rounded once: normal, centre-line direction, area, 1 / length
+            std::vector<float4> g0(F_real);
+            std::vector<float2> g1(F_real);
+            for (uint32_t i = 0; i < F_real; ++i) {
+                const int2 e = h_lr[i];
+                const double2 a = h_xc[e.x], b = e.y >= 0 ? h_xc[e.y] : h_xf[i];
+                const double dx = b.x - a.x, dy = b.y - a.y, dl = std::sqrt(dx * dx + dy * dy);
+                g0[i] = make_float4((float)h_nrm[i].x, (float)h_nrm[i].y, (float)(dx / dl), (float)(dy / dl));
+                g1[i] = make_float2((float)h_area[i], (float)(1.0 / dl));
+            }
+            vgeo.upload(g0);
+            vgeo2.upload(g1);
+            vq.alloc(N);
+            vga.alloc(N);
+            vgb.alloc(N);
+            visc32.n_cells = (int)N;
+            visc32.cfaces = cfaces.p;
+            visc32.lr = lr.p;
+            visc32.bc = bcidx.p;
+            visc32.fgeo = vgeo.p;
+            visc32.fgeo2 = vgeo2.p;
+            visc32.ivol = ivol.p;
+            visc32.q = vq.p;
+            visc32.ga = vga.p;
+            visc32.gb = vgb.p;
+            visc32.mu_ref = (float)cfg.mu_ref;
+            visc32.T_ref = (float)cfg.T_mu_ref;
+            visc32.S = (float)cfg.sutherland_S;
+            visc32.cp_over_pr = (float)visc.cp_over_pr;
+            visc32.inv_cv = (float)(1.0 / gas.cv);
+        }
     }
     // compulsory bytes of one stage: reconstruction + flux (face states in,
     // G out, face geometry) + update (G gathered, state in/out)

