@@ -68,6 +68,7 @@ enum { MGPU_RECON_FO = 0, MGPU_RECON_TENO = 1 };
 enum { MGPU_BASIS_MONOMIAL = 0, MGPU_BASIS_LEGENDRE = 1 };
 enum { MGPU_RIEMANN_RUSANOV = 0, MGPU_RIEMANN_HLL = 1, MGPU_RIEMANN_HLLC = 2 };
 enum { MGPU_INTEGRATOR_SSPRK3 = 0, MGPU_INTEGRATOR_FE = 1, MGPU_INTEGRATOR_RK4 = 2 };
+enum { MGPU_TABLES_GPU = 0, MGPU_TABLES_HOST = 1 };
 enum {
     MGPU_BC_SYMMETRY = 0,
     MGPU_BC_EXTRAPOLATION = 1,
@@ -188,6 +189,10 @@ typedef struct mgpu_config {
      * no-slip and adiabatic; other boundaries carry no viscous flux. */
     int viscous;
     double mu_ref, T_mu_ref, sutherland_S, prandtl;
+    /* Where mgpu_finalize computes the TENO least-squares tables
+     * (face_reconstruction.cpp:477-741): MGPU_TABLES_GPU (default; Legendre
+     * basis, else the host) or MGPU_TABLES_HOST.  Both give the same bits. */
+    int table_build;
 } mgpu_config;
 
 typedef struct mgpu_ctx mgpu_ctx;
@@ -359,6 +364,25 @@ int mgpu_autotune(mgpu_ctx* ctx, double* ms, int* best);
 /* Algorithmic (compulsory) bytes one reconstruction launch and one full
  * stage move, from the actual table sizes. */
 int mgpu_traffic_model(mgpu_ctx* ctx, double* recon_bytes, double* stage_bytes);
+/* A copy of one reconstruction table as the kernels read it (tiled layout,
+ * library cell order), to compare the GPU and host table builds.  dst null:
+ * only *bytes is set.  MGPU_ERR_ARG for a table this form does not hold. */
+enum {
+    MGPU_TABLE_P = 0,     /* double: pseudo-inverse (FP64 forms)          */
+    MGPU_TABLE_AREAS = 1, /* double: transformed areas (FP64 forms)       */
+    MGPU_TABLE_P32 = 2,   /* float: pseudo-inverse x areas (FP32 form)    */
+    MGPU_TABLE_NB = 3,    /* uint32: stencil neighbours (FP64 forms)      */
+    MGPU_TABLE_NB32 = 4,  /* uint32: stencil neighbours (FP32 form)       */
+    MGPU_TABLE_PHI = 5,   /* double: face-point basis shapes (FP64 forms) */
+    MGPU_TABLE_PHI32 = 6  /* float: face-point basis shapes (FP32 form)   */
+};
+int mgpu_get_table(mgpu_ctx* ctx, int field, void* dst, uint64_t* bytes);
+/* Wall seconds of mgpu_finalize's phases, seconds[7]: 0 face and cell
+ * numbering, 1 geometry and gather lists, 2 TENO stencil search (host), 3
+ * table pack (host; includes the host least squares when built there) and
+ * upload, 4 least squares on the GPU, 5 other TENO setup, 6 the remaining
+ * uploads. */
+int mgpu_build_times(mgpu_ctx* ctx, double* seconds);
 uint32_t mgpu_n_cells(const mgpu_ctx* ctx);
 
 /* ---- unit-level GPU entry points (known-answer tests) ------------------ */

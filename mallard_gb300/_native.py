@@ -65,7 +65,7 @@ class Config(C.Structure):
         ("rho_ref", C.c_double), ("p_min", C.c_double), ("p_max", C.c_double), ("teno_variant", C.c_int),
         ("precision", C.c_int), ("reorder", C.c_int), ("device", C.c_int),
         ("viscous", C.c_int), ("mu_ref", C.c_double), ("T_mu_ref", C.c_double), ("sutherland_S", C.c_double),
-        ("prandtl", C.c_double),
+        ("prandtl", C.c_double), ("table_build", C.c_int),
     ]
 
 
@@ -114,6 +114,8 @@ def lib():
         "mgpu_enable_kernel_timing": (i32, [vp, i32]),
         "mgpu_kernel_times": (i32, [vp, vp, vp]),
         "mgpu_traffic_model": (i32, [vp, P(f64), P(f64)]),
+        "mgpu_get_table": (i32, [vp, i32, vp, P(C.c_uint64)]),
+        "mgpu_build_times": (i32, [vp, vp]),
         "mgpu_autotune": (i32, [vp, vp, P(i32)]),
         "mgpu_batch_create": (i32, [u32, vp, vp, P(Config), P(vp)]),
         "mgpu_batch_add_boundary": (i32, [vp, u32, i32, vp, i32]),

@@ -124,6 +124,27 @@ struct Visc32Args {
     float mu_ref, T_ref, S, cp_over_pr, inv_cv;
 };
 
+// GPU build of the TENO least-squares tables (teno_tables.cu): one warp per
+// stencil of every cell, results in the tiled layout of TenoArgs.
+constexpr int LSQ_MAXQ = 8;
+struct LsqBuildArgs {
+    int n_cells;              // cells, library numbering
+    const uint32_t* cell_old; // library -> caller cell id
+    const double2* nodes;     // node coordinates
+    const uint3* tri;         // nodes of each cell (caller numbering)
+    const uint32_t* off_st;   // [4 n_cells + 1] stencil offsets (reference layout, caller numbering)
+    const uint32_t* st;       // stencil cells, target first (caller numbering)
+    int M, K, nq;             // stencil size, dofs, cell quadrature points
+    double qp[2 * LSQ_MAXQ], qw[LSQ_MAXQ];
+    int pidx[2 * 10];
+    double ipt[10];           // basis means of the target (face_reconstruction.cpp:598-602)
+    double* P;                // FP64 forms: pseudo-inverse, [tiles][4][M-1][K-1][8]
+    double* ar;               // FP64 forms: transformed areas, [tiles][4][M-1][8]
+    float* P4;                // FP32 form (P null): pseudo-inverse x areas, grouped by four
+    unsigned* err;            // 1 stencil size, 2 full-rank system, 4 singular Jacobian
+};
+cudaError_t launch_teno_lsq(const LsqBuildArgs& a, cudaStream_t s);
+
 struct SpecArgs {
     int n_cells;
     const int4* cfaces;     // faces of the cell in the reference's order, -1 = none

@@ -75,6 +75,9 @@ struct LsqWork;
 LsqWork* lsq_work_new();
 void lsq_work_free(LsqWork* w);
 void teno_stencil_lsq(const mgpu_mesh& m, const TenoTables& t, size_t stencil, LsqWork& w, double* pinv, double* areas);
+// Transformed area of cell c in its own reference frame (the first entry of
+// teno_stencil_lsq's areas for any stencil of c).
+double teno_target_area(const mgpu_mesh& m, const TenoTables& t, uint32_t c, LsqWork& w);
 // Complete tables in the reference layout.
 void build_teno_tables(const mgpu_mesh& m, int basis, int p, double factor, int q_cell, int q_face, TenoTables& t);
 

@@ -21,6 +21,7 @@
 
 #ifdef _OPENMP
 #include <omp.h>
+#include <chrono>
 #endif
 
 #include "host_ctx.h"
@@ -75,7 +76,68 @@ using namespace mgpu;
 // ---------------------------------------------------------------------------
 // mgpu_finalize: numbering, geometry precomputation, TENO tables, upload
 // ---------------------------------------------------------------------------
+
+// The least-squares tables of every stencil on the device (teno_tables.cu),
+// into P / ar (FP64 forms) or P4 (FP32 form), already allocated and zeroed.
+void mgpu_ctx::build_lsq_on_device(const TenoTables& t) {
+    const mgpu_mesh mv = mesh.view();
+    std::vector<uint3> h_tri(mv.n_cells);
+    for (uint32_t c = 0; c < mv.n_cells; ++c) {
+        const uint32_t* nc = mv.nodes_of_cell + mv.offsets_nodes_of_cell[c];
+        h_tri[c] = make_uint3(nc[0], nc[1], nc[2]);
+    }
+    std::vector<double2> h_nodes(mv.n_nodes);
+    for (uint32_t i = 0; i < mv.n_nodes; ++i) h_nodes[i] = make_double2(mv.node_coords[2 * (size_t)i], mv.node_coords[2 * (size_t)i + 1]);
+    DevArray<uint3> d_tri;
+    DevArray<double2> d_nodes;
+    DevArray<uint32_t> d_cold, d_off, d_st, d_err;
+    d_tri.upload(h_tri);
+    d_nodes.upload(h_nodes);
+    d_cold.upload(cell_old);
+    d_off.upload(t.off_stencils);
+    d_st.upload(t.stencils);
+    d_err.alloc(1);
+    LsqBuildArgs a{};
+    a.n_cells = (int)N;
+    a.cell_old = d_cold.p;
+    a.nodes = d_nodes.p;
+    a.tri = d_tri.p;
+    a.off_st = d_off.p;
+    a.st = d_st.p;
+    a.M = t.M;
+    a.K = t.K;
+    a.nq = t.qcell.n();
+    if (a.nq > LSQ_MAXQ || t.K > 10) throw Unsupported("GPU table build: cell quadrature or basis too large");
+    for (int q = 0; q < a.nq; ++q) {
+        a.qp[2 * q] = t.qcell.pts[2 * q];
+        a.qp[2 * q + 1] = t.qcell.pts[2 * q + 1];
+        a.qw[q] = t.qcell.wts[q];
+    }
+    for (int k = 0; k < t.K; ++k) {
+        a.pidx[2 * k] = t.pidx[2 * k];
+        a.pidx[2 * k + 1] = t.pidx[2 * k + 1];
+        a.ipt[k] = t.ipt[k];
+    }
+    a.P = single() ? nullptr : P.p;
+    a.ar = single() ? nullptr : ar.p;
+    a.P4 = single() ? P4.p : nullptr;
+    a.err = d_err.p;
+    ck(launch_teno_lsq(a, stream), "GPU table build");
+    unsigned err = 0;
+    ck(cudaMemcpyAsync(&err, d_err.p, sizeof(unsigned), cudaMemcpyDeviceToHost, stream), "D2H");
+    ck(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+    if (err & 4u) throw ArgFail("Matrix is singular.");
+    if (err & 2u) throw Unsupported("least-squares system took the full-rank branch");
+    if (err & 1u) throw Unsupported("unexpected stencil shape");
+}
+
 void mgpu_ctx::build() {
+    const auto t_start = std::chrono::steady_clock::now();
+    auto lap = [&, t = t_start](int phase) mutable {
+        const auto now = std::chrono::steady_clock::now();
+        build_s[phase] += std::chrono::duration<double>(now - t).count();
+        t = now;
+    };
     const mgpu_mesh mv = mesh.view();
     N = mv.n_cells;
     if (N == 0) throw ArgFail("mesh has no cells");
@@ -143,6 +205,7 @@ void mgpu_ctx::build() {
     face_new.assign(mv.n_faces, -1);
     for (uint32_t i = 0; i < F_real; ++i) face_new[face_old[i]] = (int32_t)i;
 
+    lap(0);
     // --- per-face geometry (reference unit<2>, spectral-radius distance)
     std::vector<int2> h_lr(F_real);
     std::vector<double2> h_nrm(F_real);
@@ -211,12 +274,14 @@ void mgpu_ctx::build() {
     if (nq > 2) throw Unsupported("the GPU path supports 1 or 2 face quadrature points");
     for (int q = 0; q < nq; ++q) qw[q] = qf.wts[q];
 
+    lap(1);
     // --- TENO tables straight into the tiled layout
     const size_t tiles = (N + TILE - 1) / TILE;
     if (cfg.recon == MGPU_RECON_TENO) {
         TenoTables t;
         build_teno_stencils(mv, cfg.basis, cfg.poly_order, cfg.max_stencil_size_factor, cfg.quadrature_order_cell,
                             cfg.quadrature_order_face, t);
+        lap(2);
         K = t.K;
         M = t.M;
         if (!((K == 10 && M == 20 && nq == 2) || (K == 6 && M == 12 && nq == 1) || (K == 3 && M == 6 && nq == 1)))
@@ -226,6 +291,9 @@ void mgpu_ctx::build() {
         // loads (flat index j*(K-1)+k for P, (face*n_q+q)*(K-1)+k for phi),
         // with the transformed areas folded into P
         const bool f32 = single();
+        // least squares on the GPU (teno_tables.cu) unless asked for the host
+        // build or the basis is monomial (std::pow)
+        const bool gpu_lsq = cfg.table_build == MGPU_TABLES_GPU && cfg.basis == MGPU_BASIS_LEGENDRE;
         const size_t GJ = (MR + 3) / 4, GP = ((size_t)MR * KR + 3) / 4, GF = ((size_t)NF * nq * KR + 3) / 4;
         auto at4 = [](size_t group, size_t lane, size_t e) { return (group * TILE + lane) * 4 + e; };
         std::vector<uint32_t> h_cface(tiles * NF * TILE, 0), h_nb, h_nb4;
@@ -233,12 +301,14 @@ void mgpu_ctx::build() {
         std::vector<float> h_P4, h_phi4;
         if (f32) {
             h_nb4.assign(tiles * S * GJ * TILE * 4, 0);
-            h_P4.assign(tiles * S * GP * TILE * 4, 0.0f);
+            if (!gpu_lsq) h_P4.assign(tiles * S * GP * TILE * 4, 0.0f);
             h_phi4.assign(tiles * GF * TILE * 4, 0.0f);
         } else {
             h_nb.assign(tiles * S * MR * TILE, 0);
-            h_ar.assign(tiles * S * MR * TILE, 0.0);
-            h_P.assign(tiles * S * MR * KR * TILE, 0.0);
+            if (!gpu_lsq) {
+                h_ar.assign(tiles * S * MR * TILE, 0.0);
+                h_P.assign(tiles * S * MR * KR * TILE, 0.0);
+            }
             h_phi.assign(tiles * NF * nq * KR * TILE, 0.0);
         }
         std::vector<uint8_t> h_sm(N, 0);
@@ -263,13 +333,22 @@ void mgpu_ctx::build() {
                         const int Ms = (int)(t.off_stencils[si + 1] - so);
                         if (Ms == 0) continue;
                         if (Ms != M || t.stencils[so] != o) throw Unsupported("unexpected stencil shape");
-                        teno_stencil_lsq(mv, t, si, *w, pinv.data(), ars.data());
-                        for (int j = 0; j < M; ++j)
-                            if (pinv[j] != 0.0) throw Unsupported("least-squares system took the full-rank branch");
-                        for (int k = 0; k < K; ++k)
-                            if (pinv[(size_t)k * M] != 0.0) throw Unsupported("least-squares system took the full-rank branch");
                         sm |= (uint8_t)(1u << s);
-                        for (int j = 1; j < M; ++j) {
+                        if (gpu_lsq) {
+                            for (int j = 1; j < M; ++j) {
+                                const size_t jj = j - 1;
+                                if (f32) h_nb4[at4((tile * S + s) * GJ + jj / 4, lane, jj % 4)] = cell_new[t.stencils[so + j]];
+                                else h_nb[((tile * S + s) * MR + jj) * TILE + lane] = cell_new[t.stencils[so + j]];
+                            }
+                            if (s == 0) ars[0] = teno_target_area(mv, t, o, *w);
+                        } else {
+                            teno_stencil_lsq(mv, t, si, *w, pinv.data(), ars.data());
+                            for (int j = 0; j < M; ++j)
+                                if (pinv[j] != 0.0) throw Unsupported("least-squares system took the full-rank branch");
+                            for (int k = 0; k < K; ++k)
+                                if (pinv[(size_t)k * M] != 0.0) throw Unsupported("least-squares system took the full-rank branch");
+                        }
+                        for (int j = 1; j < M && !gpu_lsq; ++j) {
                             if (f32) {
                                 const size_t jj = j - 1;
                                 h_nb4[at4((tile * S + s) * GJ + jj / 4, lane, jj % 4)] = cell_new[t.stencils[so + j]];
@@ -344,14 +423,23 @@ void mgpu_ctx::build() {
             }
         if (f32) {
             nb4.upload(h_nb4);
-            P4.upload(h_P4);
+            if (gpu_lsq) P4.alloc(tiles * S * GP * TILE * 4);
+            else P4.upload(h_P4);
             phi4.upload(h_phi4);
         } else {
             nb.upload(h_nb);
-            ar.upload(h_ar);
-            P.upload(h_P);
+            if (gpu_lsq) {
+                ar.alloc(tiles * S * MR * TILE);
+                P.alloc(tiles * S * MR * KR * TILE);
+            } else {
+                ar.upload(h_ar);
+                P.upload(h_P);
+            }
             phi.upload(h_phi);
         }
+        lap(3);
+        if (gpu_lsq) build_lsq_on_device(t);
+        lap(4);
         cface.upload(h_cface);
         smask.upload(h_sm);
         teno.nb = nb.p;
@@ -373,6 +461,7 @@ void mgpu_ctx::build() {
         recon_bytes = (double)F_flux * (8 + 64) + (double)N * 32;
     }
 
+    lap(5);
     // --- BCs
     bct.n = (int)bcs.size();
     for (size_t i = 0; i < bcs.size(); ++i) {
@@ -485,6 +574,7 @@ void mgpu_ctx::build() {
     const double flux_b = (double)F_flux * (nq * 64 + 32 + 8 + 16 + 8 + 1);
     const double upd_b = (double)N * (16 + 8 + 32 * 4) + (double)F_flux * 32 * 2;
     stage_bytes = recon_bytes + flux_b + upd_b;
+    lap(6);
     finalized = true;
 }
 
@@ -521,6 +611,7 @@ void mgpu_config_defaults(mgpu_config* c) {
     c->T_mu_ref = 1.0;
     c->sutherland_S = 0.0;
     c->prandtl = 0.72;
+    c->table_build = MGPU_TABLES_GPU;
 }
 
 int mgpu_create(const mgpu_mesh* mesh, const mgpu_config* cfg, mgpu_ctx** out) {
@@ -534,6 +625,8 @@ int mgpu_create(const mgpu_mesh* mesh, const mgpu_config* cfg, mgpu_ctx** out) {
         if (cfg->precision != MGPU_PREC_FP64 && cfg->precision != MGPU_PREC_FP64_FAST &&
             cfg->precision != MGPU_PREC_FP32)
             throw Unsupported("unknown precision mode");
+        if (cfg->table_build != MGPU_TABLES_GPU && cfg->table_build != MGPU_TABLES_HOST)
+            throw ArgFail("table_build: MGPU_TABLES_GPU or MGPU_TABLES_HOST");
         if (cfg->viscous && !(cfg->mu_ref >= 0.0 && cfg->prandtl > 0.0 && (cfg->sutherland_S <= 0.0 || cfg->T_mu_ref > 0.0)))
             throw ArgFail("viscous flux: mu_ref >= 0, prandtl > 0 and, with Sutherland's law, T_mu_ref > 0");
         if (cfg->precision == MGPU_PREC_FP32 &&
@@ -914,6 +1007,39 @@ int mgpu_traffic_model(mgpu_ctx* ctx, double* recon_bytes, double* stage_bytes) 
     if (recon_bytes) *recon_bytes = ctx->recon_bytes;
     if (stage_bytes) *stage_bytes = ctx->stage_bytes;
     return MGPU_OK;
+}
+
+int mgpu_build_times(mgpu_ctx* ctx, double* seconds) {
+    if (int rc = need_ready(ctx)) return rc;
+    if (!seconds) return MGPU_ERR_ARG;
+    for (int i = 0; i < 7; ++i) seconds[i] = ctx->build_s[i];
+    return MGPU_OK;
+}
+
+int mgpu_get_table(mgpu_ctx* ctx, int field, void* dst, uint64_t* bytes) {
+    if (int rc = need_ready(ctx)) return rc;
+    return guarded([&] {
+        if (!bytes) throw ArgFail("null argument");
+        const void* src = nullptr;
+        size_t n = 0;
+        switch (field) {
+            case MGPU_TABLE_P: src = ctx->P.p; n = ctx->P.bytes(); break;
+            case MGPU_TABLE_AREAS: src = ctx->ar.p; n = ctx->ar.bytes(); break;
+            case MGPU_TABLE_P32: src = ctx->P4.p; n = ctx->P4.bytes(); break;
+            case MGPU_TABLE_NB: src = ctx->nb.p; n = ctx->nb.bytes(); break;
+            case MGPU_TABLE_NB32: src = ctx->nb4.p; n = ctx->nb4.bytes(); break;
+            case MGPU_TABLE_PHI: src = ctx->phi.p; n = ctx->phi.bytes(); break;
+            case MGPU_TABLE_PHI32: src = ctx->phi4.p; n = ctx->phi4.bytes(); break;
+            default: throw ArgFail("unknown table");
+        }
+        if (!src) throw ArgFail("this form holds no such table");
+        *bytes = n;
+        if (dst) {
+            ck(cudaMemcpyAsync(dst, src, n, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+            ck(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+        }
+        return MGPU_OK;
+    });
 }
 
 uint32_t mgpu_n_cells(const mgpu_ctx* ctx) { return ctx ? ctx->mesh.n_cells : 0; }

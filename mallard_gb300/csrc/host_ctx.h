@@ -311,6 +311,8 @@ struct mgpu_ctx {
     }
 
     void build();
+    void build_lsq_on_device(const TenoTables& t);
+    double build_s[7] = {0, 0, 0, 0, 0, 0, 0};  // mgpu_build_times
 };
 
 namespace mgpu {

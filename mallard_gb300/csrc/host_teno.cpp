@@ -478,6 +478,11 @@ void teno_stencil_lsq(const mgpu_mesh& m, const TenoTables& t, size_t stencil, L
     stencil_pinv(t, Ms, w.s, pinv);
 }
 
+double teno_target_area(const mgpu_mesh& m, const TenoTables& t, uint32_t c, LsqWork& w) {
+    stencil_moments(m, t, c, &c, 1, w.s);
+    return w.s.at[0];
+}
+
 void build_teno_stencils(const mgpu_mesh& m, int basis, int p, double factor, int q_cell, int q_face, TenoTables& t) {
     if (p < 1 || p > 4) throw std::runtime_error("TENO basis order must be 1..4");
     t.basis = basis;

@@ -80,10 +80,12 @@ class Solver:
                  max_stencil_size_factor=2.0, quadrature_order_cell=0, quadrature_order_face=0,
                  riemann_solver="HLLC", time_integrator="SSPRK3", gamma=1.4, p_ref=101325.0, T_ref=298.15,
                  rho_ref=1.225, p_min=-1e20, p_max=1e20, boundaries=(), teno_variant="reference", reorder=True,
-                 device=0, precision="fp64", viscous=None):
+                 device=0, precision="fp64", viscous=None, table_build="gpu"):
         """viscous: None for the Euler path, or a dict with mu_ref and
         optionally T_mu_ref, sutherland_S, prandtl (the viscous face flux,
-        no counterpart in the reference; walls become no-slip)."""
+        no counterpart in the reference; walls become no-slip).
+        table_build: "gpu" (least-squares tables built by a kernel; Legendre
+        basis) or "host"; both give the same bits."""
         self._lib = N.lib()
         self.mesh = mesh
         self.gas = dict(gamma=gamma, p_ref=p_ref, T_ref=T_ref, rho_ref=rho_ref)
@@ -113,6 +115,9 @@ class Solver:
         self.precision = precision
         cfg.reorder = 1 if reorder else 0
         cfg.device = int(device)
+        if table_build not in ("gpu", "host"):
+            raise RuntimeError(f"Unknown table build: {table_build}.")
+        cfg.table_build = 0 if table_build == "gpu" else 1
         if viscous:
             cfg.viscous = 1
             cfg.mu_ref = float(viscous["mu_ref"])
@@ -276,6 +281,28 @@ class Solver:
         r, s = C.c_double(), C.c_double()
         N.check(self._lib.mgpu_traffic_model(self._h, C.byref(r), C.byref(s)))
         return r.value, s.value
+
+    BUILD_PHASES = ("numbering", "geometry", "stencil_search", "table_pack", "gpu_least_squares", "teno_other",
+                    "uploads")
+
+    def build_times(self):
+        """Seconds of each phase of the solver's setup (mgpu_finalize)."""
+        t = np.zeros(7)
+        N.check(self._lib.mgpu_build_times(self._h, N.ptr(t)))
+        return dict(zip(self.BUILD_PHASES, t.tolist()))
+
+    TABLES = {"P": (0, np.float64), "areas": (1, np.float64), "P32": (2, np.float32), "nb": (3, np.uint32),
+              "nb32": (4, np.uint32), "phi": (5, np.float64), "phi32": (6, np.float32)}
+
+    def get_table(self, name):
+        """One reconstruction table as the kernels read it (tiled layout,
+        library cell order), as a flat array."""
+        field, dt = self.TABLES[name]
+        n = C.c_uint64()
+        N.check(self._lib.mgpu_get_table(self._h, field, None, C.byref(n)))
+        out = np.zeros(n.value // np.dtype(dt).itemsize, dtype=dt)
+        N.check(self._lib.mgpu_get_table(self._h, field, out.ctypes.data_as(C.c_void_p), C.byref(n)))
+        return out
 
     # ---- construction from the reference's TOML input -------------------------
     @classmethod
