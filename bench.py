@@ -297,7 +297,9 @@ def time_form(m, args, form, U0, W0, device, selector, barrier=None, clocks=None
     if FORMS[form][0] == "fp32":
         shape, tms = s.autotune()
         tune = {"chosen_shape": shape, "ms_per_shape": [round(x, 4) for x in tms],
-                "shapes": "0: 128 thr/<=128 regs, 1: 128/<=80, 2: 128/<=64, 3: 256/<=64"}
+                "shapes": "0: 128 thr/<=128 regs, 1: 128/<=80, 2: 128/<=64, 3: 256/<=64, "
+                          "4-6: staged (bulk copies to shared memory) 1 slot x 4 warps/<=80, 2 x 2/<=128, "
+                          "1 x 4/<=128"}
         s.set_state(U0, W0)
     s.launch(CFL, args.warmup)
     s.synchronize()

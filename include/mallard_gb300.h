@@ -224,7 +224,8 @@ int mgpu_take_step(mgpu_ctx* ctx, double dt);
 /* n_steps x (spectral radius -> dt = cfl / max -> SSPRK3 step) without host
  * round trips; t_out (optional) receives the simulated time advanced. */
 int mgpu_run(mgpu_ctx* ctx, double cfl, uint32_t n_steps, double* t_out);
-/* Device error flags: bit 0 non-finite state, bit 1 non-positive dt. */
+/* Device error flags: bit 0 non-finite state, bit 1 non-positive dt, bit 2
+ * a bounded device wait ran out (MGPU_ERR_TIMEOUT). */
 int mgpu_status(mgpu_ctx* ctx, uint32_t* flags);
 
 /* The CFL time step of the resident state (as mgpu_calc_dt) for callers
@@ -354,13 +355,19 @@ int mgpu_batch_autotune(mgpu_batch* b, double* ms, int* shape, int* blocks_per_s
 int mgpu_enable_kernel_timing(mgpu_ctx* ctx, int enable);
 int mgpu_kernel_times(mgpu_ctx* ctx, double* ms, uint32_t* launches);
 /* Autotuner: times each launch shape of the reconstruction kernel (FP32
- * form at p = 3: 128-thread blocks with at most 128, 80 or 64 registers per
- * thread, or 256-thread blocks with 64)
- * on the current state, three launches each after a warm-up, and keeps the
- * fastest for later launches.  ms[4] receives the average time per shape
- * (0 where not applicable), best the chosen shape.  Both may be NULL.  Other
- * forms have a single shape. */
+ * form at p = 3: 0-2 128-thread blocks with at most 128, 80 or 64 registers
+ * per thread, 3 256-thread blocks with 64, 4-6 the staged kernel, whose
+ * warps copy their tile's table blocks into shared memory with bulk async
+ * copies: one stencil slot per warp and 4 warps per block with at most 80
+ * registers, two slots and 2 warps, one slot and 4 warps with 128) on the
+ * current state, three launches each after a warm-up, and keeps the fastest
+ * for later launches.  ms[7]
+ * receives the average time per shape (0 where not applicable), best the
+ * chosen shape.  Both may be NULL.  Other forms have a single shape. */
 int mgpu_autotune(mgpu_ctx* ctx, double* ms, int* best);
+/* Fix the reconstruction's launch shape (as mgpu_autotune numbers them);
+ * every shape gives the same results. */
+int mgpu_set_launch_shape(mgpu_ctx* ctx, int shape);
 /* Algorithmic (compulsory) bytes one reconstruction launch and one full
  * stage move, from the actual table sizes. */
 int mgpu_traffic_model(mgpu_ctx* ctx, double* recon_bytes, double* stage_bytes);

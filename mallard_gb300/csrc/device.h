@@ -58,6 +58,7 @@ struct TenoArgs {
     double oi[KR_MAX * KR_MAX];   // oscillation indicator without dof 0, row-major (K-1)^2
     double oi2[KR_MAX * KR_MAX];  // same, upper triangle with doubled off-diagonals (fast form)
     float oi2f[KR_MAX * KR_MAX];  // oi2 in FP32 (FP32-bulk form)
+    unsigned* err;                // status word: bit 2 when a bounded wait ran out (staged FP32 form)
 };
 
 struct FluxArgs {
@@ -179,8 +180,11 @@ MGPU_DECLARE_TENO_FLUX
 namespace f32 {
 // shape: launch shape 0..3 (128-thread blocks with at most 128, 80 or 64
 // registers, or 256-thread blocks with 64; p = 3 only, other orders use
-// shape 0), chosen by the autotuner
+// shape 0), chosen by the autotuner; the single-case launchers also take
+// shapes 4 to 6, the staged form that copies each tile's table blocks into
+// shared memory with cp.async.bulk
 constexpr int TENO32_SHAPES = 4;
+constexpr int TENO32_SHAPES_SINGLE = 7;
 // U: the FP32 copy of the stage state
 cudaError_t launch_teno(const TenoArgs& a, int K, int M, int nq, const float* U, float* fv, uint8_t* masks,
                         int shape, cudaStream_t s);

@@ -14,6 +14,7 @@
 // Stencil selection uses ratios of smoothness indicators: (SI+eps)^-6 itself
 // overflows FP32, but w_s / sum w = 1 / sum_d ((SI_s+eps)/(SI_d+eps))^6 does
 // not.  Only the corrected weighting is built in this form.
+#include <algorithm>
 #include <cstdint>
 
 #include "fp_convert.cuh"
@@ -46,21 +47,56 @@ struct IxB {
     __device__ __forceinline__ size_t f(size_t fi) const { return fbase + (((fi >> 3) * C + cs) << 3) + (fi & 7); }
 };
 
+// Table blocks of one tile: for stencil s the neighbour ids [GJ][8] uint4
+// and the pseudo-inverse [GP][8] float4, and the face shapes [GF][8] float4,
+// each contiguous in the tiled arrays.
+template <int K, int M, int NQ>
+struct TileBlocks {
+    static constexpr int KR = K - 1, MR = M - 1, NF = 3, S = 4;
+    static constexpr int GJ = (MR + 3) / 4, GP = (MR * KR + 3) / 4, GF = (NF * NQ * KR + 3) / 4;
+    static constexpr unsigned PB = GP * TILE * 16, NBB = GJ * TILE * 16, FB = GF * TILE * 16;
+};
+
+// Table source of teno32_cell: the tiled arrays in global memory.
+template <int K, int M, int NQ>
+struct GlobalSrc {
+    using B = TileBlocks<K, M, NQ>;
+    const TenoArgs& a;
+    int tile;
+    __device__ __forceinline__ unsigned tile_need(unsigned need) const { return need; }
+    __device__ __forceinline__ bool begin(int) { return true; }
+    __device__ __forceinline__ void end(int) {}
+    __device__ __forceinline__ const uint4* nb(int s) const {
+        return reinterpret_cast<const uint4*>(a.nb4) + (size_t)(tile * B::S + s) * B::GJ * TILE;
+    }
+    __device__ __forceinline__ const float4* P(int s) const {
+        return reinterpret_cast<const float4*>(a.P4) + (size_t)(tile * B::S + s) * B::GP * TILE;
+    }
+    __device__ __forceinline__ const float4* phi() { return reinterpret_cast<const float4*>(a.phi4) + (size_t)tile * B::GF * TILE; }
+    template <class T>
+    __device__ __forceinline__ T ld(const T* p) const { return __ldg(p); }
+};
+
 // Reconstruction of variable v of one cell.  live: lanes of the warp whose
-// cells exist (the four lanes of a cell share its fate).
-template <int K, int M, int NQ, bool SEL, class IX>
-__device__ __forceinline__ void teno32_cell(const TenoArgs& a, const float* __restrict__ U, float* __restrict__ fv,
+// cells exist (the four lanes of a cell share its fate).  src: where the
+// tile's table blocks are read (GlobalSrc, or shared memory filled by bulk
+// copies); the stencil loop visits src.tile_need(need), which a shared-memory
+// source makes the same for the whole warp.  Returns false when the source
+// failed (nothing written).  alive false: a lane past the mesh that only
+// takes part in the warp's collective steps (reads and writes nothing).
+template <int K, int M, int NQ, bool SEL, class IX, class SRC>
+__device__ __forceinline__ bool teno32_cell(const TenoArgs& a, const float* __restrict__ U, float* __restrict__ fv,
                                             uint8_t* __restrict__ masks, const uint8_t* __restrict__ pred, int cell,
-                                            int v, unsigned live, const IX& ix) {
+                                            int v, unsigned live, const IX& ix, SRC& src, bool alive = true) {
     constexpr int KR = K - 1, MR = M - 1, NF = 3, S = 4;
     constexpr int GJ = (MR + 3) / 4, GP = (MR * KR + 3) / 4, GF = (NF * NQ * KR + 3) / 4;
     const int tile = cell >> 3, lane = cell & 7;
-    const float uc = U[ix.u(cell) * NC + v];
-    const unsigned sm = a.smask[cell];
+    const float uc = alive ? U[ix.u(cell) * NC + v] : 0.0f;
+    const unsigned sm = alive ? a.smask[cell] : 0u;
     unsigned need = sm, pm = 0;
     bool conf = false;
     if (SEL) {
-        const unsigned p = pred[ix.u(cell) * NC + v];
+        const unsigned p = alive ? pred[ix.u(cell) * NC + v] : 0u;
         pm = p & sm & 0xFu;
         conf = (p & 0x80u) && pm;
         unsigned my = conf ? pm : sm;
@@ -69,6 +105,8 @@ __device__ __forceinline__ void teno32_cell(const TenoArgs& a, const float* __re
         need = my;
     }
 
+    const unsigned tile_need = src.tile_need(need);
+    bool ok = true;
     float coef[S][KR];
     float x[S];
 #pragma unroll
@@ -76,40 +114,45 @@ __device__ __forceinline__ void teno32_cell(const TenoArgs& a, const float* __re
 #pragma unroll
         for (int k = 0; k < KR; ++k) coef[s][k] = 0.0f;
         x[s] = 0.0f;
-        if (!((need >> s) & 1u)) continue;
-        // differences to the target cell's average over the stencil
-        const uint4* nbp = reinterpret_cast<const uint4*>(a.nb4) + ((size_t)(tile * S + s) * GJ) * TILE + lane;
-        float d[GJ * 4];
+        if (!((tile_need >> s) & 1u)) continue;
+        ok = src.begin(s) && ok;
+        if (ok && ((need >> s) & 1u)) {
+            // differences to the target cell's average over the stencil
+            const uint4* nbp = src.nb(s) + lane;
+            float d[GJ * 4];
 #pragma unroll
-        for (int g = 0; g < GJ; ++g) {
-            const uint4 n = __ldg(nbp + g * TILE);
-            const uint32_t id[4] = {n.x, n.y, n.z, n.w};
+            for (int g = 0; g < GJ; ++g) {
+                const uint4 n = src.ld(nbp + g * TILE);
+                const uint32_t id[4] = {n.x, n.y, n.z, n.w};
 #pragma unroll
-            for (int e = 0; e < 4; ++e)
-                if (g * 4 + e < MR) d[g * 4 + e] = __ldg(U + ix.u(id[e]) * NC + v) - uc;
-        }
-        // coefficients = (P x areas) . d, accumulated over the stencil in order
-        const float4* Pp = reinterpret_cast<const float4*>(a.P4) + ((size_t)(tile * S + s) * GP) * TILE + lane;
+                for (int e = 0; e < 4; ++e)
+                    if (g * 4 + e < MR) d[g * 4 + e] = __ldg(U + ix.u(id[e]) * NC + v) - uc;
+            }
+            // coefficients = (P x areas) . d, accumulated over the stencil in order
+            const float4* Pp = src.P(s) + lane;
 #pragma unroll
-        for (int g = 0; g < GP; ++g) {
-            const float4 p4 = __ldg(Pp + g * TILE);
-            const float pv[4] = {p4.x, p4.y, p4.z, p4.w};
+            for (int g = 0; g < GP; ++g) {
+                const float4 p4 = src.ld(Pp + g * TILE);
+                const float pv[4] = {p4.x, p4.y, p4.z, p4.w};
 #pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                const int fl = g * 4 + e;
-                if (fl < MR * KR) coef[s][fl % KR] = fmaf(pv[e], d[fl / KR], coef[s][fl % KR]);
+                for (int e = 0; e < 4; ++e) {
+                    const int fl = g * 4 + e;
+                    if (fl < MR * KR) coef[s][fl % KR] = fmaf(pv[e], d[fl / KR], coef[s][fl % KR]);
+                }
+            }
+            if (!(SEL && conf)) {
+                float si = 0.0f;
+#pragma unroll
+                for (int i = 0; i < KR; ++i) {
+                    float oa = a.oi2f[i * KR + i] * coef[s][i];
+#pragma unroll
+                    for (int l = i + 1; l < KR; ++l) oa = fmaf(a.oi2f[i * KR + l], coef[s][l], oa);
+                    si = fmaf(coef[s][i], oa, si);
+                }
+                x[s] = si + 1.0e-12f;
             }
         }
-        if (SEL && conf) continue;
-        float si = 0.0f;
-#pragma unroll
-        for (int i = 0; i < KR; ++i) {
-            float oa = a.oi2f[i * KR + i] * coef[s][i];
-#pragma unroll
-            for (int l = i + 1; l < KR; ++l) oa = fmaf(a.oi2f[i * KR + l], coef[s][l], oa);
-            si = fmaf(coef[s][i], oa, si);
-        }
-        x[s] = si + 1.0e-12f;
+        src.end(s);
     }
 
     unsigned mask = 0;
@@ -158,7 +201,7 @@ __device__ __forceinline__ void teno32_cell(const TenoArgs& a, const float* __re
         for (int s = 1; s < S; ++s) w[s] = ((mask >> s) & 1u) ? share : 0.0f;
     }
     }
-    if (masks) masks[ix.u(cell) * NC + v] = (uint8_t)mask;
+    if (ok && alive && masks) masks[ix.u(cell) * NC + v] = (uint8_t)mask;
     // blended coefficients
     float c[KR];
 #pragma unroll
@@ -170,11 +213,13 @@ __device__ __forceinline__ void teno32_cell(const TenoArgs& a, const float* __re
     }
 
     // face values: shapes of all face points, then one dot product each
-    const float4* php = reinterpret_cast<const float4*>(a.phi4) + (size_t)tile * GF * TILE + lane;
+    const float4* php = src.phi();
+    if (!php || !ok || !alive) return false;
+    php += lane;
     float phi[GF * 4];
 #pragma unroll
     for (int g = 0; g < GF; ++g) {
-        const float4 p4 = __ldg(php + g * TILE);
+        const float4 p4 = src.ld(php + g * TILE);
         phi[g * 4] = p4.x;
         phi[g * 4 + 1] = p4.y;
         phi[g * 4 + 2] = p4.z;
@@ -193,6 +238,7 @@ __device__ __forceinline__ void teno32_cell(const TenoArgs& a, const float* __re
             fv[((ix.f(fi) * NQ + q) * 2 + side) * NC + v] = out;
         }
     }
+    return true;
 }
 
 template <int K, int M, int NQ, bool SEL, int BS, int MINB>
@@ -203,7 +249,160 @@ __global__ void __launch_bounds__(BS, MINB) teno32_kernel(const TenoArgs a, cons
     const int cell = gt >> 2, v = gt & 3;
     const unsigned live = __ballot_sync(0xffffffffu, cell < a.n_cells);
     if (cell >= a.n_cells) return;
-    teno32_cell<K, M, NQ, SEL>(a, U, fv, masks, pred, cell, v, live, Ix1{});
+    GlobalSrc<K, M, NQ> src{a, cell >> 3};
+    teno32_cell<K, M, NQ, SEL>(a, U, fv, masks, pred, cell, v, live, Ix1{}, src);
+}
+
+// Staged form: each warp (one 8-cell tile) copies the table blocks of the
+// stencils its cells evaluate into shared memory with cp.async.bulk, NSLOT
+// stencils at a time (a slot is refilled with the next stencil as soon as
+// the warp is done with it), and the face shapes into a slot of their own;
+// an mbarrier per slot tracks the bytes.  One bulk copy replaces the dozens
+// of dependent table loads of the direct form, so the warp's table traffic
+// is in flight at once while it gathers the neighbours' states.
+constexpr unsigned STAGE_WAIT_LIMIT = 1u << 22;
+
+__device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+    const uint32_t addr = su32(bar);
+    for (unsigned i = 0; i < STAGE_WAIT_LIMIT; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(addr), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     su32(dst)),
+                 "l"(src), "r"(bytes), "r"(su32(bar))
+                 : "memory");
+}
+
+template <int K, int M, int NQ, int NSLOT>
+struct StageLayout {
+    using B = TileBlocks<K, M, NQ>;
+    static constexpr unsigned SLOT = B::PB + B::NBB;                // pseudo-inverse, then neighbour ids
+    static constexpr unsigned PHI = NSLOT * SLOT;                   // face shapes
+    static constexpr unsigned BAR = PHI + B::FB;                    // NSLOT + 1 mbarriers
+    static constexpr unsigned WARP = (BAR + 8 * (NSLOT + 1) + 127) / 128 * 128;
+    static_assert(B::PB % 128 == 0 && B::NBB % 16 == 0 && SLOT % 128 == 0 && B::FB % 16 == 0, "alignment");
+};
+
+// Table source of teno32_cell: one warp's shared-memory stage.
+template <int K, int M, int NQ, int NSLOT>
+struct StageSrc {
+    using B = TileBlocks<K, M, NQ>;
+    using L = StageLayout<K, M, NQ, NSLOT>;
+    const TenoArgs& a;
+    uint8_t* base;
+    int tile, lane32;
+    unsigned need_all = 0;  // stencils some cell of the tile evaluates
+    int cnt = 0, issued = 0;
+    bool phi_ready = false, ok = true;
+    __device__ __forceinline__ uint64_t* bar(int i) { return reinterpret_cast<uint64_t*>(base + L::BAR) + i; }
+    // the i-th stencil of need_all into slot i % NSLOT (lane 0)
+    __device__ __forceinline__ void issue(int i) {
+        unsigned m = need_all;
+        for (int k = 0; k < i; ++k) m &= m - 1;
+        const int s = __ffs(m) - 1;
+        uint8_t* slot = base + (i % NSLOT) * L::SLOT;
+        mbar_expect_tx(bar(i % NSLOT), L::SLOT);
+        bulk_g2s(slot, reinterpret_cast<const char*>(a.P4) + (size_t)(tile * B::S + s) * B::PB, B::PB, bar(i % NSLOT));
+        bulk_g2s(slot + B::PB, reinterpret_cast<const char*>(a.nb4) + (size_t)(tile * B::S + s) * B::NBB, B::NBB,
+                 bar(i % NSLOT));
+    }
+    // all lanes: the union of the cells' stencils, then the first copies
+    __device__ __forceinline__ unsigned tile_need(unsigned need) {
+        need_all = __reduce_or_sync(0xffffffffu, need);
+        cnt = __popc(need_all);
+        issued = cnt < NSLOT ? cnt : NSLOT;
+        if (lane32 == 0)
+            for (int i = 0; i < issued; ++i) issue(i);
+        return need_all;
+    }
+    __device__ __forceinline__ int index(int s) const { return __popc(need_all & ((1u << s) - 1u)); }
+    __device__ __forceinline__ bool begin(int s) {
+        const int i = index(s);
+        const bool done = mbar_wait(bar(i % NSLOT), (unsigned)(i / NSLOT) & 1u);
+        ok = __all_sync(0xffffffffu, done) && ok;
+        return ok;
+    }
+    __device__ __forceinline__ void end(int s) {
+        const int i = index(s);
+        __syncwarp();
+        // refill the slot with the next stencil, unless a wait failed
+        if (ok && i + NSLOT < cnt) {
+            if (lane32 == 0) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                issue(i + NSLOT);
+            }
+            issued = i + NSLOT + 1;
+        }
+    }
+    __device__ __forceinline__ const uint4* nb(int s) const {
+        return reinterpret_cast<const uint4*>(base + (index(s) % NSLOT) * L::SLOT + B::PB);
+    }
+    __device__ __forceinline__ const float4* P(int s) const {
+        return reinterpret_cast<const float4*>(base + (index(s) % NSLOT) * L::SLOT);
+    }
+    __device__ __forceinline__ const float4* phi() {
+        if (!phi_ready) {
+            const bool done = mbar_wait(bar(NSLOT), 0u);
+            ok = __all_sync(0xffffffffu, done) && ok;
+            phi_ready = true;
+        }
+        return ok ? reinterpret_cast<const float4*>(base + L::PHI) : nullptr;
+    }
+    template <class T>
+    __device__ __forceinline__ T ld(const T* p) const { return *p; }
+};
+
+template <int K, int M, int NQ, bool SEL, int NSLOT, int WARPS, int MINB>
+__global__ void __launch_bounds__(WARPS * 32, MINB) teno32_staged_kernel(const TenoArgs a, const float* __restrict__ U,
+                                                                         float* __restrict__ fv,
+                                                                         uint8_t* __restrict__ masks,
+                                                                         const uint8_t* __restrict__ pred,
+                                                                         unsigned* __restrict__ err) {
+    using L = StageLayout<K, M, NQ, NSLOT>;
+    using B = TileBlocks<K, M, NQ>;
+    extern __shared__ __align__(128) uint8_t stage_smem[];
+    const int w = threadIdx.x >> 5, lane32 = threadIdx.x & 31;
+    const int tile = blockIdx.x * WARPS + w;
+    const int n_tiles = (a.n_cells + 7) >> 3;
+    if (tile >= n_tiles) return;
+    StageSrc<K, M, NQ, NSLOT> src{a, stage_smem + (size_t)w * L::WARP, tile, lane32};
+    if (lane32 == 0) {
+        for (int i = 0; i <= NSLOT; ++i) mbar_init(src.bar(i), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        // the face shapes first: needed last, by every cell
+        mbar_expect_tx(src.bar(NSLOT), B::FB);
+        bulk_g2s(src.base + L::PHI, reinterpret_cast<const char*>(a.phi4) + (size_t)tile * B::FB, B::FB, src.bar(NSLOT));
+    }
+    __syncwarp();
+    const int cell = tile * 8 + (lane32 >> 2), v = lane32 & 3;
+    // cells past the mesh take part in the warp's collective steps with
+    // nothing to do: smask 0, no prediction, no writes
+    teno32_cell<K, M, NQ, SEL>(a, U, fv, masks, pred, cell, v, 0xffffffffu, Ix1{}, src, cell < a.n_cells);
+    if (!src.ok) {
+        // a wait ran out: flag it and give every copy still pending on this
+        // warp's stage one more bounded wait before the shared memory goes
+        if (lane32 == 0 && err) atomicOr(err, 1u);
+        for (int i = 0; i <= NSLOT; ++i) {
+            const int uses = i == NSLOT ? 1 : (i < src.issued ? (src.issued - i + NSLOT - 1) / NSLOT : 0);
+            if (uses > 0) mbar_wait(src.bar(i), (unsigned)(uses - 1) & 1u);
+        }
+    }
 }
 
 // Primitive recovery of a face state: FP32, or FP64 when the internal energy
@@ -456,8 +655,30 @@ cudaError_t teno_go1(const TenoArgs& a, const float* U, float* fv, uint8_t* mask
     return cudaGetLastError();
 }
 
+// Staged form (teno32_staged_kernel): one warp per tile, WARPS per block.
+template <int K, int M, int NQ, bool SEL, int NSLOT, int WARPS, int MINB>
+cudaError_t teno_staged1(const TenoArgs& a, const float* U, float* fv, uint8_t* masks, const uint8_t* pred,
+                         cudaStream_t s) {
+    constexpr unsigned smem = WARPS * StageLayout<K, M, NQ, NSLOT>::WARP;
+    static bool attr = false;
+    if (!attr) {
+        const cudaError_t e = cudaFuncSetAttribute(teno32_staged_kernel<K, M, NQ, SEL, NSLOT, WARPS, MINB>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    const long long tiles = ((long long)a.n_cells + 7) / 8;
+    const unsigned blocks = (unsigned)((tiles + WARPS - 1) / WARPS);
+    if (blocks)
+        teno32_staged_kernel<K, M, NQ, SEL, NSLOT, WARPS, MINB><<<blocks, WARPS * 32, smem, s>>>(a, U, fv, masks, pred,
+                                                                                               a.err);
+    return cudaGetLastError();
+}
+
 // Launch shapes the autotuner chooses from: (block size, minimum resident
-// blocks per SM), i.e. register caps of 128, 80 and 64 per thread.
+// blocks per SM), i.e. register caps of 128, 80 and 64 per thread; shapes
+// 4-6 are the staged form (p = 3): one stencil slot per warp, 4 warps per
+// block, at most 80 registers; two slots, 2 warps, 128; one slot, 4 warps, 128.
 template <int K, int M, int NQ, bool SEL>
 cudaError_t teno_go(const TenoArgs& a, const float* U, float* fv, uint8_t* masks, const uint8_t* pred, int shape,
                     cudaStream_t s) {
@@ -466,6 +687,11 @@ cudaError_t teno_go(const TenoArgs& a, const float* U, float* fv, uint8_t* masks
         case 1: return teno_go1<K, M, NQ, SEL, 128, 6>(a, U, fv, masks, pred, s);
         case 2: return teno_go1<K, M, NQ, SEL, 128, 8>(a, U, fv, masks, pred, s);
         case 3: return teno_go1<K, M, NQ, SEL, 256, 4>(a, U, fv, masks, pred, s);
+    }
+    if constexpr (K == 10 && M == 20 && NQ == 2) {
+        if (shape == 4) return teno_staged1<K, M, NQ, SEL, 1, 4, 6>(a, U, fv, masks, pred, s);
+        if (shape == 5) return teno_staged1<K, M, NQ, SEL, 2, 2, 7>(a, U, fv, masks, pred, s);
+        if (shape == 6) return teno_staged1<K, M, NQ, SEL, 1, 4, 4>(a, U, fv, masks, pred, s);
     }
     return cudaErrorInvalidValue;
 }
@@ -493,8 +719,9 @@ __global__ void __launch_bounds__(BS, MINB) teno32_batch_kernel(const BatchLaunc
         const bool on = cell < b.n_cells[gi] && b.flags[b.case0[gi] + cs] == 0u;
         const unsigned live = __ballot_sync(0xffffffffu, on);
         if (!on) continue;
+        GlobalSrc<K, M, NQ> src{b.teno[gi], cell >> 3};
         teno32_cell<K, M, NQ, false>(b.teno[gi], U, b.fv, nullptr, nullptr, cell, v, live,
-                                     IxB{b.ubase[gi], b.fbase[gi], C, cs});
+                                     IxB{b.ubase[gi], b.fbase[gi], C, cs}, src);
     }
 }
 

@@ -501,6 +501,7 @@ void mgpu_ctx::build() {
     G.alloc((size_t)F_flux * 4);
     scal.alloc(2);
     flags.alloc(1);
+    teno.err = flags.p;
     rmax.alloc(1);
     masks.alloc((size_t)N * 4);
     staging.alloc((size_t)N * 5);
@@ -920,6 +921,10 @@ int mgpu_status(mgpu_ctx* ctx, uint32_t* flags) {
         ck(cudaMemcpyAsync(&h, ctx->flags.p, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
         ck(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
         if (flags) *flags = h;
+        if (h & 4u) {
+            set_error("a bounded device wait ran out");
+            return MGPU_ERR_TIMEOUT;
+        }
         return h ? MGPU_ERR_NAN : MGPU_OK;
     });
 }
@@ -956,8 +961,8 @@ int mgpu_kernel_times(mgpu_ctx* ctx, double* ms, uint32_t* launches) {
 int mgpu_autotune(mgpu_ctx* ctx, double* ms, int* best) {
     if (int rc = need_ready(ctx)) return rc;
     return guarded([&] {
-        const int n = ctx->single() && ctx->K == 10 ? f32::TENO32_SHAPES : 1;
-        std::vector<double> t(f32::TENO32_SHAPES, 0.0);
+        const int n = ctx->single() && ctx->K == 10 ? f32::TENO32_SHAPES_SINGLE : 1;
+        std::vector<double> t(f32::TENO32_SHAPES_SINGLE, 0.0);
         cudaEvent_t a, b;
         ck(cudaEventCreate(&a), "cudaEventCreate");
         ck(cudaEventCreate(&b), "cudaEventCreate");
@@ -996,10 +1001,25 @@ int mgpu_autotune(mgpu_ctx* ctx, double* ms, int* best) {
             ctx->step_exec = nullptr;
         }
         if (ms)
-            for (int i = 0; i < f32::TENO32_SHAPES; ++i) ms[i] = t[i];
+            for (int i = 0; i < f32::TENO32_SHAPES_SINGLE; ++i) ms[i] = t[i];
         if (best) *best = choice;
         return MGPU_OK;
     });
+}
+
+int mgpu_set_launch_shape(mgpu_ctx* ctx, int shape) {
+    if (int rc = need_ready(ctx)) return rc;
+    const int n = ctx->single() && ctx->K == 10 ? f32::TENO32_SHAPES_SINGLE : 1;
+    if (shape < 0 || shape >= n) {
+        set_error("launch shape out of range for this form");
+        return MGPU_ERR_ARG;
+    }
+    ctx->teno_shape = shape;
+    if (ctx->step_exec) {
+        cudaGraphExecDestroy(ctx->step_exec);
+        ctx->step_exec = nullptr;
+    }
+    return MGPU_OK;
 }
 
 int mgpu_traffic_model(mgpu_ctx* ctx, double* recon_bytes, double* stage_bytes) {

@@ -272,10 +272,14 @@ class Solver:
     def autotune(self):
         """Pick the fastest launch shape of the reconstruction kernel on the
         current state; returns (chosen shape, ms per shape)."""
-        ms = np.zeros(4)
+        ms = np.zeros(7)
         best = C.c_int()
         N.check(self._lib.mgpu_autotune(self._h, N.ptr(ms), C.byref(best)))
         return best.value, ms
+
+    def set_launch_shape(self, shape):
+        """Fix the reconstruction kernel's launch shape (autotune numbering)."""
+        N.check(self._lib.mgpu_set_launch_shape(self._h, int(shape)))
 
     def traffic_model(self):
         r, s = C.c_double(), C.c_double()

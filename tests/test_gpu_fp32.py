@@ -9,7 +9,8 @@ bar is 1e-3 relative L1 density error.
 import numpy as np
 import pytest
 
-from cases import four_quadrant, make_pair, perturbed, pulse, real_faces
+import mallard_gb300 as mg
+from cases import explosion, four_quadrant, make_pair, perturbed, pulse, real_faces
 from test_gpu_parity import tri_mesh
 from conftest import rel_err
 
@@ -65,3 +66,33 @@ def test_fp32_100_steps_errors():
           f"fp64 {drift64:.2e} energy diff {e_drift:.2e}")
     assert l1 < 1e-5 and linf < 1e-4
     assert drift32 < 1e-6 and e_drift < 1e-6
+
+
+@pytest.mark.parametrize("learned", [False, True])
+def test_launch_shapes_agree(learned):
+    """Every launch shape of the FP32 reconstruction (including the staged
+    kernel, which reads its tables from shared memory filled by bulk async
+    copies) gives the same bits, with and without the learned selector; a
+    mesh whose cell count is not a multiple of the 8-cell tile exercises the
+    staged kernel's idle lanes."""
+    from mallard_gb300.selector import Selector, default_weights_path
+    m = mg.Mesh.generate("cartesian_tri", 41, 39, 1.0, 1.0)
+    m.permute_cells(9)
+    assert m.n_cells % 8 != 0
+    sel = Selector()
+    sel.load(default_weights_path())
+    out = []
+    for shape in range(7):
+        s, _ = make_pair(m, variant="corrected", precision="fp32")
+        if learned:
+            s.attach_selector(sel)
+        s.set_launch_shape(shape)
+        U, W = explosion(m)
+        s.set_state(U, W)
+        s.run(0.5, 6)
+        assert s.status() == 0
+        out.append(s.get_state()[0])
+        s.close()
+    sel.close()
+    for shape in range(1, 7):
+        np.testing.assert_array_equal(out[shape], out[0], err_msg=f"shape {shape}")
