@@ -84,6 +84,8 @@ def parse():
                     help="Reynolds number of the wedge on the ramp length (viscous flux, no-slip walls); 0 = inviscid")
     ap.add_argument("--batch-cases", type=int, default=256,
                     help="cases of the batched section (configuration 4); 0 skips it")
+    ap.add_argument("--shape", type=int, default=-1,
+                    help="fix the FP32 reconstruction's launch shape (0-6) instead of autotuning it")
     ap.add_argument("--cpu-sample-n", type=int, default=CPU_SAMPLE_N)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -294,7 +296,10 @@ def time_form(m, args, form, U0, W0, device, selector, barrier=None, clocks=None
     s.set_stream(stream.cuda_stream)
     s.set_state(U0, W0)
     tune = None
-    if FORMS[form][0] == "fp32":
+    if FORMS[form][0] == "fp32" and args.shape >= 0:
+        s.set_launch_shape(args.shape)
+        tune = {"chosen_shape": args.shape, "ms_per_shape": None, "shapes": "fixed by --shape"}
+    elif FORMS[form][0] == "fp32":
         shape, tms = s.autotune()
         tune = {"chosen_shape": shape, "ms_per_shape": [round(x, 4) for x in tms],
                 "shapes": "0: 128 thr/<=128 regs, 1: 128/<=80, 2: 128/<=64, 3: 256/<=64, "
@@ -555,8 +560,10 @@ def run_ours(args):
               for k, v in kt.items() if v[1]}
     dom = max(kshare, key=lambda k: kshare[k]["share"])
     learned = FORMS[head][1]
-    kernel_names = {"recon": ("teno32_kernel<10,20,2,SEL>" if learned else
-                              ("teno32_kernel<10,20,2>" if FORMS[head][0] == "fp32" else "teno_kernel<10,20,2>")),
+    staged = bool(r["tune"]) and r["tune"]["chosen_shape"] >= 4
+    fp32_name = "teno32_staged_kernel" if staged else "teno32_kernel"
+    kernel_names = {"recon": (f"{fp32_name}<10,20,2,SEL>" if learned else
+                              (f"{fp32_name}<10,20,2>" if FORMS[head][0] == "fp32" else "teno_kernel<10,20,2>")),
                     "selector": "mlp_kernel<1> (tcgen05)", "flux": "flux kernel", "update": "update_kernel",
                     "cfl": "spectral_kernel"}
     dom_ms, dom_n = kt[dom]

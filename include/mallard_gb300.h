@@ -404,6 +404,10 @@ int mgpu_primitives_batch(double gamma, double p_ref, double T_ref, double rho_r
                           uint32_t n, const double* U, double* primitives);
 /* FP64 FMA throughput probe: returns measured GFLOP/s (2 flops per FMA). */
 int mgpu_probe_fp64_gflops(int device, double* gflops);
+/* The FP32 form's integer-pipe conversions on the device, for testing:
+ * out32[i] = in64[i] rounded to FP32 (nearest even; magnitudes below FP32's
+ * smallest normal give a signed zero), out64[i] = in32[i] exactly. */
+int mgpu_probe_conversions(int device, const double* in64, float* out32, const float* in32, double* out64, uint64_t n);
 
 const char* mgpu_last_error(void);
 int mgpu_version(void);

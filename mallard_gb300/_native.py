@@ -116,6 +116,7 @@ def lib():
         "mgpu_traffic_model": (i32, [vp, P(f64), P(f64)]),
         "mgpu_get_table": (i32, [vp, i32, vp, P(C.c_uint64)]),
         "mgpu_set_launch_shape": (i32, [vp, i32]),
+        "mgpu_probe_conversions": (i32, [i32, vp, vp, vp, vp, C.c_uint64]),
         "mgpu_build_times": (i32, [vp, vp]),
         "mgpu_autotune": (i32, [vp, vp, P(i32)]),
         "mgpu_batch_create": (i32, [u32, vp, vp, P(Config), P(vp)]),

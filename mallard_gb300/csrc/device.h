@@ -30,6 +30,7 @@ constexpr int KR_MAX = 9;  // K-1 for p = 3
 struct GasParams {
     double gamma, R, cv, p_min, p_max;
     double icv;  // 1 / cv (fast forms)
+    float gamma_f, R_f, cv_f, p_min_f, p_max_f;  // the same rounded to FP32 on the host (FP32 form)
 };
 
 struct BcEntry {
@@ -71,6 +72,7 @@ struct FluxArgs {
     double* G;
     const double* U;        // stage input, for the positivity fallback
     double qw[4];           // face quadrature weights
+    float qw_f[4];          // the same rounded to FP32 (FP32 form)
 };
 
 struct UpdateArgs {
@@ -263,5 +265,7 @@ cudaError_t launch_permute_rows(int n, int width, const uint32_t* idx, const dou
 cudaError_t launch_riemann_batch(int rsolver, uint32_t n, const double* buf_in, double* flux, cudaStream_t s);
 cudaError_t launch_primitives_batch(const GasParams& g, uint32_t n, const double* U, double* W, cudaStream_t s);
 cudaError_t run_fp64_probe(int device, double* gflops);
+// f32_rn of n doubles and f64_of of n floats (host arrays), on the device
+cudaError_t run_convert_probe(int device, const double* in64, float* out32, const float* in32, double* out64, size_t n);
 
 }  // namespace mgpu

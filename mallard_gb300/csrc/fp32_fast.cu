@@ -411,7 +411,7 @@ __device__ __forceinline__ void primitives_guarded(const GasParams& g, const flo
     primitives(g, U, W);
     const float rho = U[0];
     const float E = U[3] / rho;
-    const float e = W[3] * f(g.cv);
+    const float e = W[3] * g.cv_f;
     if (!(e > 1.0e-3f * E)) {
         const double Ud[4] = {U[0], U[1], U[2], U[3]};
         double Wd[5];
@@ -537,7 +537,7 @@ __device__ __forceinline__ void flux32_face(const FluxArgs& a, const float* __re
     const float n[2] = {f(nn.x), f(nn.y)};
     const int bi = a.bc[fi];
     const int type = bi < 0 ? -1 : bct.bc[bi].type;
-    const float gam = f(g.gamma);
+    const float gam = g.gamma_f;
     float F[4] = {0.0f, 0.0f, 0.0f, 0.0f};
 #pragma unroll
     for (int q = 0; q < NQ; ++q) {
@@ -590,8 +590,8 @@ __device__ __forceinline__ void flux32_face(const FluxArgs& a, const float* __re
                 const float sos = sqrtf(gam * pl[2] / rho_l);
                 const float po = (um < sos) ? f(bct.bc[bi].data[0]) : pl[2];
                 const float T = pl[3];
-                const float rho = po / (f(g.R) * T);
-                const float e = f(g.cv) * T;
+                const float rho = po / (g.R_f * T);
+                const float e = g.cv_f * T;
                 cr[0] = rho;
                 pr[0] = pl[0];
                 pr[1] = pl[1];
@@ -602,20 +602,21 @@ __device__ __forceinline__ void flux32_face(const FluxArgs& a, const float* __re
             riemann<RS>(Ft, n, cl[0], pl, pl[2], gam, pl[4], cr[0], pr, pr[2], gam, pr[4]);
         }
 #pragma unroll
-        for (int i = 0; i < 4; i++) F[i] = fmaf(f(a.qw[q]), Ft[i], F[i]);
+        for (int i = 0; i < 4; i++) F[i] = fmaf(a.qw_f[q], Ft[i], F[i]);
     }
     const double area = a.area[fi];
     double2* Gf = reinterpret_cast<double2*>(Gout + ix.f(fi) * 4);
+    // FP32 -> FP64 exactly on the integer pipe (f64_of), products in FP64
     if (VISC && (type < 0 || type == MGPU_BC_WALL_ADIABATIC)) {
         float Fv[4];
         visc32_face(*va, fi, lr, type == MGPU_BC_WALL_ADIABATIC, n, Fv);
-        Gf[0] = make_double2(area * (double)(F[0] * 0.5f), area * (double)(F[1] * 0.5f) - area * (double)Fv[1]);
-        Gf[1] = make_double2(area * (double)(F[2] * 0.5f) - area * (double)Fv[2],
-                             area * (double)(F[3] * 0.5f) - area * (double)Fv[3]);
+        Gf[0] = make_double2(area * f64_of(F[0] * 0.5f), area * f64_of(F[1] * 0.5f) - area * f64_of(Fv[1]));
+        Gf[1] = make_double2(area * f64_of(F[2] * 0.5f) - area * f64_of(Fv[2]),
+                             area * f64_of(F[3] * 0.5f) - area * f64_of(Fv[3]));
         return;
     }
-    Gf[0] = make_double2(area * (double)(F[0] * 0.5f), area * (double)(F[1] * 0.5f));
-    Gf[1] = make_double2(area * (double)(F[2] * 0.5f), area * (double)(F[3] * 0.5f));
+    Gf[0] = make_double2(area * f64_of(F[0] * 0.5f), area * f64_of(F[1] * 0.5f));
+    Gf[1] = make_double2(area * f64_of(F[2] * 0.5f), area * f64_of(F[3] * 0.5f));
 }
 
 template <int RS, int NQ, bool VISC>

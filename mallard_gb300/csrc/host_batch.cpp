@@ -181,7 +181,10 @@ int mgpu_batch_finalize(mgpu_batch* b) {
             fa.nrm = c->nrm.p;
             fa.area = c->area.p;
             fa.bc = c->bcidx.p;
-            for (int i = 0; i < 4; ++i) fa.qw[i] = c->qw[i];
+            for (int i = 0; i < 4; ++i) {
+                fa.qw[i] = c->qw[i];
+                fa.qw_f[i] = (float)c->qw[i];
+            }
             hf.push_back(fa);
             hu.push_back(c->update_args());
             SpecArgs sa{};

@@ -681,6 +681,11 @@ int mgpu_create(const mgpu_mesh* mesh, const mgpu_config* cfg, mgpu_ctx** out) {
         ctx->gas.p_min = cfg->p_min;
         ctx->gas.p_max = cfg->p_max;
         ctx->gas.icv = 1.0 / ctx->gas.cv;
+        ctx->gas.gamma_f = (float)ctx->gas.gamma;
+        ctx->gas.R_f = (float)ctx->gas.R;
+        ctx->gas.cv_f = (float)ctx->gas.cv;
+        ctx->gas.p_min_f = (float)ctx->gas.p_min;
+        ctx->gas.p_max_f = (float)ctx->gas.p_max;
         ck(cudaSetDevice(cfg->device), "cudaSetDevice");
         ck(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking), "cudaStreamCreate");
         ctx->own_stream = true;
@@ -1108,6 +1113,14 @@ int mgpu_primitives_batch(double gamma, double p_ref, double T_ref, double rho_r
         dw.alloc((size_t)n * 5);
         ck(launch_primitives_batch(g, n, du.p, dw.p, 0), "primitives launch");
         ck(cudaMemcpy(Wh, dw.p, (size_t)n * 5 * sizeof(double), cudaMemcpyDeviceToHost), "D2H");
+        return MGPU_OK;
+    });
+}
+
+int mgpu_probe_conversions(int device, const double* in64, float* out32, const float* in32, double* out64, uint64_t n) {
+    return guarded([&] {
+        if (n && (!in64 || !out32 || !in32 || !out64)) throw ArgFail("null argument");
+        ck(run_convert_probe(device, in64, out32, in32, out64, (size_t)n), "conversion probe");
         return MGPU_OK;
     });
 }

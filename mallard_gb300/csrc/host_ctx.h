@@ -221,7 +221,10 @@ struct mgpu_ctx {
         a.fv = fv.p;
         a.G = G.p;
         a.U = Uin;
-        for (int i = 0; i < 4; i++) a.qw[i] = qw[i];
+        for (int i = 0; i < 4; i++) {
+            a.qw[i] = qw[i];
+            a.qw_f[i] = (float)qw[i];
+        }
         const bool pos = cfg.recon == MGPU_RECON_TENO && cfg.teno_variant == MGPU_TENO_CORRECTED;
         if (single()) {
             viscous_gradients32(Uin == U.p ? U32.p : Ut32.p);

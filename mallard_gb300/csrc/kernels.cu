@@ -751,6 +751,37 @@ cudaError_t launch_primitives_batch(const GasParams& g, uint32_t n, const double
     return cudaGetLastError();
 }
 
+__global__ void convert_probe_kernel(size_t n, const double* in64, float* out32, const float* in32, double* out64) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out32[i] = f32_rn(in64[i]);
+    out64[i] = f64_of(in32[i]);
+}
+
+cudaError_t run_convert_probe(int device, const double* in64, float* out32, const float* in32, double* out64, size_t n) {
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess || n == 0) return e;
+    double *d64 = nullptr, *o64 = nullptr;
+    float *d32 = nullptr, *o32 = nullptr;
+    e = cudaMalloc(&d64, n * 8);
+    if (e == cudaSuccess) e = cudaMalloc(&o64, n * 8);
+    if (e == cudaSuccess) e = cudaMalloc(&d32, n * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&o32, n * 4);
+    if (e == cudaSuccess) e = cudaMemcpy(d64, in64, n * 8, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d32, in32, n * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        convert_probe_kernel<<<(unsigned)((n + 255) / 256), 256>>>(n, d64, o32, d32, o64);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(out32, o32, n * 4, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(out64, o64, n * 8, cudaMemcpyDeviceToHost);
+    cudaFree(d64);
+    cudaFree(o64);
+    cudaFree(d32);
+    cudaFree(o32);
+    return e;
+}
+
 cudaError_t run_fp64_probe(int device, double* gflops) {
     cudaError_t e = cudaSetDevice(device);
     if (e != cudaSuccess) return e;

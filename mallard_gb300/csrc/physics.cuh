@@ -23,17 +23,27 @@ constexpr int NPR = 5;
 // Euler physics (src/physics/physics.h:842-867)
 // ---------------------------------------------------------------------------
 
+// A gas constant in the arithmetic type: the FP64 value, or its FP32
+// rounding made once on the host (a device F2F conversion issues on the
+// FP64 unit).
+template <class T>
+__device__ __forceinline__ T cst(double d, float f);
+template <>
+__device__ __forceinline__ double cst<double>(double d, float) { return d; }
+template <>
+__device__ __forceinline__ float cst<float>(double, float f) { return f; }
+
 template <class T>
 __device__ __forceinline__ void primitives(const GasParams& g, const T* U, T* W) {
     const T rho = U[0];
     const T u0 = U[1] / rho, u1 = U[2] / rho;
     const T E = U[3] / rho;
     const T e = E - T(0.5) * (u0 * u0 + u1 * u1);
-    const T p = fmax(T(g.p_min), fmin(T(g.p_max), (T(g.gamma) - T(1.0)) * rho * e));
+    const T p = fmax(cst<T>(g.p_min, g.p_min_f), fmin(cst<T>(g.p_max, g.p_max_f), (cst<T>(g.gamma, g.gamma_f) - T(1.0)) * rho * e));
     W[0] = u0;
     W[1] = u1;
     W[2] = p;
-    W[3] = e / T(g.cv);
+    W[3] = e / cst<T>(g.cv, g.cv_f);
     W[4] = e + p / rho;
 }
 
@@ -44,7 +54,7 @@ __device__ __forceinline__ bool admissible(const GasParams& g, const T* W) {
     if (!(rho > T(0.0))) return false;
     const T u0 = W[1] / rho, u1 = W[2] / rho;
     const T e = W[3] / rho - T(0.5) * (u0 * u0 + u1 * u1);
-    return (T(g.gamma) - T(1.0)) * rho * e > T(0.0);
+    return (cst<T>(g.gamma, g.gamma_f) - T(1.0)) * rho * e > T(0.0);
 }
 
 // ---------------------------------------------------------------------------

@@ -48,6 +48,15 @@ constexpr int THREADS = ROWS * NV;            // one thread per (cell, variable)
 static_assert(BLOB % 16 == 0 && SM_ACT % 128 == 0, "alignment");
 static_assert(BLOB == WEIGHT_IMAGE_BYTES, "weight image size");
 
+// GELU of the inference epilogue with the hardware tanh (tanh.approx.f32,
+// relative error about 2^-11): its output is rounded to BF16 (2^-8) next.
+__device__ __forceinline__ float gelu_approx(float x) {
+    const float c = 0.7978845608028654f;  // sqrt(2 / pi)
+    float t;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(c * (x + 0.044715f * x * x * x)));
+    return 0.5f * x * (1.0f + t);
+}
+
 __device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
 __device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
@@ -239,7 +248,7 @@ __global__ void __launch_bounds__(THREADS, 2) mlp_kernel(const uint8_t* __restri
             // the MMAs that read act have completed: overwrite it with this layer's output
             tmem_ld16(tl, out);
 #pragma unroll
-            for (int i = 0; i < 16; ++i) out[i] = gelu(out[i] + b[cgrp * 16 + i]);
+            for (int i = 0; i < 16; ++i) out[i] = gelu_approx(out[i] + b[cgrp * 16 + i]);
             *reinterpret_cast<uint4*>(act + chunk_off(erow, cgrp * 16, HID)) = pack8(out);
             *reinterpret_cast<uint4*>(act + chunk_off(erow, cgrp * 16 + 8, HID)) = pack8(out + 8);
             fence_async_smem();

@@ -76,3 +76,44 @@ def test_primitives_random_bit_identical():
 def test_fp64_probe_runs():
     g = mg.fp64_peak_gflops()
     assert g > 10.0
+
+
+def test_integer_pipe_conversions():
+    """f32_rn (FP64 -> FP32, nearest even, flush below FP32's normal range)
+    and f64_of (FP32 -> FP64, exact) against numpy, over random magnitudes,
+    rounding ties, subnormals, signed zeros, infinities and NaN."""
+    import ctypes as C
+    from mallard_gb300 import _native as N
+    r = np.random.default_rng(11)
+    x = np.concatenate([
+        r.standard_normal(20000) * 10.0 ** r.uniform(-40, 40, 20000),
+        r.uniform(-1, 1, 5000),
+        # exact ties and neighbours of ties between two floats
+        (np.float32(r.uniform(1, 2, 2000)).astype(np.float64) + np.float64(2.0 ** -24)),
+        (np.float32(r.uniform(1, 2, 2000)).astype(np.float64) + np.float64(2.0 ** -24) * (1 + 2.0 ** -20)),
+        [0.0, -0.0, np.inf, -np.inf, np.nan, 3.5e38, -3.5e38, 3.4028235677973366e38, 1.1754943508222875e-38,
+         1.17549435e-38 * 0.5, 1e-300, -1e-300, 5e-324],
+    ]).astype(np.float64)
+    f = np.concatenate([
+        r.standard_normal(20000).astype(np.float32) * np.float32(10.0) ** r.uniform(-37, 37, 20000).astype(np.float32),
+        (r.integers(1, 1 << 23, 3000).astype(np.uint32)).view(np.float32),  # subnormals
+        np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 1.4e-45, -1.4e-45, 3.4028235e38], dtype=np.float32),
+    ]).astype(np.float32)
+    n = max(len(x), len(f))
+    x = np.resize(x, n)
+    f = np.resize(f, n)
+    o32 = np.zeros(n, dtype=np.float32)
+    o64 = np.zeros(n, dtype=np.float64)
+    lib = N.lib()
+    N.check(lib.mgpu_probe_conversions(0, N.ptr(x), N.ptr(o32), N.ptr(f), N.ptr(o64), C.c_uint64(n)))
+    with np.errstate(over="ignore"):
+        ref32 = x.astype(np.float32)
+    tiny = np.abs(x) < np.float64(np.finfo(np.float32).tiny)
+    ref32[tiny] = np.copysign(np.float32(0.0), x[tiny]).astype(np.float32)
+    nan = np.isnan(x)
+    assert np.isnan(o32[nan]).all()
+    np.testing.assert_array_equal(o32[~nan].view(np.uint32), ref32[~nan].view(np.uint32))
+    ref64 = f.astype(np.float64)
+    fn = np.isnan(f)
+    assert np.isnan(o64[fn]).all()
+    np.testing.assert_array_equal(o64[~fn].view(np.uint64), ref64[~fn].view(np.uint64))
