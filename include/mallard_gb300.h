@@ -140,6 +140,24 @@ int mgpu_mesh_from_connectivity(uint32_t n_nodes, const double* node_coords, uin
 int mgpu_mesh_permute_cells(mgpu_mesh_buf* m, uint64_t seed, uint32_t* new_of_old);
 int mgpu_mesh_view(const mgpu_mesh_buf* m, mgpu_mesh* view);
 void mgpu_mesh_free(mgpu_mesh_buf* m);
+/* Mesh ingest (the reference's "file" mesh type, src/mesh/mesh.cpp:41-43,
+ * whose default filename is mesh.msh and which the reference leaves
+ * unimplemented).  Gmsh ASCII MSH 2.2 or 4.1, 2-D: triangles and
+ * quadrilaterals are the cells (file order), line elements name the boundary
+ * zones by physical group (else by curve).  Faces: one per distinct cell edge,
+ * numbered in order of first appearance; zone 0 "interior", then the
+ * boundary zones in order of first appearance, then "boundary" for boundary
+ * faces no line element names. */
+int mgpu_mesh_read_gmsh(const char* path, mgpu_mesh_buf** out);
+/* The library's binary mesh format (connectivity, zones and zone names;
+ * geometry is derived again on reading, so a round trip gives equal bits). */
+int mgpu_mesh_write(const mgpu_mesh_buf* m, const char* path);
+int mgpu_mesh_read(const char* path, mgpu_mesh_buf** out);
+/* Zone names: generated meshes name theirs (interior, right, top, left,
+ * bottom; the ramp channel interior, inflow, outflow, wall, top), read meshes
+ * take the file's, others zone<i>. */
+int mgpu_mesh_zone_name(const mgpu_mesh_buf* m, uint32_t zone, char* name, uint32_t len);
+int mgpu_mesh_set_zone_name(mgpu_mesh_buf* m, uint32_t zone, const char* name);
 
 /* ---- TENO tables (host) ----------------------------------------------- */
 /* The tables TENO::init builds (face_reconstruction.cpp:109-788), in the

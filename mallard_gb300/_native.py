@@ -116,6 +116,11 @@ def lib():
         "mgpu_traffic_model": (i32, [vp, P(f64), P(f64)]),
         "mgpu_get_table": (i32, [vp, i32, vp, P(C.c_uint64)]),
         "mgpu_set_launch_shape": (i32, [vp, i32]),
+        "mgpu_mesh_read_gmsh": (i32, [C.c_char_p, P(vp)]),
+        "mgpu_mesh_read": (i32, [C.c_char_p, P(vp)]),
+        "mgpu_mesh_write": (i32, [vp, C.c_char_p]),
+        "mgpu_mesh_zone_name": (i32, [vp, u32, C.c_char_p, u32]),
+        "mgpu_mesh_set_zone_name": (i32, [vp, u32, C.c_char_p]),
         "mgpu_probe_conversions": (i32, [i32, vp, vp, vp, vp, C.c_uint64]),
         "mgpu_build_times": (i32, [vp, vp]),
         "mgpu_autotune": (i32, [vp, vp, P(i32)]),

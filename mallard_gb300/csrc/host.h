@@ -103,4 +103,19 @@ void set_error(const std::string& msg);
 
 struct mgpu_mesh_buf {
     mgpu::HostMesh m;
+    std::vector<std::string> zone_names;  // [n_zones]; zone 0 "interior"
 };
+
+namespace mgpu {
+// Names of the zones of a buffer without names of its own: the generators'
+// (right, top, left, bottom), else zone<i>.
+void default_zone_names(mgpu_mesh_buf& b);
+// Faces, cells_of_face and zones of a mesh given by its nodes and cells
+// (host_mesh_io.cpp): one face per distinct cell edge, numbered in order of
+// first appearance (cells in order, edges k -> k+1), nodes as in the cell
+// that meets it first, which is its side-0 cell.  Boundary faces go to the
+// zone of the boundary edge listed with the same two nodes (edge_zone,
+// 1-based into names), else to a zone "boundary".
+void build_faces(mgpu_mesh_buf& b, const std::vector<std::pair<uint64_t, uint32_t>>& edge_zone,
+                 const std::vector<std::string>& names);
+}  // namespace mgpu

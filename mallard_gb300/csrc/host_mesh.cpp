@@ -478,6 +478,7 @@ int mgpu_mesh_generate_ramp(uint32_t nx, uint32_t ny, double Lx, double Ly, doub
             delete b;
             throw;
         }
+        b->zone_names = {"interior", "inflow", "outflow", "wall", "top"};
         *out = b;
         return MGPU_OK;
     } catch (const std::exception& e) {
@@ -501,6 +502,7 @@ int mgpu_mesh_generate(int mesh_type, uint32_t nx, uint32_t ny, double Lx, doubl
             mgpu::set_error("Unknown mesh type.");
             return MGPU_ERR_ARG;
         }
+        mgpu::default_zone_names(*b);
         *out = b;
         return MGPU_OK;
     } catch (const std::exception& e) {
@@ -547,6 +549,7 @@ int mgpu_mesh_from_connectivity(uint32_t n_nodes, const double* node_coords, uin
             if (m.cof[i] >= (int32_t)n_cells || (m.cof[i] < 0 && (i % 2 == 0 || m.cof[i] != -1)))
                 throw std::runtime_error("mesh: cells_of_face out of range");
         mgpu::derive_geometry(m);
+        mgpu::default_zone_names(*b);
         *out = b;
         return MGPU_OK;
     } catch (const std::exception& e) {

@@ -32,8 +32,16 @@ class Mesh:
         v = N.MeshView()
         N.check(self._lib.mgpu_mesh_view(self._h, C.byref(v)))
         self._load(v)
-        self.zone_names = list(zone_names) if zone_names else (
-            GENERATED_ZONES if self.n_zones == 5 else ["interior"] + [f"zone{i}" for i in range(1, self.n_zones)])
+        if zone_names:
+            self.zone_names = list(zone_names)
+            for i, name in enumerate(self.zone_names):
+                N.check(self._lib.mgpu_mesh_set_zone_name(self._h, i, name.encode()))
+        else:
+            buf = C.create_string_buffer(4096)
+            self.zone_names = []
+            for i in range(self.n_zones):
+                N.check(self._lib.mgpu_mesh_zone_name(self._h, i, buf, len(buf)))
+                self.zone_names.append(buf.value.decode())
 
     def _load(self, v):
         self.n_nodes, self.n_cells, self.n_faces, self.n_zones = v.n_nodes, v.n_cells, v.n_faces, v.n_zones
@@ -72,7 +80,7 @@ class Mesh:
         h = C.c_void_p()
         N.check(N.lib().mgpu_mesh_generate_ramp(nx, ny, float(Lx), float(Ly), float(x0), float(ramp_deg),
                                                 float(jitter), int(seed), C.byref(h)))
-        return cls(h, ["interior", "inflow", "outflow", "wall", "top"])
+        return cls(h)
 
     @classmethod
     def from_connectivity(cls, node_coords, offsets_nodes_of_cell, nodes_of_cell, offsets_faces_of_cell,
@@ -90,6 +98,33 @@ class Mesh:
             len(a[5]) - 1, N.ptr(a[5]), N.ptr(a[6]), N.ptr(a[7]), len(a[8]) - 1, N.ptr(a[8]), N.ptr(a[9]),
             C.byref(h)))
         return cls(h, zone_names)
+
+    @classmethod
+    def read_gmsh(cls, path):
+        """A 2-D Gmsh mesh (ASCII MSH 2.2 or 4.1): triangles and quadrilaterals
+        as cells, boundary zones named by the physical groups of the line
+        elements (the reference's unimplemented "file" mesh type)."""
+        h = C.c_void_p()
+        N.check(N.lib().mgpu_mesh_read_gmsh(str(path).encode(), C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def read(cls, path):
+        """A mesh in the library's binary format (Mesh.write)."""
+        h = C.c_void_p()
+        N.check(N.lib().mgpu_mesh_read(str(path).encode(), C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def read_file(cls, path):
+        """Gmsh (.msh) or the library's binary format, by the file's first bytes."""
+        with open(path, "rb") as f:
+            head = f.read(8)
+        return cls.read(path) if head == b"MGPUMSH1" else cls.read_gmsh(path)
+
+    def write(self, path):
+        """Save in the library's binary format (connectivity, zones, names)."""
+        N.check(self._lib.mgpu_mesh_write(self._h, str(path).encode()))
 
     def permute_cells(self, seed):
         """Relabel cells with a seeded random permutation; returns new_of_old."""

@@ -324,8 +324,16 @@ class Solver:
         m = inp.get("mesh", {})
         mtype = m.get("type", "file")
         if mtype == "file":
-            raise RuntimeError("MeshType::FILE not implemented.")
-        mesh = Mesh.generate(mtype, m.get("Nx", 100), m.get("Ny", 100), m.get("Lx", 1.0), m.get("Ly", 1.0))
+            # the reference's [mesh] filename key and default (mesh.cpp:41-43);
+            # relative to the input file when one was given
+            fname = m.get("filename", "mesh.msh")
+            import os
+            if not os.path.isabs(fname) and isinstance(source, (str, os.PathLike)) and "\n" not in str(source) \
+                    and os.path.exists(str(source)):
+                fname = os.path.join(os.path.dirname(os.path.abspath(str(source))), fname)
+            mesh = Mesh.read_file(fname)
+        else:
+            mesh = Mesh.generate(mtype, m.get("Nx", 100), m.get("Ny", 100), m.get("Lx", 1.0), m.get("Ly", 1.0))
         phys = inp["physics"]
         for key in ("gamma", "p_ref", "T_ref", "rho_ref"):
             if key not in phys:
