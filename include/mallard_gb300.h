@@ -420,6 +420,29 @@ int mgpu_riemann_flux_batch(int solver, uint32_t n, const double* n_unit, const 
 /* Euler primitive recovery for n states on the GPU. */
 int mgpu_primitives_batch(double gamma, double p_ref, double T_ref, double rho_ref, double p_min, double p_max,
                           uint32_t n, const double* U, double* primitives);
+/* ---- output ------------------------------------------------------------- */
+/* VTU output of the solution in the reference's format (DataWriter::write_vtu,
+ * src/io/data_writer.cpp:93-244: VTK XML UnstructuredGrid, raw appended
+ * data, Float64 cell arrays, files <prefix>_<step, 6 digits>.vtu), written
+ * asynchronously.  variables: comma-separated [[write_data]] names among RHO,
+ * RHOU_X, RHOU_Y, RHOE, U_X, U_Y, P, T, H, CFL (CFL = dt x the spectral radius
+ * of the last time step).  mgpu_writer_write writes when step % interval ==
+ * 0 or force: it snapshots the arrays on the device (ordered after the work
+ * queued on the context's stream, which waits for the snapshot only) and
+ * returns; a copy stream and a worker thread copy them to pinned memory and
+ * write the file while the solver goes on.  mgpu_writer_flush waits for every
+ * queued file and reports the first I/O error; destroy flushes. */
+typedef struct mgpu_writer mgpu_writer;
+int mgpu_writer_create(mgpu_ctx* ctx, const char* prefix, const char* variables, uint32_t interval,
+                       mgpu_writer** out);
+int mgpu_writer_write(mgpu_writer* w, uint32_t step, int force);
+int mgpu_writer_flush(mgpu_writer* w);
+void mgpu_writer_destroy(mgpu_writer* w);
+/* The same file format from host arrays: data [n_vars][n_cells] in the
+ * mesh's cell order (host only). */
+int mgpu_vtu_write(const mgpu_mesh_buf* mesh, const char* path, uint32_t n_vars, const char* const* names,
+                   const double* data);
+
 /* FP64 FMA throughput probe: returns measured GFLOP/s (2 flops per FMA). */
 int mgpu_probe_fp64_gflops(int device, double* gflops);
 /* The FP32 form's integer-pipe conversions on the device, for testing:

@@ -7,6 +7,7 @@ with primitive recovery and the CFL reduction, behind a C ABI
 
 from ._native import MgpuError, lib  # noqa: F401
 from .mesh import Mesh, teno_tables  # noqa: F401
+from .output import VtuWriter, read_vtu, write_vtu  # noqa: F401
 from .solver import (Solver, fp64_peak_gflops, gas_constants, initial_state, primitives,  # noqa: F401
                      riemann_flux, state_from_primitives)
 

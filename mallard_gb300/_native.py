@@ -117,6 +117,11 @@ def lib():
         "mgpu_get_table": (i32, [vp, i32, vp, P(C.c_uint64)]),
         "mgpu_set_launch_shape": (i32, [vp, i32]),
         "mgpu_mesh_read_gmsh": (i32, [C.c_char_p, P(vp)]),
+        "mgpu_writer_create": (i32, [vp, C.c_char_p, C.c_char_p, u32, P(vp)]),
+        "mgpu_writer_write": (i32, [vp, u32, i32]),
+        "mgpu_writer_flush": (i32, [vp]),
+        "mgpu_writer_destroy": (None, [vp]),
+        "mgpu_vtu_write": (i32, [vp, C.c_char_p, u32, vp, vp]),
         "mgpu_mesh_read": (i32, [C.c_char_p, P(vp)]),
         "mgpu_mesh_write": (i32, [vp, C.c_char_p]),
         "mgpu_mesh_zone_name": (i32, [vp, u32, C.c_char_p, u32]),

@@ -262,6 +262,9 @@ cudaError_t launch_dt(const unsigned long long* rmax_bits, double cfl, double* d
 cudaError_t launch_set_scalar(double* dst, double value, cudaStream_t s);
 cudaError_t launch_permute_rows(int n, int width, const uint32_t* idx, const double* src, double* dst, bool scatter,
                                 cudaStream_t s);
+// dst[idx[c]] = src[c * stride] for c < n
+cudaError_t launch_permute_column(int n, int stride, const uint32_t* idx, const double* src, double* dst,
+                                  cudaStream_t s);
 cudaError_t launch_riemann_batch(int rsolver, uint32_t n, const double* buf_in, double* flux, cudaStream_t s);
 cudaError_t launch_primitives_batch(const GasParams& g, uint32_t n, const double* U, double* W, cudaStream_t s);
 cudaError_t run_fp64_probe(int device, double* gflops);

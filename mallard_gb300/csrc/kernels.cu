@@ -564,6 +564,15 @@ __global__ void permute_rows_kernel(int n, int width, const uint32_t* __restrict
     else dst[(size_t)c * width + k] = src[o * width + k];
 }
 
+// One column of a row-major array, scattered to caller order: dst[idx[c]] =
+// src[c * stride] (the output writer's snapshot).
+__global__ void permute_column_kernel(int n, int stride, const uint32_t* __restrict__ idx,
+                                      const double* __restrict__ src, double* __restrict__ dst) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    dst[idx[c]] = src[(size_t)c * stride];
+}
+
 // ---------------------------------------------------------------------------
 // Unit-level kernels
 // ---------------------------------------------------------------------------
@@ -729,6 +738,13 @@ cudaError_t launch_permute_rows(int n, int width, const uint32_t* idx, const dou
     const unsigned blocks = (unsigned)((threads + 255) / 256);
     if (blocks == 0) return cudaSuccess;
     permute_rows_kernel<<<blocks, 256, 0, s>>>(n, width, idx, src, dst, scatter ? 1 : 0);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_permute_column(int n, int stride, const uint32_t* idx, const double* src, double* dst,
+                                  cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    permute_column_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, stride, idx, src, dst);
     return cudaGetLastError();
 }
 

@@ -162,6 +162,10 @@ class Solver:
                                             int(data.size)))
 
     def close(self):
+        # output writers snapshot this context: finish and release them first
+        for w in getattr(self, "_writers", []):
+            w.close()
+        self._writers = []
         h = getattr(self, "_h", None)
         if h:
             self._lib.mgpu_destroy(h)
@@ -357,6 +361,18 @@ class Solver:
             bnds.append({k: b[k] for k in ("name", "type", "u", "p", "T") if k in b})
         solver = cls(mesh, boundaries=bnds, teno_variant=teno_variant, reorder=reorder, device=device, **kw)
         U0, W0 = initial_state(mesh, inp.get("initialize", {}), solver.gas)
+        # [[write_data]] (DataWriter::init, data_writer.cpp:29-75): VTU writers in solver.writers
+        from .output import VtuWriter
+        solver.writers = []
+        for wd in inp.get("write_data", []):
+            for key in ("prefix", "format", "interval", "variables"):
+                if key not in wd:
+                    raise RuntimeError(f"DataWriter: {key} not specified.")
+            if wd["format"] == "tecplot":
+                raise RuntimeError("DataWriter::write_tecplot not implemented.")
+            if wd["format"] != "vtu":
+                raise RuntimeError(f"DataWriter: Unknown format type: {wd['format']}.")
+            solver.writers.append(VtuWriter(solver, wd["prefix"], wd["variables"], wd["interval"]))
         return solver, U0, W0, inp.get("run", {})
 
 

@@ -230,5 +230,5 @@ def test_solver_from_toml_with_a_file_mesh(tmp_path):
     solver.run(0.5, 10)
     U, _ = solver.get_state()
     assert solver.status() == 0
-    np.testing.assert_allclose(U, U0, rtol=1e-12)
+    np.testing.assert_allclose(U, U0, rtol=1e-12, atol=1e-12 * np.abs(U0).max())
     solver.close()
