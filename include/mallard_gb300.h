@@ -357,13 +357,19 @@ int mgpu_batch_synchronize(mgpu_batch* b);
  * to the batch's own stream. */
 int mgpu_batch_set_stream(mgpu_batch* b, void* stream);
 /* Per case (global order: group 0's cases first): status flags (bit 0
- * non-finite state, bit 1 invalid dt) and time; either may be NULL. */
+ * non-finite state, bit 1 invalid dt, bit 2 a bounded device wait ran out)
+ * and time; either may be NULL. */
 int mgpu_batch_status(mgpu_batch* b, uint32_t* flags, double* times);
-/* Autotuner of the batched reconstruction: times the 4 launch shapes x 4
- * grid sizes (one thread per item, or a persistent grid of 2, 4, 8 CTAs per
- * SM) on the current states and keeps the fastest.  ms[16] receives the
- * times (shape-major); any output may be NULL. */
+/* Autotuner of the batched reconstruction: times the direct kernel's 4
+ * launch shapes x 4 grid sizes (one thread per item, or a persistent grid of
+ * 2, 4, 8 CTAs per SM) and the staged kernel's 3 shapes (4-6, as
+ * mgpu_autotune numbers them; one warp per item) on the current states and
+ * keeps the fastest.  ms[28] receives the times (shape-major, 4 per shape, 0
+ * where not applicable); any output may be NULL. */
 int mgpu_batch_autotune(mgpu_batch* b, double* ms, int* shape, int* blocks_per_sm);
+/* Fix the batched reconstruction's launch shape (0-6) and grid (CTAs per
+ * SM, 0 = one thread per item; the staged shapes ignore it). */
+int mgpu_batch_set_launch_shape(mgpu_batch* b, int shape, int blocks_per_sm);
 
 /* Diagnostics for measurement.  Kernel timing brackets every launch of the
  * reconstruction, flux, update, CFL and selector kernels with CUDA events on

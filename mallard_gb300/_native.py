@@ -116,6 +116,7 @@ def lib():
         "mgpu_traffic_model": (i32, [vp, P(f64), P(f64)]),
         "mgpu_get_table": (i32, [vp, i32, vp, P(C.c_uint64)]),
         "mgpu_set_launch_shape": (i32, [vp, i32]),
+        "mgpu_batch_set_launch_shape": (i32, [vp, i32, i32]),
         "mgpu_mesh_read_gmsh": (i32, [C.c_char_p, P(vp)]),
         "mgpu_writer_create": (i32, [vp, C.c_char_p, C.c_char_p, u32, P(vp)]),
         "mgpu_writer_write": (i32, [vp, u32, i32]),

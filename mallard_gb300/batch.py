@@ -103,9 +103,14 @@ class Batch:
         N.check(self._lib.mgpu_batch_status(self._h, N.ptr(f), N.ptr(t)))
         return f, t
 
+    def set_launch_shape(self, shape, blocks_per_sm=0):
+        """Fix the batched reconstruction's launch shape (autotune numbering)."""
+        N.check(self._lib.mgpu_batch_set_launch_shape(self._h, int(shape), int(blocks_per_sm)))
+
     def autotune(self):
-        """(shape, CTAs per SM or 0, ms[4][4]) of the batched reconstruction."""
-        ms = np.zeros(16)
+        """(shape, CTAs per SM or 0, ms[7][4]) of the batched reconstruction
+        (shapes 4-6, the staged kernel, have one grid: ms[s][0])."""
+        ms = np.zeros(28)
         sh, bps = C.c_int(), C.c_int()
         N.check(self._lib.mgpu_batch_autotune(self._h, N.ptr(ms), C.byref(sh), C.byref(bps)))
-        return sh.value, bps.value, ms.reshape(4, 4)
+        return sh.value, bps.value, ms.reshape(7, 4)

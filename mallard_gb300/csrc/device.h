@@ -182,11 +182,9 @@ MGPU_DECLARE_TENO_FLUX
 namespace f32 {
 // shape: launch shape 0..3 (128-thread blocks with at most 128, 80 or 64
 // registers, or 256-thread blocks with 64; p = 3 only, other orders use
-// shape 0), chosen by the autotuner; the single-case launchers also take
-// shapes 4 to 6, the staged form that copies each tile's table blocks into
-// shared memory with cp.async.bulk
-constexpr int TENO32_SHAPES = 4;
-constexpr int TENO32_SHAPES_SINGLE = 7;
+// shape 0) or 4..6, the staged form that copies each tile's table blocks
+// into shared memory with cp.async.bulk; chosen by the autotuner
+constexpr int TENO32_SHAPES = 7;
 // U: the FP32 copy of the stage state
 cudaError_t launch_teno(const TenoArgs& a, int K, int M, int nq, const float* U, float* fv, uint8_t* masks,
                         int shape, cudaStream_t s);

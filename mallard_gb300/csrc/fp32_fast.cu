@@ -741,6 +741,62 @@ __global__ void __launch_bounds__(128) flux32_batch_kernel(const BatchLaunch b, 
     }
 }
 
+// Batched reconstruction, staged (teno32_staged_kernel's scheme): one warp
+// per (group, mesh tile, case); the C cases of a mesh tile are consecutive
+// warps, so their bulk copies of the tile's table blocks come from L2 after
+// the first.  A case that is frozen skips the warp; a wait that runs out
+// sets bit 2 of the case's flags (which then freezes it).
+template <int K, int M, int NQ, int NSLOT, int WARPS, int MINB>
+__global__ void __launch_bounds__(WARPS * 32, MINB) teno32_batch_staged_kernel(const BatchLaunch b,
+                                                                               const float* __restrict__ U) {
+    using L = StageLayout<K, M, NQ, NSLOT>;
+    using B = TileBlocks<K, M, NQ>;
+    extern __shared__ __align__(128) uint8_t stage_smem[];
+    const int w = threadIdx.x >> 5, lane32 = threadIdx.x & 31;
+    const long long gt = ((long long)blockIdx.x * WARPS + w) * 32;  // the warp's first item
+    if (gt >= b.teno0[b.n_groups]) return;
+    const int gi = batch_group(b.teno0, b.n_groups, gt);
+    const unsigned tc = (unsigned)(gt - b.teno0[gi]) >> 5, C = b.C[gi], cs = tc % C;
+    const int tile = (int)(tc / C);
+    const unsigned gc = b.case0[gi] + cs;
+    if (b.flags[gc] != 0u) return;
+    const TenoArgs& a = b.teno[gi];
+    StageSrc<K, M, NQ, NSLOT> src{a, stage_smem + (size_t)w * L::WARP, tile, lane32};
+    if (lane32 == 0) {
+        for (int i = 0; i <= NSLOT; ++i) mbar_init(src.bar(i), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        mbar_expect_tx(src.bar(NSLOT), B::FB);
+        bulk_g2s(src.base + L::PHI, reinterpret_cast<const char*>(a.phi4) + (size_t)tile * B::FB, B::FB, src.bar(NSLOT));
+    }
+    __syncwarp();
+    const int cell = tile * 8 + (lane32 >> 2), v = lane32 & 3;
+    teno32_cell<K, M, NQ, false>(a, U, b.fv, nullptr, nullptr, cell, v, 0xffffffffu,
+                                 IxB{b.ubase[gi], b.fbase[gi], C, cs}, src, cell < b.n_cells[gi]);
+    if (!src.ok) {
+        if (lane32 == 0) atomicOr(b.flags + gc, 4u);
+        for (int i = 0; i <= NSLOT; ++i) {
+            const int uses = i == NSLOT ? 1 : (i < src.issued ? (src.issued - i + NSLOT - 1) / NSLOT : 0);
+            if (uses > 0) mbar_wait(src.bar(i), (unsigned)(uses - 1) & 1u);
+        }
+    }
+}
+
+template <int K, int M, int NQ, int NSLOT, int WARPS, int MINB>
+cudaError_t teno_batch_staged(const BatchLaunch& b, const float* U, cudaStream_t s) {
+    constexpr unsigned smem = WARPS * StageLayout<K, M, NQ, NSLOT>::WARP;
+    static bool attr = false;
+    if (!attr) {
+        const cudaError_t e = cudaFuncSetAttribute(teno32_batch_staged_kernel<K, M, NQ, NSLOT, WARPS, MINB>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    const long long warps = b.teno0[b.n_groups] / 32;
+    const long long blocks = (warps + WARPS - 1) / WARPS;
+    if (blocks > 0) teno32_batch_staged_kernel<K, M, NQ, NSLOT, WARPS, MINB><<<(unsigned)blocks, WARPS * 32, smem, s>>>(b, U);
+    return cudaGetLastError();
+}
+
 template <int K, int M, int NQ, int BS, int MINB>
 cudaError_t teno_batch_go(const BatchLaunch& b, const float* U, int blocks_per_sm, cudaStream_t s) {
     int dev = 0, sms = 0;
@@ -761,6 +817,9 @@ cudaError_t launch_teno_batch(const BatchLaunch& b, const float* U, int shape, i
         case 1: return teno_batch_go<10, 20, 2, 128, 6>(b, U, blocks_per_sm, s);
         case 2: return teno_batch_go<10, 20, 2, 128, 8>(b, U, blocks_per_sm, s);
         case 3: return teno_batch_go<10, 20, 2, 256, 4>(b, U, blocks_per_sm, s);
+        case 4: return teno_batch_staged<10, 20, 2, 1, 4, 6>(b, U, s);
+        case 5: return teno_batch_staged<10, 20, 2, 2, 2, 7>(b, U, s);
+        case 6: return teno_batch_staged<10, 20, 2, 1, 4, 4>(b, U, s);
     }
     return cudaErrorInvalidValue;
 }

@@ -966,8 +966,8 @@ int mgpu_kernel_times(mgpu_ctx* ctx, double* ms, uint32_t* launches) {
 int mgpu_autotune(mgpu_ctx* ctx, double* ms, int* best) {
     if (int rc = need_ready(ctx)) return rc;
     return guarded([&] {
-        const int n = ctx->single() && ctx->K == 10 ? f32::TENO32_SHAPES_SINGLE : 1;
-        std::vector<double> t(f32::TENO32_SHAPES_SINGLE, 0.0);
+        const int n = ctx->single() && ctx->K == 10 ? f32::TENO32_SHAPES : 1;
+        std::vector<double> t(f32::TENO32_SHAPES, 0.0);
         cudaEvent_t a, b;
         ck(cudaEventCreate(&a), "cudaEventCreate");
         ck(cudaEventCreate(&b), "cudaEventCreate");
@@ -1006,7 +1006,7 @@ int mgpu_autotune(mgpu_ctx* ctx, double* ms, int* best) {
             ctx->step_exec = nullptr;
         }
         if (ms)
-            for (int i = 0; i < f32::TENO32_SHAPES_SINGLE; ++i) ms[i] = t[i];
+            for (int i = 0; i < f32::TENO32_SHAPES; ++i) ms[i] = t[i];
         if (best) *best = choice;
         return MGPU_OK;
     });
@@ -1014,7 +1014,7 @@ int mgpu_autotune(mgpu_ctx* ctx, double* ms, int* best) {
 
 int mgpu_set_launch_shape(mgpu_ctx* ctx, int shape) {
     if (int rc = need_ready(ctx)) return rc;
-    const int n = ctx->single() && ctx->K == 10 ? f32::TENO32_SHAPES_SINGLE : 1;
+    const int n = ctx->single() && ctx->K == 10 ? f32::TENO32_SHAPES : 1;
     if (shape < 0 || shape >= n) {
         set_error("launch shape out of range for this form");
         return MGPU_ERR_ARG;

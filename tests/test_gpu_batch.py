@@ -41,10 +41,14 @@ def _single(m, U, W, steps):
     return Ug, t
 
 
-def test_batch_matches_single_case_runs():
+@pytest.mark.parametrize("shape", [0, 4, 5])
+def test_batch_matches_single_case_runs(shape):
+    """Every case of a batch over two meshes against its own single-case run
+    (direct shape 0, staged shapes 4 and 5)."""
     meshes, states = _cases()
     steps = 25
     with Batch(meshes, [3, 2], boundaries=BCS, **GAS) as b:
+        b.set_launch_shape(shape)
         assert b.n_cases == 5
         for g, k, U, W in states:
             b.set_state(g, k, U, W)
@@ -74,8 +78,8 @@ def test_batch_autotune_and_independent_time_steps():
         for g, k, U, W in states:
             b.set_state(g, k, U, W)
         sh, bps, ms = b.autotune()
-        assert 0 <= sh < 4 and bps in (0, 2, 4, 8)
-        assert np.all(ms > 0)
+        assert 0 <= sh < 7 and bps in (0, 2, 4, 8)
+        assert np.all(ms[:4] > 0) and np.all(ms[4:, 0] > 0) and np.all(ms[4:, 1:] == 0)
         for g, k, U, W in states:
             b.set_state(g, k, U, W)
         b.run(0.5, 5)
