@@ -481,24 +481,11 @@ def run_ours(args):
     import mallard_gb300 as mg
     from cases import four_quadrant
 
-    rank, local, world = dist_env()
-    torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from mallard_gb300.replicas import Replicas
 
-    def barrier():
-        if dist:
-            dist.barrier()
-        torch.cuda.synchronize()
-
-    def max_over_ranks(x):
-        if not dist:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    reps = Replicas("nccl")
+    rank, local, world = reps.rank, reps.local, reps.world
+    barrier, max_over_ranks = reps.barrier, reps.max
 
     t_setup = time.perf_counter()
     m = case_mesh(args.n)
@@ -648,8 +635,7 @@ def run_ours(args):
         if batched:
             line["batched"] = batched
         print(json.dumps(line), flush=True)
-    if dist:
-        dist.destroy_process_group()
+    reps.close()
 
 
 def main():
