@@ -328,6 +328,10 @@ int mgpu_set_selector_every_stage(mgpu_ctx* ctx, int every_stage);
  * [1] cells with every variable confident, [2] confident variables,
  * [3] stencils evaluated, [4] stencils full TENO evaluates, [5] error flag. */
 int mgpu_selector_stats(mgpu_ctx* ctx, uint64_t* counts);
+/* The selector's last predictions per cell and variable, caller order
+ * [n_cells][4]: predicted TENO mask | 0x80 when confident; raw = 1 before
+ * the neighbour check, 0 after it (what the reconstruction used). */
+int mgpu_selector_predictions(mgpu_ctx* ctx, int raw, uint8_t* out);
 
 /* ---- batched form -------------------------------------------------------
  * No counterpart in the reference.  Many independent cases on a few meshes

@@ -160,6 +160,7 @@ def lib():
         "mgpu_selector_infer": (i32, [vp, vp, u32, C.c_float, C.c_float, vp, vp]),
         "mgpu_set_selector": (i32, [vp, vp, C.c_float, C.c_float]),
         "mgpu_selector_stats": (i32, [vp, vp]),
+        "mgpu_selector_predictions": (i32, [vp, i32, vp]),
         "mgpu_set_selector_every_stage": (i32, [vp, i32]),
     }
     for name, (res, args) in sig.items():

@@ -493,6 +493,21 @@ int mgpu_set_selector_every_stage(mgpu_ctx* ctx, int every_stage) {
     });
 }
 
+int mgpu_selector_predictions(mgpu_ctx* ctx, int raw, uint8_t* out) {
+    if (int rc = need_ready(ctx)) return rc;
+    return guarded([&] {
+        if (!out) throw ArgFail("null argument");
+        if (!ctx->pred.p) throw ArgFail("no selector attached");
+        std::vector<uint8_t> pr((size_t)ctx->N * 4);
+        ck(cudaMemcpyAsync(pr.data(), raw ? ctx->pred.p : ctx->trusted.p, pr.size(), cudaMemcpyDeviceToHost,
+                           ctx->stream),
+           "D2H");
+        ck(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+        for (uint32_t c = 0; c < ctx->N; ++c) std::memcpy(out + 4 * (size_t)ctx->cell_old[c], &pr[4 * (size_t)c], 4);
+        return MGPU_OK;
+    });
+}
+
 int mgpu_selector_stats(mgpu_ctx* ctx, uint64_t* counts) {
     if (int rc = need_ready(ctx)) return rc;
     return guarded([&] {

@@ -266,6 +266,13 @@ class Solver:
                                             float(directional_threshold)))
         N.check(self._lib.mgpu_set_selector_every_stage(self._h, 1 if every_stage else 0))
 
+    def selector_predictions(self, raw=True):
+        """[n_cells][4] uint8: the selector's last predictions (mask | 0x80
+        when confident), before (raw) or after the neighbour check."""
+        out = np.zeros((self.mesh.n_cells, 4), dtype=np.uint8)
+        N.check(self._lib.mgpu_selector_predictions(self._h, 1 if raw else 0, N.ptr(out)))
+        return out
+
     def selector_stats(self):
         """Counts over the last reconstruction with the selector attached."""
         c = np.zeros(6, dtype=np.uint64)

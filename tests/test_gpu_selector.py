@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 import mallard_gb300 as mg
-from mallard_gb300.selector import Selector
+from mallard_gb300.selector import Selector, default_weights_path
 from mallard_gb300.mesh import teno_tables
 from cases import explosion, make_pair, perturbed
 from oracle import mlp
@@ -203,3 +203,28 @@ def test_shipped_selector_error_and_work(problem):
     assert st["error"] == 0
     assert np.isfinite(l1) and l1 <= (1e-3 if problem == "explosion" else 2e-3)
     assert frac < 0.8
+
+
+def test_in_solver_predictions_match_harvested_features():
+    """The FP32 form's in-solver inference (features built from the FP32
+    stage state inside the tcgen05 kernel) predicts exactly what the
+    stand-alone inference predicts from the harvested features of the same
+    state: same features, same BF16 operands, same logits."""
+    m = mg.Mesh.generate("cartesian_tri", 20, 20, 1.0, 1.0)
+    U, W = explosion(m, radius=0.25)
+    with Selector() as sel:
+        sel.load(default_weights_path())
+        s, _ = make_pair(m, variant="corrected", precision="fp32", reorder=False)
+        s.attach_selector(sel, threshold=0.98, directional_threshold=2.0)
+        s.set_state(U, W)
+        s.run(0.5, 1)   # predicts from the initial state
+        P_in = s.selector_predictions(raw=True)
+        s.close()
+        h, _ = make_pair(m, variant="corrected", precision="fp64", reorder=False)
+        h.set_state(U, W)
+        sel.clear()
+        assert sel.harvest(h, keep_central=1.0, seed=0) == m.n_cells
+        X, _ = sel.samples()
+        h.close()
+        _, P = sel.infer(X, threshold=0.98, directional_threshold=2.0)
+    np.testing.assert_array_equal(P_in, P)
