@@ -299,12 +299,14 @@ struct mgpu_ctx {
 
     // ---- host <-> device in caller numbering ------------------------------
     // One copy engine transfer of the caller's buffer (pinned or pageable)
-    // into a staging array, then a permutation kernel on the device.
+    // into a staging array, then a permutation kernel on the device.  Not
+    // synchronised: stream order protects the staging array, and every
+    // caller synchronises before it returns (the host buffer is borrowed
+    // until then).
     void upload_cells(double* dst, const double* src, int width) {
         const size_t bytes = (size_t)N * width * sizeof(double);
         ck(cudaMemcpyAsync(staging.p, src, bytes, cudaMemcpyHostToDevice, stream), "H2D");
         ck(launch_permute_rows((int)N, width, perm_old.p, staging.p, dst, false, stream), "permute");
-        ck(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
     }
     void download_cells(const double* src, double* dst, int width) {
         const size_t bytes = (size_t)N * width * sizeof(double);

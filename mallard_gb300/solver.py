@@ -186,12 +186,18 @@ class Solver:
         W = None if primitives is None else np.ascontiguousarray(primitives, dtype=np.float64).reshape(self.n_cells, 5)
         N.check(self._lib.mgpu_set_state(self._h, N.ptr(U), N.ptr(W)))
 
-    def get_state(self, U=None, W=None):
+    def get_state(self, U=None, W=None, primitives=True):
         """Conservatives and primitives in the caller's cell order; pass
-        (e.g. pinned) output arrays to receive them in place."""
+        (e.g. pinned) output arrays to receive them in place.  primitives
+        False: the conservatives alone (W is None)."""
         U = np.empty((self.n_cells, 4)) if U is None else U
-        W = np.empty((self.n_cells, 5)) if W is None else W
+        if primitives:
+            W = np.empty((self.n_cells, 5)) if W is None else W
+        else:
+            W = None
         for a, w in ((U, 4), (W, 5)):
+            if a is None:
+                continue
             if a.dtype != np.float64 or not a.flags.c_contiguous or a.size != self.n_cells * w:
                 raise ValueError("state buffers must be contiguous float64 of the mesh size")
         N.check(self._lib.mgpu_get_state(self._h, N.ptr(U), N.ptr(W)))
