@@ -229,6 +229,10 @@ int mgpu_destroy(mgpu_ctx* ctx);
 int mgpu_set_stream(mgpu_ctx* ctx, void* stream);
 int mgpu_synchronize(mgpu_ctx* ctx);
 
+/* State in the caller's cell order, [n_cells][4] and [n_cells][5].
+ * set_state: primitives NULL recovers them on the device from U with the
+ * reference's arithmetic (physics.h:842-867).  get_state: either output may
+ * be NULL.  Host buffers (pinned or pageable) are borrowed for the call. */
 int mgpu_set_state(mgpu_ctx* ctx, const double* U, const double* primitives);
 int mgpu_get_state(mgpu_ctx* ctx, double* U, double* primitives);
 
