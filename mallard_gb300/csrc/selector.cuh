@@ -51,17 +51,20 @@ __device__ __forceinline__ uint32_t stencil_cell(const TenoArgs& a, int tile, in
 }
 
 // The 19 stencil values of variable v minus uc, for stencil s of a cell.
-// NB4: 16-byte index loads from the FP32 form's grouped layout.
+// NB4: 16-byte index loads from the FP32 form's grouped layout; nbs (not
+// null): the same layout for tiles tile0.. staged in shared memory.
 template <bool NB4, class T, class ToF>
 __device__ __forceinline__ void stencil_diffs(const TenoArgs& a, const T* __restrict__ U, int tile, int lane, int s,
-                                              int v, float uc, ToF to_f, float* d) {
+                                              int v, float uc, ToF to_f, float* d, const uint4* nbs = nullptr,
+                                              int tile0 = 0) {
     if (NB4) {
         constexpr int GJ = (MR + 3) / 4;
-        const uint4* p = reinterpret_cast<const uint4*>(a.nb4) + (((size_t)tile * S + s) * GJ) * TILE + lane;
+        const uint4* p = nbs ? nbs + (((size_t)(tile - tile0) * S + s) * GJ) * TILE + lane
+                             : reinterpret_cast<const uint4*>(a.nb4) + (((size_t)tile * S + s) * GJ) * TILE + lane;
         uint32_t id[GJ * 4];
 #pragma unroll
         for (int g = 0; g < GJ; ++g) {
-            const uint4 q = __ldg(p + g * TILE);
+            const uint4 q = nbs ? p[g * TILE] : __ldg(p + g * TILE);
             id[4 * g] = q.x;
             id[4 * g + 1] = q.y;
             id[4 * g + 2] = q.z;
@@ -80,10 +83,10 @@ __device__ __forceinline__ void stencil_diffs(const TenoArgs& a, const T* __rest
 // nearest).  Writes PER_VAR floats.
 template <bool NB4, class T, class ToF>
 __device__ __forceinline__ void features(const TenoArgs& a, const T* __restrict__ U, int cell, int v, unsigned smask,
-                                         ToF to_f, float* x) {
+                                         ToF to_f, float* x, const uint4* nbs = nullptr, int tile0 = 0) {
     const int tile = cell >> 3, lane = cell & 7;
     const float uc = to_f(__ldg(U + (size_t)cell * 4 + v));
-    stencil_diffs<NB4>(a, U, tile, lane, 0, v, uc, to_f, x);
+    stencil_diffs<NB4>(a, U, tile, lane, 0, v, uc, to_f, x, nbs, tile0);
     float lo = 0.0f, hi = 0.0f;
 #pragma unroll
     for (int j = 0; j < MR; ++j) {
@@ -101,7 +104,7 @@ __device__ __forceinline__ void features(const TenoArgs& a, const T* __restrict_
         float f = -1.0f;
         if ((smask >> s) & 1u) {
             float d[MR];
-            stencil_diffs<NB4>(a, U, tile, lane, s, v, uc, to_f, d);
+            stencil_diffs<NB4>(a, U, tile, lane, s, v, uc, to_f, d, nbs, tile0);
             float l = 0.0f, h = 0.0f;
 #pragma unroll
             for (int j = 0; j < MR; ++j) {

@@ -42,10 +42,15 @@ constexpr int BLOB = SM_B + (HID + HID + OUT) * 4;  // 25216
 // one activation buffer: each layer's operand is written after the previous
 // layer's MMAs (which read the buffer) have completed
 constexpr int SM_ACT = BLOB;                  // 128 x 96 BF16 (then 128 x 64, twice)
-constexpr int SM_BAR = SM_ACT + ROWS * IN * 2;
+// the stencil neighbour ids of the CTA's 16 tiles (FP32 form's grouped
+// layout), staged by one bulk copy for the feature gathers
+constexpr int NB_GJ = (MR + 3) / 4;
+constexpr int SM_NB = SM_ACT + ROWS * IN * 2;
+constexpr int NB_TILE_BYTES = S * NB_GJ * TILE * 16;  // 2560
+constexpr int SM_BAR = SM_NB + (ROWS / TILE) * NB_TILE_BYTES;
 constexpr int SM_TOTAL = SM_BAR + 32;
 constexpr int THREADS = ROWS * NV;            // one thread per (cell, variable)
-static_assert(BLOB % 16 == 0 && SM_ACT % 128 == 0, "alignment");
+static_assert(BLOB % 16 == 0 && SM_ACT % 128 == 0 && SM_NB % 16 == 0 && SM_BAR % 8 == 0, "alignment");
 static_assert(BLOB == WEIGHT_IMAGE_BYTES, "weight image size");
 
 // GELU of the inference epilogue with the hardware tanh (tanh.approx.f32,
@@ -175,13 +180,22 @@ __global__ void __launch_bounds__(THREADS, 2) mlp_kernel(const uint8_t* __restri
     extern __shared__ __align__(128) uint8_t smem[];
     uint64_t* bar_w = reinterpret_cast<uint64_t*>(smem + SM_BAR);
     uint64_t* bar_m = bar_w + 1;
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(bar_w + 2);
+    uint64_t* bar_n = bar_w + 2;
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bar_w + 3);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int tile0 = blockIdx.x * (ROWS / TILE);
+    const int n_tiles = SRC == 1 ? min(ROWS / TILE, (n + TILE - 1) / TILE - tile0) : 0;
 
     if (tid == 0) {
         mbar_init(bar_w, 1);
         mbar_init(bar_m, 1);
+        mbar_init(bar_n, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        if (SRC == 1) {
+            mbar_expect_tx(bar_n, (unsigned)(n_tiles * NB_TILE_BYTES));
+            bulk_g2s(smem + SM_NB, reinterpret_cast<const uint8_t*>(a.nb4) + (size_t)tile0 * NB_TILE_BYTES,
+                     (unsigned)(n_tiles * NB_TILE_BYTES), bar_n);
+        }
     }
     if (warp == 0) tmem_alloc(tslot);
     tc_before();
@@ -195,15 +209,18 @@ __global__ void __launch_bounds__(THREADS, 2) mlp_kernel(const uint8_t* __restri
 
     // layer-0 operand: features of (row, v) in BF16
     uint8_t* act = smem + SM_ACT;
+    bool ok_n = true;
+    if (SRC == 1) ok_n = __syncthreads_and(mbar_wait(bar_n, 0));
     {
         const int row = tid >> 2, v = tid & 3, cell = blockIdx.x * ROWS + row;
         float x[PER_VAR];
-        if (cell < n) {
+        if (cell < n && ok_n) {
             if (SRC == 0) {
 #pragma unroll
                 for (int k = 0; k < PER_VAR; ++k) x[k] = X[(size_t)cell * IN + v * PER_VAR + k];
             } else {
-                features<true>(a, U, cell, v, a.smask[cell], AsFloat{}, x);
+                features<true>(a, U, cell, v, a.smask[cell], AsFloat{}, x,
+                               reinterpret_cast<const uint4*>(smem + SM_NB), tile0);
             }
         } else {
 #pragma unroll
@@ -219,7 +236,7 @@ __global__ void __launch_bounds__(THREADS, 2) mlp_kernel(const uint8_t* __restri
         }
     }
     fence_async_smem();
-    bool ok = mbar_wait(bar_w, 0);
+    bool ok = mbar_wait(bar_w, 0) && ok_n;
     ok = __syncthreads_and(ok);
 
     const float* bias = reinterpret_cast<const float*>(smem + SM_B);
@@ -263,8 +280,9 @@ __global__ void __launch_bounds__(THREADS, 2) mlp_kernel(const uint8_t* __restri
     const int cell = blockIdx.x * ROWS + erow;
     if (!ok) {
         if (tid == 0) atomicOr(err, 1u);
-        // give the copy and the last commit one more bounded wait
+        // give the copies and the last commit one more bounded wait
         mbar_wait(bar_w, 0);
+        if (SRC == 1) mbar_wait(bar_n, 0);
         if (phase > 0) mbar_wait(bar_m, (phase - 1) & 1);
     } else if (cgrp < OUT / 16 && cell < n) {
         if (logits) {
