@@ -240,6 +240,18 @@ int mgpu_writer_write(mgpu_writer* w, uint32_t step, int force) {
         }
         const int id = w->next;
         w->next ^= 1;
+        // a failure before the job is queued gives the slot back
+        struct Release {
+            mgpu_writer* w;
+            mgpu_writer::Slot* s;
+            bool armed = true;
+            ~Release() {
+                if (!armed) return;
+                std::lock_guard<std::mutex> lk(w->mu);
+                s->busy = false;
+                w->cv.notify_all();
+            }
+        } release{w, &s};
         // snapshot: the copy stream follows the solver's stream, and the
         // solver's stream waits only for the snapshot
         cudaEvent_t after = nullptr;
@@ -268,6 +280,7 @@ int mgpu_writer_write(mgpu_writer* w, uint32_t step, int force) {
             std::lock_guard<std::mutex> lk(w->mu);
             w->jobs.push_back({id, step});
         }
+        release.armed = false;
         w->cv.notify_all();
         return MGPU_OK;
     });
