@@ -370,12 +370,14 @@ int mgpu_batch_set_stream(mgpu_batch* b, void* stream);
 int mgpu_batch_status(mgpu_batch* b, uint32_t* flags, double* times);
 /* Autotuner of the batched reconstruction: times the direct kernel's 4
  * launch shapes x 4 grid sizes (one thread per item, or a persistent grid of
- * 2, 4, 8 CTAs per SM) and the staged kernel's 3 shapes (4-6, as
- * mgpu_autotune numbers them; one warp per item) on the current states and
- * keeps the fastest.  ms[28] receives the times (shape-major, 4 per shape, 0
- * where not applicable); any output may be NULL. */
+ * 2, 4, 8 CTAs per SM), the staged kernel's 3 shapes (4-6, as mgpu_autotune
+ * numbers them; one warp per item) and the resident kernel's 2 (7, 8: one
+ * CTA of 4 or 8 warps per mesh tile, the tile's tables copied into shared
+ * memory once and used for every case) on the current states and keeps the
+ * fastest.  ms[36] receives the times (shape-major, 4 per shape, 0 where not
+ * applicable); any output may be NULL. */
 int mgpu_batch_autotune(mgpu_batch* b, double* ms, int* shape, int* blocks_per_sm);
-/* Fix the batched reconstruction's launch shape (0-6) and grid (CTAs per
+/* Fix the batched reconstruction's launch shape (0-8) and grid (CTAs per
  * SM, 0 = one thread per item; the staged shapes ignore it). */
 int mgpu_batch_set_launch_shape(mgpu_batch* b, int shape, int blocks_per_sm);
 

@@ -108,9 +108,9 @@ class Batch:
         N.check(self._lib.mgpu_batch_set_launch_shape(self._h, int(shape), int(blocks_per_sm)))
 
     def autotune(self):
-        """(shape, CTAs per SM or 0, ms[7][4]) of the batched reconstruction
-        (shapes 4-6, the staged kernel, have one grid: ms[s][0])."""
-        ms = np.zeros(28)
+        """(shape, CTAs per SM or 0, ms[9][4]) of the batched reconstruction
+        (shapes 4-8, the staged and resident kernels, have one grid: ms[s][0])."""
+        ms = np.zeros(36)
         sh, bps = C.c_int(), C.c_int()
         N.check(self._lib.mgpu_batch_autotune(self._h, N.ptr(ms), C.byref(sh), C.byref(bps)))
-        return sh.value, bps.value, ms.reshape(7, 4)
+        return sh.value, bps.value, ms.reshape(9, 4)

@@ -185,6 +185,9 @@ namespace f32 {
 // shape 0) or 4..6, the staged form that copies each tile's table blocks
 // into shared memory with cp.async.bulk; chosen by the autotuner
 constexpr int TENO32_SHAPES = 7;
+// the batched reconstruction also has shapes 7 and 8: one CTA of 4 or 8
+// warps per mesh tile, its tables resident in shared memory for all cases
+constexpr int TENO32_BATCH_SHAPES = 9;
 // U: the FP32 copy of the stage state
 cudaError_t launch_teno(const TenoArgs& a, int K, int M, int nq, const float* U, float* fv, uint8_t* masks,
                         int shape, cudaStream_t s);

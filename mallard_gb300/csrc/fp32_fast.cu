@@ -781,6 +781,103 @@ __global__ void __launch_bounds__(WARPS * 32, MINB) teno32_batch_staged_kernel(c
     }
 }
 
+// Table source of teno32_cell: every stencil block of the tile resident in
+// the CTA's shared memory (slot s = stencil s), loaded once.
+template <int K, int M, int NQ>
+struct ResidentSrc {
+    using B = TileBlocks<K, M, NQ>;
+    using L = StageLayout<K, M, NQ, 4>;
+    const uint8_t* base;
+    unsigned need_all;
+    __device__ __forceinline__ unsigned tile_need(unsigned) const { return need_all; }
+    __device__ __forceinline__ bool begin(int) { return true; }
+    __device__ __forceinline__ void end(int) {}
+    __device__ __forceinline__ const uint4* nb(int s) const {
+        return reinterpret_cast<const uint4*>(base + s * L::SLOT + B::PB);
+    }
+    __device__ __forceinline__ const float4* P(int s) const { return reinterpret_cast<const float4*>(base + s * L::SLOT); }
+    __device__ __forceinline__ const float4* phi() { return reinterpret_cast<const float4*>(base + L::PHI); }
+    template <class T>
+    __device__ __forceinline__ T ld(const T* p) const { return *p; }
+};
+
+// Batched reconstruction with resident tables: one CTA per (mesh group,
+// mesh tile).  The tile's table blocks are bulk-copied into shared memory
+// once; the CTA's warps then take the group's cases in turn (case w, w +
+// WARPS, ...), so a table byte crosses from L2 once per tile instead of
+// once per case.  Frozen cases are skipped; a wait that runs out flags the
+// group's cases (bit 2).
+template <int K, int M, int NQ, int WARPS, int MINB>
+__global__ void __launch_bounds__(WARPS * 32, MINB) teno32_batch_resident_kernel(const BatchLaunch b,
+                                                                                 const float* __restrict__ U) {
+    using L = StageLayout<K, M, NQ, 4>;
+    using B = TileBlocks<K, M, NQ>;
+    extern __shared__ __align__(128) uint8_t stage_smem[];
+    uint64_t* bar = reinterpret_cast<uint64_t*>(stage_smem + L::BAR);
+    long long t = blockIdx.x;
+    int gi = 0;
+    while (gi + 1 < b.n_groups && t >= (long long)((b.n_cells[gi] + 7) / 8)) {
+        t -= (b.n_cells[gi] + 7) / 8;
+        ++gi;
+    }
+    const int tile = (int)t, n = b.n_cells[gi];
+    const TenoArgs& a = b.teno[gi];
+    unsigned need_all = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+        if (tile * 8 + k < n) need_all |= a.smask[tile * 8 + k];
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        unsigned bytes = B::FB;
+        for (int s = 0; s < B::S; ++s)
+            if ((need_all >> s) & 1u) bytes += L::SLOT;
+        mbar_expect_tx(bar, bytes);
+        bulk_g2s(stage_smem + L::PHI, reinterpret_cast<const char*>(a.phi4) + (size_t)tile * B::FB, B::FB, bar);
+        for (int s = 0; s < B::S; ++s) {
+            if (!((need_all >> s) & 1u)) continue;
+            bulk_g2s(stage_smem + s * L::SLOT, reinterpret_cast<const char*>(a.P4) + (size_t)(tile * B::S + s) * B::PB,
+                     B::PB, bar);
+            bulk_g2s(stage_smem + s * L::SLOT + B::PB,
+                     reinterpret_cast<const char*>(a.nb4) + (size_t)(tile * B::S + s) * B::NBB, B::NBB, bar);
+        }
+    }
+    __syncthreads();
+    const bool ok = __syncthreads_and(mbar_wait(bar, 0));
+    const unsigned C = b.C[gi];
+    if (!ok) {
+        if (threadIdx.x == 0)
+            for (unsigned cs = 0; cs < C; ++cs) atomicOr(b.flags + b.case0[gi] + cs, 4u);
+        mbar_wait(bar, 0);
+        return;
+    }
+    ResidentSrc<K, M, NQ> src{stage_smem, need_all};
+    const int warp = threadIdx.x >> 5, lane32 = threadIdx.x & 31;
+    const int cell = tile * 8 + (lane32 >> 2), v = lane32 & 3;
+    for (unsigned cs = warp; cs < C; cs += WARPS) {
+        if (b.flags[b.case0[gi] + cs] != 0u) continue;
+        teno32_cell<K, M, NQ, false>(a, U, b.fv, nullptr, nullptr, cell, v, 0xffffffffu,
+                                     IxB{b.ubase[gi], b.fbase[gi], C, cs}, src, cell < n);
+    }
+}
+
+template <int K, int M, int NQ, int WARPS, int MINB>
+cudaError_t teno_batch_resident(const BatchLaunch& b, const float* U, cudaStream_t s) {
+    constexpr unsigned smem = StageLayout<K, M, NQ, 4>::WARP;
+    static bool attr = false;
+    if (!attr) {
+        const cudaError_t e = cudaFuncSetAttribute(teno32_batch_resident_kernel<K, M, NQ, WARPS, MINB>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    long long tiles = 0;
+    for (int g = 0; g < b.n_groups; ++g) tiles += (b.n_cells[g] + 7) / 8;
+    if (tiles > 0)
+        teno32_batch_resident_kernel<K, M, NQ, WARPS, MINB><<<(unsigned)tiles, WARPS * 32, smem, s>>>(b, U);
+    return cudaGetLastError();
+}
+
 template <int K, int M, int NQ, int NSLOT, int WARPS, int MINB>
 cudaError_t teno_batch_staged(const BatchLaunch& b, const float* U, cudaStream_t s) {
     constexpr unsigned smem = WARPS * StageLayout<K, M, NQ, NSLOT>::WARP;
@@ -820,6 +917,8 @@ cudaError_t launch_teno_batch(const BatchLaunch& b, const float* U, int shape, i
         case 4: return teno_batch_staged<10, 20, 2, 1, 4, 6>(b, U, s);
         case 5: return teno_batch_staged<10, 20, 2, 2, 2, 7>(b, U, s);
         case 6: return teno_batch_staged<10, 20, 2, 1, 4, 4>(b, U, s);
+        case 7: return teno_batch_resident<10, 20, 2, 4, 6>(b, U, s);
+        case 8: return teno_batch_resident<10, 20, 2, 8, 3>(b, U, s);
     }
     return cudaErrorInvalidValue;
 }

@@ -371,7 +371,7 @@ int mgpu_batch_status(mgpu_batch* b, uint32_t* flags, double* times) {
 
 int mgpu_batch_set_launch_shape(mgpu_batch* b, int shape, int blocks_per_sm) {
     if (int rc = need_batch(b)) return rc;
-    if (shape < 0 || shape >= f32::TENO32_SHAPES || blocks_per_sm < 0) {
+    if (shape < 0 || shape >= f32::TENO32_BATCH_SHAPES || blocks_per_sm < 0) {
         set_error("launch shape out of range");
         return MGPU_ERR_ARG;
     }
@@ -394,9 +394,9 @@ int mgpu_batch_autotune(mgpu_batch* b, double* ms, int* shape, int* blocks_per_s
         ck(cudaEventCreate(&e1), "cudaEventCreate");
         double best = 1e300;
         int bs = 0, bg = 0;
-        for (int sh = 0; sh < f32::TENO32_SHAPES; ++sh)
+        for (int sh = 0; sh < f32::TENO32_BATCH_SHAPES; ++sh)
             for (int gi = 0; gi < 4; ++gi) {
-                if (sh >= 4 && gi > 0) continue;  // the staged shapes launch one warp per item
+                if (sh >= 4 && gi > 0) continue;  // the staged and resident shapes have one grid
                 ck(f32::launch_teno_batch(b->bl, b->U32.p, sh, grids[gi], b->stream), "reconstruction");
                 ck(cudaEventRecord(e0, b->stream), "cudaEventRecord");
                 for (int r = 0; r < 3; ++r)

@@ -41,10 +41,10 @@ def _single(m, U, W, steps):
     return Ug, t
 
 
-@pytest.mark.parametrize("shape", [0, 4, 5])
+@pytest.mark.parametrize("shape", [0, 4, 5, 7, 8])
 def test_batch_matches_single_case_runs(shape):
     """Every case of a batch over two meshes against its own single-case run
-    (direct shape 0, staged shapes 4 and 5)."""
+    (direct shape 0, staged shapes 4 and 5, resident-table shapes 7 and 8)."""
     meshes, states = _cases()
     steps = 25
     with Batch(meshes, [3, 2], boundaries=BCS, **GAS) as b:
@@ -78,7 +78,7 @@ def test_batch_autotune_and_independent_time_steps():
         for g, k, U, W in states:
             b.set_state(g, k, U, W)
         sh, bps, ms = b.autotune()
-        assert 0 <= sh < 7 and bps in (0, 2, 4, 8)
+        assert 0 <= sh < 9 and bps in (0, 2, 4, 8)
         assert np.all(ms[:4] > 0) and np.all(ms[4:, 0] > 0) and np.all(ms[4:, 1:] == 0)
         for g, k, U, W in states:
             b.set_state(g, k, U, W)
