@@ -7,10 +7,11 @@
 //           (stencil order), divided by the variable's range over that
 //           stencil (target included);
 //   19      log10 of that range, scaled: (log10 r + 6) / 6 clamped to
-//           [-1, 1]; -1 when the range is zero (below 1e-30);
+//           [-1, 1]; -1 when the range is flat (at most FLAT_RANGE);
 //   20..22  range over directional stencil d (target included) divided by
-//           the central range, clipped to 4 and scaled by 1/4; -1 when the
-//           stencil does not exist (boundary face);
+//           the central range, clipped to 4 and scaled by 1/4 (for a flat
+//           central range: 1 if the directional one is not flat, else 0); -1
+//           when the stencil does not exist (boundary face);
 //   23      zero.
 // Its output is 4 heads (one per variable) of 8 logits over TENO's
 // decisions for that variable: class 0 = central stencil only, class
@@ -27,6 +28,13 @@
 
 namespace mgpu {
 namespace sel {
+
+// Ranges up to this are flat: differences, log-range and directional ratios
+// as for an exactly uniform stencil.  TENO itself treats such stencils as
+// smooth (its smoothness indicators, ~ range^2, fall below its epsilon
+// 1e-12), and the FP32 form's round-off leaves ranges of 1e-7 .. 2e-6 in
+// uniform flow, which the network must read as uniform.
+constexpr float FLAT_RANGE = 1.0e-5f;
 
 // GELU, tanh form: 0.5 x (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3)))
 __device__ __forceinline__ float gelu(float x) {
@@ -93,8 +101,8 @@ __device__ __forceinline__ void features(const TenoArgs& a, const T* __restrict_
         lo = fminf(lo, x[j]);
         hi = fmaxf(hi, x[j]);
     }
-    // ranges below 1e-30 count as zero (their reciprocal would overflow)
-    const float r0 = hi - lo > 1.0e-30f ? hi - lo : 0.0f;
+    // flat ranges count as zero
+    const float r0 = hi - lo > FLAT_RANGE ? hi - lo : 0.0f;
     const float inv = r0 > 0.0f ? 1.0f / r0 : 0.0f;
 #pragma unroll
     for (int j = 0; j < MR; ++j) x[j] *= inv;
@@ -112,7 +120,7 @@ __device__ __forceinline__ void features(const TenoArgs& a, const T* __restrict_
                 h = fmaxf(h, d[j]);
             }
             const float rs = h - l;
-            f = r0 > 0.0f ? fminf(rs * inv, 4.0f) * 0.25f : (rs > 0.0f ? 1.0f : 0.0f);
+            f = r0 > 0.0f ? fminf(rs * inv, 4.0f) * 0.25f : (rs > FLAT_RANGE ? 1.0f : 0.0f);
         }
         x[MR + s] = f;
     }

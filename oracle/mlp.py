@@ -18,6 +18,7 @@ import numpy as np
 NV, PER_VAR, HID, NCLS = 4, 24, 64, 8
 IN, OUT = NV * PER_VAR, NV * NCLS
 MR = 19
+FLAT_RANGE = np.float32(1e-5)  # ranges up to this count as zero (selector.cuh)
 OFF_W1 = 0
 OFF_B1 = OFF_W1 + IN * HID
 OFF_W2 = OFF_B1 + HID
@@ -128,7 +129,8 @@ def features(U, off_stencils, stencils, cells=None):
     TENO stencils in the reference layout (4 stencils per cell, target
     first, empty stencils where a face is on the boundary): per variable the
     19 central-stencil differences divided by their range, the scaled log10
-    of the range, the directional ranges relative to it and a zero."""
+    of the range, the directional ranges relative to it and a zero; ranges
+    up to FLAT_RANGE count as zero."""
     U = np.asarray(U, dtype=np.float64)
     n = U.shape[0]
     cells = np.arange(n) if cells is None else np.asarray(cells)
@@ -145,7 +147,7 @@ def features(U, off_stencils, stencils, cells=None):
             lo = min(np.float32(0.0), d.min())
             hi = max(np.float32(0.0), d.max())
             r0 = np.float32(hi - lo)
-            r0 = r0 if r0 > np.float32(1e-30) else np.float32(0.0)
+            r0 = r0 if r0 > FLAT_RANGE else np.float32(0.0)
             inv = one / r0 if r0 > 0 else np.float32(0.0)
             row[:MR] = d * inv
             row[MR] = np.clip((np.log10(np.float32(r0)) + 6.0) / 6.0, -1.0, 1.0) if r0 > 0 else -1.0
@@ -159,6 +161,6 @@ def features(U, off_stencils, stencils, cells=None):
                 if r0 > 0:
                     row[MR + s] = min(np.float32(rs * inv), np.float32(4.0)) * np.float32(0.25)
                 else:
-                    row[MR + s] = 1.0 if rs > 0 else 0.0
+                    row[MR + s] = 1.0 if rs > FLAT_RANGE else 0.0
             row[PER_VAR - 1] = 0.0
     return out

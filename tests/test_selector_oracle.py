@@ -73,8 +73,10 @@ def test_features_shape_and_ranges():
     # a uniform state gives zero differences and the "no range" marker
     X0 = mlp.features(np.ones((m.n_cells, 4)), t["offsets_stencils"], t["stencils"]).reshape(m.n_cells, 4, mlp.PER_VAR)
     assert np.all(X0[:, :, :19] == 0) and np.all(X0[:, :, 19] == -1)
-    # ranges below 1e-30 count as zero
+    # ranges up to 1e-5 (round-off noise of the FP32 form, denormals) count as zero
     Ut = np.ones((m.n_cells, 4))
     Ut[:, 1] = 1e-40 * r.random(m.n_cells)
+    Ut[:, 2] = 1.0 + 2e-6 * r.random(m.n_cells)
     Xt = mlp.features(Ut, t["offsets_stencils"], t["stencils"]).reshape(m.n_cells, 4, mlp.PER_VAR)
-    assert np.isfinite(Xt).all() and np.all(Xt[:, 1, 19] == -1)
+    assert np.isfinite(Xt).all() and np.all(Xt[:, 1:3, 19] == -1) and np.all(Xt[:, 1:3, :19] == 0)
+    assert np.all(Xt[:, 1:3, 20:23] <= 0)
