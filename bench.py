@@ -29,11 +29,11 @@ learned form, all on the GPU, replayed as a CUDA graph.  Inputs (tables
 Metric: Mcell-updates/s = cells x steps / seconds / 1e6 (one cell-update =
 one cell advanced one full SSPRK3 step).
 
-A second section, "wedge", times the benchmark spec's 4M-cell configuration:
+A second section, "wedge", times the 4M-cell supersonic wedge workload:
 the supersonic ramp channel (Delaunay mesh, viscous at Re 1e5 with no-slip
 walls), plain FP64 against FP32 + learned selector, with the learned
 form's density error.  A third,
-"batched", times configuration 4: 256 four-quadrant cases of uneven mesh
+"batched", times the ensemble workload: 256 four-quadrant cases of uneven mesh
 size stepped together by the batched FP32 form.
 
 --impl reference times the CPU oracle (the restatement of the reference's
@@ -85,7 +85,7 @@ def parse():
     ap.add_argument("--wedge-re", type=float, default=1e5,
                     help="Reynolds number of the wedge on the ramp length (viscous flux, no-slip walls); 0 = inviscid")
     ap.add_argument("--batch-cases", type=int, default=256,
-                    help="cases of the batched section (configuration 4); 0 skips it")
+                    help="cases of the batched section (the four-quadrant ensemble); 0 skips it")
     ap.add_argument("--shape", type=int, default=-1,
                     help="fix the FP32 reconstruction's launch shape (0-6) instead of autotuning it")
     ap.add_argument("--cpu-sample-n", type=int, default=CPU_SAMPLE_N)
@@ -414,7 +414,7 @@ def run_wedge(args, device, selector):
 
 
 def run_batched(args, device):
-    """Configuration 4: n_cases independent four-quadrant problems on unit
+    """The ensemble workload: n_cases independent four-quadrant problems on unit
     squares, mesh size drawn per case from {64, 128, 256, 512}^2 quads
     (cartesian_tri, so twice as many triangles), quadrant states drawn per
     case (rho ~ U[0.1, 2], p ~ U[0.03, 2], u, v ~ U[-1.5, 1.5]); the

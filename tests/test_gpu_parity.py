@@ -1,6 +1,6 @@
 """Parity of the GPU path (through the C ABI) with the CPU oracle.
 
-Tolerance: the spec bar, 1e-12 relative per cell and variable per stage
+Tolerance: the parity bar, 1e-12 relative per cell and variable per stage
 and 1e-10 after 100 steps, relative to max(|ref|, 1e-3 * max|ref| of the
 variable).  The FP64 kernels keep the reference's operation order without
 FMA contraction, so most values are expected to agree bit for bit; the tests
