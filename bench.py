@@ -22,8 +22,8 @@ form's rate, per-kernel times and its density L1 / L-infinity and mass /
 energy differences against the plain FP64 state after the same steps.
 
 One step = spectral radius + dt + three stages of (reconstruction, face flux,
-residual gather + update), plus one selector inference per step in the
-learned form, all on the GPU, replayed as a CUDA graph.  Inputs (tables
+residual gather + update), plus one selector inference every second step in
+the learned form (--sel-interval), all on the GPU, replayed as CUDA graphs.  Inputs (tables
 7-15 GB) are far larger than L2, so no explicit flush is done.
 
 Metric: Mcell-updates/s = cells x steps / seconds / 1e6 (one cell-update =
@@ -86,6 +86,9 @@ def parse():
                     help="Reynolds number of the wedge on the ramp length (viscous flux, no-slip walls); 0 = inviscid")
     ap.add_argument("--batch-cases", type=int, default=256,
                     help="cases of the batched section (the four-quadrant ensemble); 0 skips it")
+    ap.add_argument("--sel-interval", type=int, default=2,
+                    help="steps per selector prediction in the learned form (1 = every step; 2 keeps stale "
+                         "predictions inside the neighbour check's one-cell margin at CFL <= 0.5)")
     ap.add_argument("--shape", type=int, default=-1,
                     help="fix the FP32 reconstruction's launch shape (0-6) instead of autotuning it")
     ap.add_argument("--cpu-sample-n", type=int, default=CPU_SAMPLE_N)
@@ -256,10 +259,11 @@ def load_selector(device):
     return sel, "trained at startup (quick)"
 
 
-def selector_summary(selector, stats):
+def selector_summary(selector, stats, interval=1):
+    when = "once per step" if interval == 1 else f"every {interval} steps"
     return {"weights": selector[1], "central_threshold": SEL_THRESHOLD,
             "directional_predictions": "not trusted (full TENO)",
-            "predict": "once per step, from the step's initial state; trusted where the face neighbours are confident too",
+            "predict": f"{when}, from the step's initial state; trusted where the face neighbours are confident too",
             "confident_cells": stats["confident_cells"] / stats["cells"],
             "confident_variables": stats["confident_variables"] / (4 * stats["cells"]),
             "stencils_evaluated_frac": stats["stencils_evaluated"] / stats["stencils_full"],
@@ -282,7 +286,7 @@ def make_solver(m, args, form, device, selector):
                   boundaries=[{"name": z, "type": "extrapolation"} for z in ("right", "top", "left", "bottom")],
                   teno_variant=args.variant, reorder=True, device=device, precision=prec)
     if learned:
-        s.attach_selector(selector[0], threshold=SEL_THRESHOLD)
+        s.attach_selector(selector[0], threshold=SEL_THRESHOLD, interval=args.sel_interval)
     return s
 
 
@@ -380,7 +384,7 @@ def run_wedge(args, device, selector):
         t1 = time.perf_counter()
         s, U0, W0 = wedge_setup(mesh, precision=prec, reynolds=re)
         if form == "fp32_learned":
-            s.attach_selector(selector[0], threshold=SEL_THRESHOLD)
+            s.attach_selector(selector[0], threshold=SEL_THRESHOLD, interval=args.sel_interval)
         setup = time.perf_counter() - t1
         stream = torch.cuda.Stream()
         s.set_stream(stream.cuda_stream)
@@ -406,7 +410,7 @@ def run_wedge(args, device, selector):
         out[form] = {"value": mesh.n_cells * args.steps / (ms * 1e-3) / 1e6, "ms_per_step": ms / args.steps,
                      "finite": bool(np.isfinite(U).all()) and s.status() == 0, "setup_s": setup}
         if form == "fp32_learned":
-            out[form]["selector"] = selector_summary(selector, s.selector_stats())
+            out[form]["selector"] = selector_summary(selector, s.selector_stats(), args.sel_interval)
         s.close()
     out["fp32_learned"].update(errors_vs(mesh, finals["fp32_learned"], finals["fp64"]))
     out["speedup_learned_vs_fp64"] = out["fp32_learned"]["value"] / out["fp64"]["value"]
@@ -528,7 +532,7 @@ def run_ours(args):
                        "finite": bool(np.isfinite(r["U"]).all()) and r["flags"] == 0,
                        "kernel_ms_per_launch": {k: v[0] / max(v[1], 1) for k, v in kt.items() if v[1]}}
         if r["stats"]:
-            forms[form]["selector"] = selector_summary(selector, r["stats"])
+            forms[form]["selector"] = selector_summary(selector, r["stats"], args.sel_interval)
         if r["tune"]:
             forms[form]["autotune"] = r["tune"]
     # ---- the headline form
@@ -597,12 +601,14 @@ def run_ours(args):
                 "unit": "GB/s", "frac": achieved / hbm_peak if achieved else None,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if pk.exists() else "fallback 6800 GB/s",
                 "traffic": traffic, "algorithmic_bytes_per_launch": algo}
-    launches_per_step = 11 + (2 if learned else 0)  # + selector inference and neighbour check
-    gpu_launches = args.steps * launches_per_step
+    # 11 per step; the selector's inference and neighbour check on the
+    # prediction steps (the first of the timed call, then every interval)
+    pred_steps = -(-args.steps // max(args.sel_interval, 1)) if learned else 0
+    gpu_launches = args.steps * 11 + 2 * pred_steps
     forms[head] = {"value": value, "ms_per_step": ms_max / args.steps, "finite": finite,
                    "kernel_ms_per_launch": {k: v[0] / max(v[1], 1) for k, v in kt.items() if v[1]}}
     if stats:
-        forms[head]["selector"] = selector_summary(selector, stats)
+        forms[head]["selector"] = selector_summary(selector, stats, args.sel_interval)
     if r["tune"]:
         forms[head]["autotune"] = r["tune"]
     solver.close()

@@ -328,6 +328,11 @@ int mgpu_set_selector(mgpu_ctx* ctx, mgpu_selector* sel, float thr_central, floa
  * initial state, and the three SSPRK3 stages use those predictions;
  * every_stage != 0 predicts at every stage instead. */
 int mgpu_set_selector_every_stage(mgpu_ctx* ctx, int every_stage);
+/* Predict every `steps` CFL steps of mgpu_run (default 1; each call starts
+ * with a prediction); the steps between reuse the last trusted predictions.
+ * Information crosses at most CFL cells per step, so with CFL <= 0.5 an
+ * interval of 2 stays inside the one-ring margin of the neighbour check. */
+int mgpu_set_selector_interval(mgpu_ctx* ctx, uint32_t steps);
 /* Counts over the last reconstruction with the selector: [0] cells,
  * [1] cells with every variable confident, [2] confident variables,
  * [3] stencils evaluated, [4] stencils full TENO evaluates, [5] error flag. */

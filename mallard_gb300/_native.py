@@ -161,6 +161,7 @@ def lib():
         "mgpu_set_selector": (i32, [vp, vp, C.c_float, C.c_float]),
         "mgpu_selector_stats": (i32, [vp, vp]),
         "mgpu_selector_predictions": (i32, [vp, i32, vp]),
+        "mgpu_set_selector_interval": (i32, [vp, u32]),
         "mgpu_set_selector_every_stage": (i32, [vp, i32]),
     }
     for name, (res, args) in sig.items():

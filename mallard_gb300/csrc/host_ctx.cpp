@@ -754,10 +754,7 @@ int mgpu_set_stream(mgpu_ctx* ctx, void* stream) {
             ck(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking), "cudaStreamCreate");
             ctx->own_stream = true;
         }
-        if (ctx->step_exec) {
-            cudaGraphExecDestroy(ctx->step_exec);
-            ctx->step_exec = nullptr;
-        }
+        ctx->drop_graphs();
         return MGPU_OK;
     });
 }
@@ -884,30 +881,32 @@ int mgpu_run(mgpu_ctx* ctx, double cfl, uint32_t n_steps, double* t_out) {
     if (int rc = need_ready(ctx)) return rc;
     return guarded([&] {
         ck(launch_set_scalar(ctx->t_ptr(), 0.0, ctx->stream), "set t");
+        // a prediction step every sel_interval steps, counted from this call
+        const uint32_t every = ctx->sel_on ? ctx->sel_interval : 1;
         if (ctx->timing) {
-            for (uint32_t s = 0; s < n_steps; ++s) ctx->cfl_step(cfl);
+            for (uint32_t s = 0; s < n_steps; ++s) ctx->cfl_step(cfl, s % every == 0);
         } else {
-            if (!ctx->step_exec || ctx->step_cfl != cfl) {
-                if (ctx->step_exec) {
-                    cudaGraphExecDestroy(ctx->step_exec);
-                    ctx->step_exec = nullptr;
-                }
+            if (ctx->step_cfl != cfl) ctx->drop_graphs();
+            auto capture = [&](bool predict, cudaGraphExec_t* exec) {
                 cudaGraph_t g = nullptr;
                 ck(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
                 try {
-                    ctx->cfl_step(cfl);
+                    ctx->cfl_step(cfl, predict);
                 } catch (...) {
                     cudaStreamEndCapture(ctx->stream, &g);
                     if (g) cudaGraphDestroy(g);
                     throw;
                 }
                 ck(cudaStreamEndCapture(ctx->stream, &g), "cudaStreamEndCapture");
-                cudaError_t e = cudaGraphInstantiate(&ctx->step_exec, g, 0);
+                cudaError_t e = cudaGraphInstantiate(exec, g, 0);
                 cudaGraphDestroy(g);
                 ck(e, "cudaGraphInstantiate");
-                ctx->step_cfl = cfl;
-            }
-            for (uint32_t s = 0; s < n_steps; ++s) ck(cudaGraphLaunch(ctx->step_exec, ctx->stream), "cudaGraphLaunch");
+            };
+            if (!ctx->step_exec) capture(true, &ctx->step_exec);
+            if (every > 1 && !ctx->step_exec_np) capture(false, &ctx->step_exec_np);
+            ctx->step_cfl = cfl;
+            for (uint32_t s = 0; s < n_steps; ++s)
+                ck(cudaGraphLaunch(s % every == 0 ? ctx->step_exec : ctx->step_exec_np, ctx->stream), "cudaGraphLaunch");
         }
         if (t_out) {
             double h = 0;
@@ -1001,10 +1000,7 @@ int mgpu_autotune(mgpu_ctx* ctx, double* ms, int* best) {
         cudaEventDestroy(a);
         cudaEventDestroy(b);
         ctx->teno_shape = choice;
-        if (ctx->step_exec) {  // recapture with the chosen shape
-            cudaGraphExecDestroy(ctx->step_exec);
-            ctx->step_exec = nullptr;
-        }
+        ctx->drop_graphs();  // recapture with the chosen shape
         if (ms)
             for (int i = 0; i < f32::TENO32_SHAPES; ++i) ms[i] = t[i];
         if (best) *best = choice;
@@ -1020,10 +1016,7 @@ int mgpu_set_launch_shape(mgpu_ctx* ctx, int shape) {
         return MGPU_ERR_ARG;
     }
     ctx->teno_shape = shape;
-    if (ctx->step_exec) {
-        cudaGraphExecDestroy(ctx->step_exec);
-        ctx->step_exec = nullptr;
-    }
+    ctx->drop_graphs();
     return MGPU_OK;
 }
 

@@ -93,6 +93,7 @@ struct mgpu_ctx {
     bool sel_on = false;
     float sel_thr_central = 0.0f, sel_thr_directional = 0.0f;
     bool sel_every_stage = false;
+    uint32_t sel_interval = 1;  // steps per selector prediction
     int teno_shape = 0;  // FP32 reconstruction launch shape (mgpu_autotune)
     DevArray<uint8_t> sel_wimg, pred, trusted;  // raw predictions, after the neighbour check
     DevArray<unsigned> sel_err;
@@ -120,9 +121,15 @@ struct mgpu_ctx {
     DevArray<uint32_t> perm_old;   // internal cell -> caller cell
     TenoArgs teno{};
 
-    // CUDA graph of one CFL step, keyed by cfl
-    cudaGraphExec_t step_exec = nullptr;
+    // CUDA graphs of one CFL step, keyed by cfl: with the selector's
+    // prediction, and (prediction interval > 1) without it
+    cudaGraphExec_t step_exec = nullptr, step_exec_np = nullptr;
     double step_cfl = -1.0;
+    void drop_graphs() {
+        if (step_exec) cudaGraphExecDestroy(step_exec);
+        if (step_exec_np) cudaGraphExecDestroy(step_exec_np);
+        step_exec = step_exec_np = nullptr;
+    }
 
     // per-launch timing
     bool timing = false;
@@ -135,7 +142,7 @@ struct mgpu_ctx {
     double recon_bytes = 0, stage_bytes = 0;
 
     ~mgpu_ctx() {
-        if (step_exec) cudaGraphExecDestroy(step_exec);
+        drop_graphs();
         for (auto& m : marks) {
             cudaEventDestroy(m.a);
             cudaEventDestroy(m.b);
@@ -261,11 +268,12 @@ struct mgpu_ctx {
         return cfg.time_integrator == MGPU_INTEGRATOR_FE ? 1 : (cfg.time_integrator == MGPU_INTEGRATOR_RK4 ? 4 : 3);
     }
 
-    void stage(int k) {
+    void stage(int k, bool predict_step = true) {
         const double* in = (k == 1) ? U.p : Ut.p;
-        // the selector predicts once per step, from the step's initial state,
-        // unless asked to predict at every stage
-        reconstruct(in, nullptr, k == 1 || sel_every_stage);
+        // the selector predicts at the first stage of a prediction step (every
+        // sel_interval-th), from the step's initial state, or at every stage
+        // when asked to
+        reconstruct(in, nullptr, (k == 1 && predict_step) || sel_every_stage);
         flux(in);
         viscous(in);
         UpdateArgs a = update_args();
@@ -292,9 +300,9 @@ struct mgpu_ctx {
         ck(launch_dt(rmax.p, cfl, dt_ptr(), accumulate_t ? t_ptr() : nullptr, flags.p, stream), "dt launch");
     }
 
-    void cfl_step(double cfl) {
+    void cfl_step(double cfl, bool predict_step = true) {
         spectral_and_dt(cfl, true);
-        for (int k = 1; k <= n_stages(); ++k) stage(k);
+        for (int k = 1; k <= n_stages(); ++k) stage(k, predict_step);
     }
 
     // ---- host <-> device in caller numbering ------------------------------

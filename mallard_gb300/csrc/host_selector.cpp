@@ -453,10 +453,7 @@ int mgpu_set_selector(mgpu_ctx* ctx, mgpu_selector* s, float thr_central, float 
     return guarded([&] {
         if (!s || !(thr_central > 0.0f)) {
             ctx->sel_on = false;
-            if (ctx->step_exec) {
-                cudaGraphExecDestroy(ctx->step_exec);
-                ctx->step_exec = nullptr;
-            }
+            ctx->drop_graphs();
             return MGPU_OK;
         }
         if (!ctx->single() || ctx->K != 10) throw Unsupported("the learned selector drives the FP32 form at p = 3");
@@ -473,10 +470,7 @@ int mgpu_set_selector(mgpu_ctx* ctx, mgpu_selector* s, float thr_central, float 
         ctx->sel_thr_central = thr_central;
         ctx->sel_thr_directional = thr_directional;
         ctx->sel_on = true;
-        if (ctx->step_exec) {  // the captured step no longer matches
-            cudaGraphExecDestroy(ctx->step_exec);
-            ctx->step_exec = nullptr;
-        }
+        ctx->drop_graphs();  // the captured step no longer matches
         return MGPU_OK;
     });
 }
@@ -485,10 +479,17 @@ int mgpu_set_selector_every_stage(mgpu_ctx* ctx, int every_stage) {
     if (int rc = need_ready(ctx)) return rc;
     return guarded([&] {
         ctx->sel_every_stage = every_stage != 0;
-        if (ctx->step_exec) {
-            cudaGraphExecDestroy(ctx->step_exec);
-            ctx->step_exec = nullptr;
-        }
+        ctx->drop_graphs();
+        return MGPU_OK;
+    });
+}
+
+int mgpu_set_selector_interval(mgpu_ctx* ctx, uint32_t steps) {
+    if (int rc = need_ready(ctx)) return rc;
+    return guarded([&] {
+        if (steps == 0) throw ArgFail("the prediction interval is at least one step");
+        ctx->sel_interval = steps;
+        ctx->drop_graphs();
         return MGPU_OK;
     });
 }

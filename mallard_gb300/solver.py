@@ -260,17 +260,20 @@ class Solver:
         return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(("recon", "flux", "update", "cfl", "selector"))}
 
     # ---- learned stencil selector (FP32 form) --------------------------------
-    def attach_selector(self, selector, threshold=0.98, directional_threshold=2.0, every_stage=False):
+    def attach_selector(self, selector, threshold=0.98, directional_threshold=2.0, every_stage=False, interval=1):
         """Drive this FP32-form solver's TENO decisions with a trained
         selector: a variable predicted central with probability >= threshold
         skips the smoothness indicators and the directional stencils; a
         directional prediction is trusted only at >= directional_threshold
         (the default 2 trusts none).  Predictions are made once per time step
-        unless every_stage.  selector None detaches."""
+        (every interval steps in run()) unless every_stage.  selector None
+        detaches."""
         N.check(self._lib.mgpu_set_selector(self._h, selector._h if selector is not None else None,
                                             float(threshold) if selector is not None else 0.0,
                                             float(directional_threshold)))
-        N.check(self._lib.mgpu_set_selector_every_stage(self._h, 1 if every_stage else 0))
+        if selector is not None:
+            N.check(self._lib.mgpu_set_selector_every_stage(self._h, 1 if every_stage else 0))
+            N.check(self._lib.mgpu_set_selector_interval(self._h, int(interval)))
 
     def selector_predictions(self, raw=True):
         """[n_cells][4] uint8: the selector's last predictions (mask | 0x80

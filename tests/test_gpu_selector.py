@@ -161,8 +161,9 @@ def test_learned_form_error_and_gain():
     assert frac_t < 0.6 and frac_t < frac_u
 
 
+@pytest.mark.parametrize("interval", [1, 2])
 @pytest.mark.parametrize("problem", ["explosion", "four_quadrant"])
-def test_shipped_selector_error_and_work(problem):
+def test_shipped_selector_error_and_work(problem, interval):
     """The trained weights shipped with the package, on problems they were not
     trained on, at the default central threshold 0.98 with one prediction per
     step: density L1 error against the plain FP64 run and the share of the
@@ -190,7 +191,7 @@ def test_shipped_selector_error_and_work(problem):
     with Selector() as sel:
         sel.load(path)
         f32, _ = make_pair(m, variant="corrected", precision="fp32")
-        f32.attach_selector(sel, threshold=0.98)
+        f32.attach_selector(sel, threshold=0.98, interval=interval)
         f32.set_state(U, W)
         f32.run(0.5, steps)
         Ug, _ = f32.get_state()
@@ -198,7 +199,7 @@ def test_shipped_selector_error_and_work(problem):
     vol = m.cell_volume
     l1 = np.sum(vol * np.abs(Ug[:, 0] - Ur[:, 0])) / np.sum(vol * np.abs(Ur[:, 0]))
     frac = st["stencils_evaluated"] / st["stencils_full"]
-    print(f"shipped selector on {problem}: L1 {l1:.2e}, stencils {frac:.3f}, confident cells "
+    print(f"shipped selector on {problem}, interval {interval}: L1 {l1:.2e}, stencils {frac:.3f}, confident cells "
           f"{st['confident_cells'] / st['cells']:.3f}")
     assert st["error"] == 0
     assert np.isfinite(l1) and l1 <= (1e-3 if problem == "explosion" else 2e-3)
