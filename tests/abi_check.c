@@ -44,12 +44,14 @@ int main(int argc, char** argv) {
     snprintf(path, sizeof path, "%s/rho_000000.vtu", dir);
     if (mgpu_vtu_write(buf, path, 1, names, rho) != MGPU_OK) return fail("vtu");
     /* a bad argument comes back as a status code with a message */
-    const int bad = mgpu_mesh_generate(99, 4, 4, 1.0, 1.0, &back) == MGPU_ERR_ARG;
+    mgpu_mesh_buf* none = NULL;
+    const int bad = mgpu_mesh_generate(99, 4, 4, 1.0, 1.0, &none) == MGPU_ERR_ARG && none == NULL;
     printf("cells=%u faces=%u zones=%u zone1=%s matrices=%llu oi11=%.17g read_cells=%u bad_arg=%d version=%d\n",
            v.n_cells, v.n_faces, v.n_zones, zone, (unsigned long long)n_mat, oi[11], w.n_cells, bad, mgpu_version());
     free(oi);
     free(rho);
     mgpu_teno_tables_free(t);
+    mgpu_mesh_free(back);
     mgpu_mesh_free(buf);
     return 0;
 }
