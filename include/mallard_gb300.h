@@ -232,7 +232,10 @@ int mgpu_synchronize(mgpu_ctx* ctx);
 /* State in the caller's cell order, [n_cells][4] and [n_cells][5].
  * set_state: primitives NULL recovers them on the device from U with the
  * reference's arithmetic (physics.h:842-867).  get_state: either output may
- * be NULL.  Host buffers (pinned or pageable) are borrowed for the call. */
+ * be NULL.  Host buffers (pinned or pageable) are borrowed for the call.
+ * The FP32 form's steps carry no FP64 primitives (its flux and time step
+ * read the FP32 state copy): after a step, get_state recovers them from U
+ * as set_state does; before any step it returns the ones set_state had. */
 int mgpu_set_state(mgpu_ctx* ctx, const double* U, const double* primitives);
 int mgpu_get_state(mgpu_ctx* ctx, double* U, double* primitives);
 
@@ -240,7 +243,8 @@ int mgpu_get_state(mgpu_ctx* ctx, double* U, double* primitives);
 int mgpu_calc_face_values(mgpu_ctx* ctx, const double* U, double* face_values, uint8_t* teno_masks);
 int mgpu_calc_rhs(mgpu_ctx* ctx, const double* U, double* rhs);
 
-/* Time stepping on the resident state. */
+/* Time stepping on the resident state.  The FP32 form computes the
+ * spectral radius in FP32 from its FP32 state copy. */
 int mgpu_calc_dt(mgpu_ctx* ctx, double cfl, double* dt, double* cfl_local);
 int mgpu_take_step(mgpu_ctx* ctx, double dt);
 /* n_steps x (spectral radius -> dt = cfl / max -> SSPRK3 step) without host
@@ -361,6 +365,7 @@ void mgpu_batch_destroy(mgpu_batch* b);
 uint32_t mgpu_batch_n_cases(const mgpu_batch* b);
 /* Also resets the case's time and status flags; prim may be NULL. */
 int mgpu_batch_set_state(mgpu_batch* b, uint32_t group, uint32_t index, const double* U, const double* prim);
+/* prim: recovered from U after a step (as for the FP32 form's mgpu_get_state). */
 int mgpu_batch_get_state(mgpu_batch* b, uint32_t group, uint32_t index, double* U, double* prim);
 /* n_steps CFL steps of every case, each a replay of one captured CUDA graph
  * (spectral radius and dt per case, three SSPRK3 stages); asynchronous. */

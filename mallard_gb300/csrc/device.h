@@ -161,6 +161,10 @@ struct SpecArgs {
     double* rho_cell;
     unsigned long long* rmax_bits;
     double gamma;
+    // FP32 form: the radius comes from the FP32 state rows (spectral32.cuh)
+    const float4* u32;      // null in the FP64 forms
+    double p_min, p_max;
+    float gamma_f, p_min_f, p_max_f;
 };
 
 // Launchers.  All return cudaGetLastError() of the launch.

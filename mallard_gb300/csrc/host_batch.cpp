@@ -36,6 +36,9 @@ struct mgpu_batch {
     DevArray<UpdateArgs> d_upd;
     DevArray<SpecArgs> d_spec;
     int teno_shape = 0, teno_blocks_per_sm = 0;  // autotuned launch of the reconstruction
+    // per case: the steps left its FP64 primitives behind (they are recovered
+    // from U when mgpu_batch_get_state asks for them)
+    std::vector<uint8_t> prim_stale;
     cudaGraphExec_t exec = nullptr;
     double exec_cfl = -1.0;
     ~mgpu_batch() {
@@ -193,8 +196,7 @@ int mgpu_batch_finalize(mgpu_batch* b) {
             sa.lr = c->lr.p;
             sa.nrm = c->nrm.p;
             sa.dxn = c->dxn.p;
-            sa.idxn = c->idxn.p;
-            sa.gamma = c->gas.gamma;
+            c->spec_fp32(sa);  // gas constants; the state rows are the batch's (below)
             hs.push_back(sa);
             if (c->nq != b->groups[0]->nq) throw Unsupported("all meshes need the same face quadrature");
         }
@@ -218,6 +220,7 @@ int mgpu_batch_finalize(mgpu_batch* b) {
         b->d_teno.upload(ht);
         b->d_flux.upload(hf);
         b->d_upd.upload(hu);
+        for (SpecArgs& sa : hs) sa.u32 = reinterpret_cast<const float4*>(b->U32.p);
         b->d_spec.upload(hs);
         bl.teno = b->d_teno.p;
         bl.flux = b->d_flux.p;
@@ -236,6 +239,7 @@ int mgpu_batch_finalize(mgpu_batch* b) {
         bl.t = b->t.p;
         bl.rmax = b->rmax.p;
         bl.flags = b->flags.p;
+        b->prim_stale.assign(b->n_cases, 0);
         b->finalized = true;
         return MGPU_OK;
     });
@@ -271,6 +275,7 @@ int mgpu_batch_set_state(mgpu_batch* b, uint32_t group, uint32_t cs, const doubl
         ck(cudaMemsetAsync(b->flags.p + gc, 0, sizeof(unsigned), b->stream), "cudaMemsetAsync");
         ck(cudaMemsetAsync(b->t.p + gc, 0, sizeof(double), b->stream), "cudaMemsetAsync");
         ck(cudaStreamSynchronize(b->stream), "cudaStreamSynchronize");
+        b->prim_stale[gc] = 0;
         return MGPU_OK;
     });
 }
@@ -289,6 +294,13 @@ int mgpu_batch_get_state(mgpu_batch* b, uint32_t group, uint32_t cs, double* Uh,
             ck(cudaStreamSynchronize(b->stream), "cudaStreamSynchronize");
         }
         if (primh) {
+            const uint32_t gc = b->bl.case0[group] + cs;
+            if (b->prim_stale[gc]) {
+                ck(launch_batch_prims((int)c.N, c.gas, b->U.p, b->prim.p, b->snd.p, b->U32.p, b->bl.ubase[group],
+                                      b->C[group], cs, b->stream),
+                   "primitives");
+                b->prim_stale[gc] = 0;
+            }
             ck(launch_batch_rows((int)c.N, 5, c.perm_old.p, b->prim.p, c.staging.p, b->bl.ubase[group], b->C[group],
                                  cs, false, b->stream),
                "rows");
@@ -324,6 +336,7 @@ int mgpu_batch_run(mgpu_batch* b, double cfl, uint32_t n_steps) {
             ck(e, "cudaGraphInstantiate");
             b->exec_cfl = cfl;
         }
+        if (n_steps > 0) std::fill(b->prim_stale.begin(), b->prim_stale.end(), 1);
         for (uint32_t s = 0; s < n_steps; ++s) ck(cudaGraphLaunch(b->exec, b->stream), "cudaGraphLaunch");
         return MGPU_OK;
     });

@@ -781,6 +781,7 @@ int mgpu_set_state(mgpu_ctx* ctx, const double* Uh, const double* primh) {
         if (ctx->single()) ck(launch_to_f32((size_t)ctx->N * 4, ctx->U.p, ctx->U32.p, ctx->stream), "FP32 copy");
         ck(cudaMemsetAsync(ctx->flags.p, 0, sizeof(unsigned), ctx->stream), "cudaMemsetAsync");
         ck(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+        ctx->prim_stale = false;
         return MGPU_OK;
     });
 }
@@ -789,7 +790,10 @@ int mgpu_get_state(mgpu_ctx* ctx, double* Uh, double* primh) {
     if (int rc = need_ready(ctx)) return rc;
     return guarded([&] {
         if (Uh) ctx->download_cells(ctx->U.p, Uh, 4);
-        if (primh) ctx->download_cells(ctx->prim.p, primh, 5);
+        if (primh) {
+            ctx->refresh_prims();
+            ctx->download_cells(ctx->prim.p, primh, 5);
+        }
         return MGPU_OK;
     });
 }
@@ -873,6 +877,7 @@ int mgpu_take_step(mgpu_ctx* ctx, double dt) {
     return guarded([&] {
         ck(launch_set_scalar(ctx->dt_ptr(), dt, ctx->stream), "set dt");
         for (int k = 1; k <= ctx->n_stages(); ++k) ctx->stage(k);
+        ctx->prim_stale = ctx->single();
         return MGPU_OK;
     });
 }
@@ -881,6 +886,7 @@ int mgpu_run(mgpu_ctx* ctx, double cfl, uint32_t n_steps, double* t_out) {
     if (int rc = need_ready(ctx)) return rc;
     return guarded([&] {
         ck(launch_set_scalar(ctx->t_ptr(), 0.0, ctx->stream), "set t");
+        if (n_steps > 0 && ctx->single()) ctx->prim_stale = true;
         // a prediction step every sel_interval steps, counted from this call
         const uint32_t every = ctx->sel_on ? ctx->sel_interval : 1;
         if (ctx->timing) {
@@ -1142,7 +1148,7 @@ bool ctx_spectral_view(mgpu_ctx* ctx, SpecArgs* s, const uint32_t** cell_old, cu
     s->dxn = ctx->dxn.p;
     s->U = ctx->U.p;
     s->prim = ctx->prim.p;
-    s->gamma = ctx->gas.gamma;
+    ctx->spec_fp32(*s);
     *cell_old = ctx->perm_old.p;
     *stream = ctx->stream;
     *device = ctx->cfg.device;

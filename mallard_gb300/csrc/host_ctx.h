@@ -256,8 +256,9 @@ struct mgpu_ctx {
         a.U = U.p;
         a.Ut = Ut.p;
         a.W = W.p;
-        a.prim = prim.p;
-        a.snd = snd.p;
+        // the FP32 form writes no FP64 primitives in its steps (refresh_prims)
+        a.prim = single() ? nullptr : prim.p;
+        a.snd = single() ? nullptr : snd.p;
         a.rhs = rhs.p;
         a.flags = flags.p;
         return a;
@@ -295,9 +296,33 @@ struct mgpu_ctx {
         s.snd = snd.p;
         s.rho_cell = rho_cell.p;
         s.rmax_bits = rmax.p;
-        s.gamma = gas.gamma;
+        spec_fp32(s);
         timed(3, [&] { return launch_spectral(s, rcp(), stream); });
         ck(launch_dt(rmax.p, cfl, dt_ptr(), accumulate_t ? t_ptr() : nullptr, flags.p, stream), "dt launch");
+    }
+
+    // Gas constants of the spectral radius; in the FP32 form, its FP32 state
+    // rows (the radius is then computed from them in FP32).
+    void spec_fp32(SpecArgs& s) const {
+        s.gamma = gas.gamma;
+        s.p_min = gas.p_min;
+        s.p_max = gas.p_max;
+        s.gamma_f = gas.gamma_f;
+        s.p_min_f = gas.p_min_f;
+        s.p_max_f = gas.p_max_f;
+        s.idxn = idxn.p;
+        s.u32 = single() ? reinterpret_cast<const float4*>(U32.p) : nullptr;
+    }
+
+    // The FP32 form's steps leave the FP64 primitives and sound speeds
+    // behind (nothing in its step reads them); they are recovered from U,
+    // with the reference's formula, when a caller asks for them.
+    bool prim_stale = false;
+    void refresh_prims() {
+        if (!prim_stale) return;
+        ck(launch_primitives_batch(gas, N, U.p, prim.p, stream), "primitives");
+        ck(launch_sound((int)N, gas.gamma, U.p, prim.p, snd.p, stream), "sound speed");
+        prim_stale = false;
     }
 
     void cfl_step(double cfl, bool predict_step = true) {

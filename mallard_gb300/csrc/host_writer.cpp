@@ -254,6 +254,9 @@ int mgpu_writer_write(mgpu_writer* w, uint32_t step, int force) {
         } release{w, &s};
         // snapshot: the copy stream follows the solver's stream, and the
         // solver's stream waits only for the snapshot
+        bool wants_prims = false;
+        for (int k : w->vars) wants_prims = wants_prims || (k >= 4 && k < 9);
+        if (wants_prims) ctx->refresh_prims();
         cudaEvent_t after = nullptr;
         ck(cudaEventCreateWithFlags(&after, cudaEventDisableTiming), "cudaEventCreate");
         ck(cudaEventRecord(after, ctx->stream), "cudaEventRecord");

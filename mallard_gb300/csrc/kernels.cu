@@ -325,7 +325,7 @@ cudaError_t launch_spectral(const SpecArgs& a, bool fast, cudaStream_t s) {
     const unsigned blocks = (unsigned)((a.n_cells + 255) / 256);
     if (blocks == 0) return cudaSuccess;
     if (fast) return spectral_fast(a, blocks, s);
-    spectral_kernel<false><<<blocks, 256, 0, s>>>(a);
+    spectral_kernel<0><<<blocks, 256, 0, s>>>(a);
     return cudaGetLastError();
 }
 

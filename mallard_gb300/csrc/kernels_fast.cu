@@ -17,7 +17,8 @@ cudaError_t update_fast(const UpdateArgs& a, const GasParams& g, int stage, int 
 }
 
 cudaError_t spectral_fast(const SpecArgs& a, unsigned blocks, cudaStream_t s) {
-    spectral_kernel<true><<<blocks, 256, 0, s>>>(a);
+    if (a.u32) spectral_kernel<2><<<blocks, 256, 0, s>>>(a);
+    else spectral_kernel<1><<<blocks, 256, 0, s>>>(a);
     return cudaGetLastError();
 }
 

@@ -20,6 +20,7 @@
 
 #include "device.h"
 #include "host.h"
+#include "spectral32.cuh"
 
 namespace mgpu {
 // Defined in host_ctx.cpp: the context's spectral-radius inputs.
@@ -37,16 +38,26 @@ __device__ __align__(256) unsigned long long g_partial_max[kMaxBlocks];
 std::mutex g_setup_mutex;
 unsigned long long* g_partial_addr[kMaxDevices] = {};
 
-// Per cell: the same spectral radius as the time-step kernel of the main path
-// (SpectralRadiusFunctor, solver.cpp:634-706); per block: the maximum, as
-// the bit pattern of a non-negative double, written to this block's slot.
+struct Rows {
+    __device__ __forceinline__ size_t u(size_t c) const { return c; }
+};
+
+// Per cell: the spectral radius of the time-step kernel of the main path
+// (SpectralRadiusFunctor, solver.cpp:634-706): the FP64 formula with the
+// reference's divisions, or (F32) the FP32 form's radius from its FP32
+// state rows, bit for bit; per block: the maximum, as the bit pattern of a
+// non-negative double, written to this block's slot.
+template <bool F32>
 __global__ void __launch_bounds__(kBlock) spectral_partial_kernel(const mgpu::SpecArgs a,
                                                                  unsigned long long* __restrict__ partial,
                                                                  double* __restrict__ rho_out,
                                                                  const uint32_t* __restrict__ cell_old) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     double tot = 0.0;
-    if (c < a.n_cells) {
+    if (F32 && c < a.n_cells) {
+        tot = mgpu::f64_of(mgpu::spectral_cell32(a, c, Rows{}));
+        if (rho_out) rho_out[cell_old[c]] = tot;
+    } else if (c < a.n_cells) {
         const int4 cf = a.cfaces[c];
         const int ent[4] = {cf.x, cf.y, cf.z, cf.w};
         double conv = 0.0, acou = 0.0;
@@ -166,7 +177,12 @@ extern "C" int mgpu_calc_dt_noalloc(mgpu_ctx* ctx, double cfl, double* dt_device
     unsigned long long* partial = nullptr;
     if (e == cudaSuccess) e = partial_scratch(device, &partial);
     if (e == cudaSuccess && blocks > 0) {
-        spectral_partial_kernel<<<(unsigned)blocks, kBlock, 0, stream>>>(a, partial, spectral_radius_device, cell_old);
+        if (a.u32)
+            spectral_partial_kernel<true><<<(unsigned)blocks, kBlock, 0, stream>>>(a, partial, spectral_radius_device,
+                                                                                  cell_old);
+        else
+            spectral_partial_kernel<false><<<(unsigned)blocks, kBlock, 0, stream>>>(a, partial, spectral_radius_device,
+                                                                                   cell_old);
         e = cudaGetLastError();
         if (e == cudaSuccess) {
             dt_from_partials_kernel<<<1, 1024, 0, stream>>>(partial, (int)blocks, cfl, dt_device);

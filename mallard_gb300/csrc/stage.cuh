@@ -12,6 +12,7 @@
 #include "device.h"
 #include "fp_convert.cuh"
 #include "physics.cuh"
+#include "spectral32.cuh"
 
 namespace mgpu {
 
@@ -68,8 +69,9 @@ struct IxB {
 // State arrays an update reads and writes (one case's, or a batch's).
 struct StageState {
     const double* G;
-    double *U, *Ut, *W, *prim, *snd, *rhs;
-    float* u32;  // FP32 copy of the stage's output state, or null
+    double *U, *Ut, *W, *rhs;
+    double *prim, *snd;  // null in the FP32 form, which recovers them on demand
+    float* u32;          // FP32 copy of the stage's output state, or null
 };
 
 __device__ __forceinline__ void store_f32(float* dst, const double* x) {
@@ -201,13 +203,15 @@ __device__ __forceinline__ void update_cell(const UpdateArgs& a, const StageStat
         Uo2[0] = make_double2(u[0], u[1]);
         Uo2[1] = make_double2(u[2], u[3]);
         if (st.u32) store_f32(st.u32 + row * 4, u);
-        double p[5];
-        if (FAST) primitives_rcp(g, u, p);
-        else primitives(g, u, p);
-        double* po = st.prim + row * NPR;
+        if (st.prim) {
+            double p[5];
+            if (FAST) primitives_rcp(g, u, p);
+            else primitives(g, u, p);
+            double* po = st.prim + row * NPR;
 #pragma unroll
-        for (int i = 0; i < NPR; i++) po[i] = p[i];
-        st.snd[row] = sound_speed(g.gamma, u[0], p);
+            for (int i = 0; i < NPR; i++) po[i] = p[i];
+            st.snd[row] = sound_speed(g.gamma, u[0], p);
+        }
         bool ok = true;
 #pragma unroll
         for (int i = 0; i < 4; i++) ok = ok && isfinite(u[i]);
@@ -219,7 +223,7 @@ template <int STAGE, bool FAST, int SCHEME>
 __global__ void __launch_bounds__(256) update_kernel(const UpdateArgs a, const GasParams g) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= a.n_cells) return;
-    const StageState st{a.G, a.U, a.Ut, a.W, a.prim, a.snd, a.rhs, a.u32};
+    const StageState st{a.G, a.U, a.Ut, a.W, a.rhs, a.prim, a.snd, a.u32};
     update_cell<STAGE, FAST, SCHEME>(a, st, g, c, Ix1{}, a.dt, a.flags);
 }
 
@@ -272,12 +276,14 @@ __device__ __forceinline__ double spectral_cell(const SpecArgs& a, const double*
     return tot;
 }
 
-template <bool FAST>
+// MODE 0: the reference's divisions; 1: the FP64-fast form; 2: the FP32
+// form (spectral32.cuh, from the FP32 state rows).
+template <int MODE>
 __global__ void __launch_bounds__(256) spectral_kernel(const SpecArgs a) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     double tot = 0.0;
     if (c < a.n_cells) {
-        tot = spectral_cell<FAST>(a, a.prim, a.snd, c, Ix1{});
+        tot = MODE == 2 ? f64_of(spectral_cell32(a, c, Ix1{})) : spectral_cell<MODE == 1>(a, a.prim, a.snd, c, Ix1{});
         a.rho_cell[c] = tot;
     }
     // block max of positive doubles via their bit patterns
@@ -323,13 +329,14 @@ __global__ void __launch_bounds__(256) update_batch_kernel(const BatchLaunch b, 
         const int c = (int)(tc / C) * 8 + (int)(t & 7);
         const unsigned gc = b.case0[gi] + cs;
         if (c >= b.n_cells[gi] || b.flags[gc] != 0u) continue;
-        const StageState st{b.G, b.U, b.Ut, b.W, b.prim, b.snd, nullptr, STAGE == 3 ? b.U32 : b.Ut32};
+        const StageState st{b.G, b.U, b.Ut, b.W, nullptr, nullptr, nullptr, STAGE == 3 ? b.U32 : b.Ut32};
         update_cell<STAGE, true, MGPU_INTEGRATOR_SSPRK3>(b.upd[gi], st, g, c, IxB{b.ubase[gi], b.fbase[gi], C, cs}, b.dt + gc, b.flags + gc);
     }
 }
 
-// Spectral radius per cell, maximum per case (8 lanes of one case-tile
-// reduce, then one atomic per tile).
+// Spectral radius per cell (the FP32 form's, from the FP32 state rows),
+// maximum per case (8 lanes of one case-tile reduce, then one atomic per
+// tile).
 __global__ void __launch_bounds__(256) spectral_batch_kernel(const BatchLaunch b) {
     const long long total = b.cell0[b.n_groups];
     for (long long gt = (long long)blockIdx.x * 256 + threadIdx.x; gt < total; gt += (long long)gridDim.x * 256) {
@@ -339,7 +346,7 @@ __global__ void __launch_bounds__(256) spectral_batch_kernel(const BatchLaunch b
         const int c = (int)(tc / C) * 8 + (int)(t & 7);
         double tot = 0.0;
         if (c < b.n_cells[gi] && b.flags[b.case0[gi] + cs] == 0u)
-            tot = spectral_cell<true>(b.spec[gi], b.prim, b.snd, c, IxB{b.ubase[gi], b.fbase[gi], C, cs});
+            tot = f64_of(spectral_cell32(b.spec[gi], c, IxB{b.ubase[gi], b.fbase[gi], C, cs}));
         unsigned long long bits = (unsigned long long)__double_as_longlong(tot);
 #pragma unroll
         for (int o = 4; o > 0; o >>= 1) {

@@ -41,6 +41,22 @@ def _single(m, U, W, steps):
     return Ug, t
 
 
+def test_batch_primitives_after_steps():
+    """The batch's steps carry no FP64 primitives: get_state recovers them
+    for the case asked for, from the conserved state it returns; before any
+    step it returns the ones set_state was given."""
+    meshes, states = _cases()
+    with Batch(meshes, [3, 2], boundaries=BCS, **GAS) as b:
+        for g, k, U, W in states:
+            b.set_state(g, k, U, W)
+        np.testing.assert_array_equal(b.get_state(0, 1)[1], states[1][3])
+        b.run(0.5, 5)
+        b.synchronize()
+        for g, k, _, _ in states:
+            Ub, Wb = b.get_state(g, k)
+            np.testing.assert_array_equal(Wb, mg.primitives(Ub, **GAS))
+
+
 @pytest.mark.parametrize("shape", [0, 4, 5, 7, 8])
 def test_batch_matches_single_case_runs(shape):
     """Every case of a batch over two meshes against its own single-case run

@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 import mallard_gb300 as mg
-from cases import explosion, four_quadrant, make_pair, perturbed, pulse, real_faces
+from cases import GAS, explosion, four_quadrant, make_pair, perturbed, pulse, real_faces
 from test_gpu_parity import tri_mesh
 from conftest import rel_err
 
@@ -66,6 +66,32 @@ def test_fp32_100_steps_errors():
           f"fp64 {drift64:.2e} energy diff {e_drift:.2e}")
     assert l1 < 1e-5 and linf < 1e-4
     assert drift32 < 1e-6 and e_drift < 1e-6
+
+
+def test_fp32_primitives_and_time_step():
+    """The FP32 form's steps carry no FP64 primitives: get_state recovers
+    them from the conserved state it returns (bit for bit the primitive
+    recovery of that state), and leaves the ones set_state was given alone
+    until a step runs.  Its time step, computed in FP32 from the FP32 state
+    copy, is the FP64 forms' to FP32 round-off."""
+    m = tri_mesh(24, seed=20261203)
+    s, _ = make_pair(m, variant="corrected", precision="fp32")
+    U, W = explosion(m)
+    s.set_state(U, W)
+    np.testing.assert_array_equal(s.get_state()[1], W)
+    s.run(0.5, 5)
+    assert s.status() == 0
+    Ug, Wg = s.get_state()
+    np.testing.assert_array_equal(Wg, mg.primitives(Ug, **GAS))
+    dt32, cfl32 = s.calc_dt(0.5)
+    s64, _ = make_pair(m, variant="corrected", precision="fp64")
+    s64.set_state(Ug)
+    dt64, cfl64 = s64.calc_dt(0.5)
+    print(f"FP32 time step vs FP64: {abs(dt32 - dt64) / dt64:.2e}")
+    assert abs(dt32 - dt64) <= 1e-6 * dt64
+    np.testing.assert_allclose(cfl32, cfl64, rtol=1e-5)
+    s.close()
+    s64.close()
 
 
 @pytest.mark.parametrize("learned", [False, True])

@@ -47,6 +47,29 @@ def test_calc_dt_noalloc_matches_calc_dt_on_two_calls():
     s.close()
 
 
+def test_calc_dt_noalloc_fp32_form_bit_for_bit():
+    """The FP32 form: both entry points compute the radius in FP32 from the
+    FP32 state rows, with the same roundings, after steps as before them."""
+    torch = pytest.importorskip("torch")
+    m = mg.Mesh.generate("cartesian_tri", 48, 40, 1.0, 1.0)
+    m.permute_cells(11)
+    s = mg.Solver(m, teno_variant="corrected", precision="fp32",
+                  boundaries=[{"name": z, "type": "extrapolation"} for z in ("right", "top", "left", "bottom")])
+    U, W = four_quadrant(m)
+    s.set_state(U, W)
+    lib = N.lib()
+    dt_dev = torch.full((1,), -1.0, dtype=torch.float64, device="cuda")
+    rho_dev = torch.full((m.n_cells,), -1.0, dtype=torch.float64, device="cuda")
+    for call in range(2):
+        dt_ref, cfl_local = s.calc_dt(0.5)
+        N.check(lib.mgpu_calc_dt_noalloc(s._h, 0.5, _dev_ptr(dt_dev), _dev_ptr(rho_dev)))
+        s.synchronize()
+        assert float(dt_dev.cpu().numpy()[0]) == dt_ref, call
+        np.testing.assert_array_equal(dt_ref * rho_dev.cpu().numpy(), cfl_local)
+        s.run(0.5, 3)
+    s.close()
+
+
 def test_calc_dt_noalloc_after_a_larger_mesh():
     """A smaller mesh after a larger one: stale partial slots are never read."""
     torch = pytest.importorskip("torch")
