@@ -93,7 +93,12 @@ __device__ __forceinline__ void update_cell(const UpdateArgs& a, const StageStat
         const double2* Gf = reinterpret_cast<const double2*>(st.G + ix.f((size_t)(ent[e] >> 1)) * 4);
         const double2 g0 = Gf[0], g1 = Gf[1];
         const double x[4] = {g0.x, g0.y, g1.x, g1.y};
-        if (ent[e] & 1) {
+        if (FAST && e == 0) {
+            // the first contribution starts the sum (0 + x is x but for the
+            // sign of a zero): one FP64 add less per variable
+#pragma unroll
+            for (int i = 0; i < 4; i++) r[i] = (ent[e] & 1) ? -x[i] : x[i];
+        } else if (ent[e] & 1) {
 #pragma unroll
             for (int i = 0; i < 4; i++) r[i] = r[i] + (-x[i]);
         } else {
@@ -101,10 +106,17 @@ __device__ __forceinline__ void update_cell(const UpdateArgs& a, const StageStat
             for (int i = 0; i < 4; i++) r[i] = r[i] + x[i];
         }
     }
-    if (FAST) {
-        const double iv = a.ivol[c];
+    // FAST SSPRK3 stages fold 1/volume into their per-cell coefficients
+    // (dt/volume, ...: one FP64 multiply each instead of four); elsewhere
+    // iv stays 1 and the residual itself is scaled
+    constexpr bool FOLD = FAST && STAGE > 0 && SCHEME == MGPU_INTEGRATOR_SSPRK3;
+    double iv = 1.0;
+    if (FOLD) {
+        iv = a.ivol[c];
+    } else if (FAST) {
+        const double v = a.ivol[c];
 #pragma unroll
-        for (int i = 0; i < 4; i++) r[i] = r[i] * iv;
+        for (int i = 0; i < 4; i++) r[i] = r[i] * v;
     } else {
         const double vol = a.vol[c];
 #pragma unroll
@@ -159,12 +171,12 @@ __device__ __forceinline__ void update_cell(const UpdateArgs& a, const StageStat
     } else if (STAGE == 1) {
         const double2 u0 = U2[0], u1 = U2[1];
         const double u[4] = {u0.x, u0.y, u1.x, u1.y};
-        const double c1 = dt * (1.0 / 6.0);
+        const double ht = dt * iv, hw = dt * (1.0 / 6.0) * iv;
         double t[4], w[4];
 #pragma unroll
         for (int i = 0; i < 4; i++) {
-            t[i] = u[i] + dt * r[i];
-            w[i] = u[i] + c1 * r[i];
+            t[i] = u[i] + ht * r[i];
+            w[i] = u[i] + hw * r[i];
         }
         Ut2[0] = make_double2(t[0], t[1]);
         Ut2[1] = make_double2(t[2], t[3]);
@@ -177,7 +189,7 @@ __device__ __forceinline__ void update_cell(const UpdateArgs& a, const StageStat
         const double u[4] = {u0.x, u0.y, u1.x, u1.y};
         const double s[4] = {s0.x, s0.y, s1.x, s1.y};
         double w[4] = {w0.x, w0.y, w1.x, w1.y};
-        const double c1 = dt * (1.0 / 6.0), q = dt / 4.0;
+        const double c1 = dt * (1.0 / 6.0) * iv, q = dt / 4.0 * iv;
         double t[4];
 #pragma unroll
         for (int i = 0; i < 4; i++) {
@@ -194,7 +206,7 @@ __device__ __forceinline__ void update_cell(const UpdateArgs& a, const StageStat
     } else {
         const double2 w0 = W2[0], w1 = W2[1];
         const double w[4] = {w0.x, w0.y, w1.x, w1.y};
-        const double c3 = dt * (2.0 / 3.0);
+        const double c3 = dt * (2.0 / 3.0) * iv;
 #pragma unroll
         for (int i = 0; i < 4; i++) u[i] = w[i] + c3 * r[i];
     }
