@@ -425,7 +425,9 @@ enum {
     MGPU_TABLE_NB = 3,    /* uint32: stencil neighbours (FP64 forms)      */
     MGPU_TABLE_NB32 = 4,  /* uint32: stencil neighbours (FP32 form)       */
     MGPU_TABLE_PHI = 5,   /* double: face-point basis shapes (FP64 forms) */
-    MGPU_TABLE_PHI32 = 6  /* float: face-point basis shapes (FP32 form)   */
+    MGPU_TABLE_PHI32 = 6  /* uint16: per cell, 3 bits per face slot: the
+                           * reference edge whose shape set the FP32 form's
+                           * face points use (7: none)                    */
 };
 int mgpu_get_table(mgpu_ctx* ctx, int field, void* dst, uint64_t* bytes);
 /* Wall seconds of mgpu_finalize's phases, seconds[7]: 0 face and cell

@@ -55,7 +55,12 @@ struct TenoArgs {
     // that a lane reads 16 bytes (transformed areas folded into P)
     const uint32_t* nb4;  // [tiles][4][ceil((M-1)/4)][8][4]
     const float* P4;      // [tiles][4][ceil((M-1)(K-1)/4)][8][4], entry j*(K-1)+k
-    const float* phi4;    // [tiles][ceil(3 n_q (K-1)/4)][8][4], entry (face*n_q+q)*(K-1)+k
+    // Face shapes of the FP32 form.  Mapped into its triangle's reference
+    // frame, a face's points are the Gauss points of one of the reference
+    // triangle's three edges, run in one of two directions: six shape sets,
+    // shared by all cells, picked per face slot by a 3-bit code.
+    const uint16_t* fcode;   // [tiles][8]: per cell, bits 3f..3f+2 = code of face slot f
+    const float4* phi_tab4;  // [8 codes][ceil(n_q (K-1)/4)] float4, entry q*(K-1)+k
     double oi[KR_MAX * KR_MAX];   // oscillation indicator without dof 0, row-major (K-1)^2
     double oi2[KR_MAX * KR_MAX];  // same, upper triangle with doubled off-diagonals (fast form)
     float oi2f[KR_MAX * KR_MAX];  // oi2 in FP32 (FP32-bulk form)

@@ -48,13 +48,15 @@ struct IxB {
 };
 
 // Table blocks of one tile: for stencil s the neighbour ids [GJ][8] uint4
-// and the pseudo-inverse [GP][8] float4, and the face shapes [GF][8] float4,
-// each contiguous in the tiled arrays.
+// and the pseudo-inverse [GP][8] float4, and the face-shape codes of its 8
+// cells (16 bytes), each contiguous in the tiled arrays.
 template <int K, int M, int NQ>
 struct TileBlocks {
     static constexpr int KR = K - 1, MR = M - 1, NF = 3, S = 4;
-    static constexpr int GJ = (MR + 3) / 4, GP = (MR * KR + 3) / 4, GF = (NF * NQ * KR + 3) / 4;
-    static constexpr unsigned PB = GP * TILE * 16, NBB = GJ * TILE * 16, FB = GF * TILE * 16;
+    static constexpr int GJ = (MR + 3) / 4, GP = (MR * KR + 3) / 4;
+    static constexpr int GT = (NQ * KR + 3) / 4;  // float4 per shape set of the code table
+    static constexpr unsigned PB = GP * TILE * 16, NBB = GJ * TILE * 16, CB = TILE * 2;
+    static_assert(CB == 16, "one 16-byte bulk copy of a tile's codes");
 };
 
 // Table source of teno32_cell: the tiled arrays in global memory.
@@ -72,7 +74,7 @@ struct GlobalSrc {
     __device__ __forceinline__ const float4* P(int s) const {
         return reinterpret_cast<const float4*>(a.P4) + (size_t)(tile * B::S + s) * B::GP * TILE;
     }
-    __device__ __forceinline__ const float4* phi() { return reinterpret_cast<const float4*>(a.phi4) + (size_t)tile * B::GF * TILE; }
+    __device__ __forceinline__ const uint16_t* codes() { return a.fcode + (size_t)tile * TILE; }
     template <class T>
     __device__ __forceinline__ T ld(const T* p) const { return __ldg(p); }
 };
@@ -89,7 +91,7 @@ __device__ __forceinline__ bool teno32_cell(const TenoArgs& a, const float* __re
                                             uint8_t* __restrict__ masks, const uint8_t* __restrict__ pred, int cell,
                                             int v, unsigned live, const IX& ix, SRC& src, bool alive = true) {
     constexpr int KR = K - 1, MR = M - 1, NF = 3, S = 4;
-    constexpr int GJ = (MR + 3) / 4, GP = (MR * KR + 3) / 4, GF = (NF * NQ * KR + 3) / 4;
+    constexpr int GJ = (MR + 3) / 4, GP = (MR * KR + 3) / 4, GT = (NQ * KR + 3) / 4;
     const int tile = cell >> 3, lane = cell & 7;
     const float uc = alive ? U[ix.u(cell) * NC + v] : 0.0f;
     const unsigned sm = alive ? a.smask[cell] : 0u;
@@ -212,29 +214,31 @@ __device__ __forceinline__ bool teno32_cell(const TenoArgs& a, const float* __re
         c[k] = t;
     }
 
-    // face values: shapes of all face points, then one dot product each
-    const float4* php = src.phi();
-    if (!php || !ok || !alive) return false;
-    php += lane;
-    float phi[GF * 4];
-#pragma unroll
-    for (int g = 0; g < GF; ++g) {
-        const float4 p4 = src.ld(php + g * TILE);
-        phi[g * 4] = p4.x;
-        phi[g * 4 + 1] = p4.y;
-        phi[g * 4 + 2] = p4.z;
-        phi[g * 4 + 3] = p4.w;
-    }
+    // face values: the shapes of each face slot's code (a 3-bit index into
+    // the shared table: always in bounds), then one dot product per point
+    const uint16_t* codes = src.codes();
+    if (!codes || !ok || !alive) return false;
+    const unsigned code = src.ld(codes + lane);
 #pragma unroll
     for (int fl = 0; fl < NF; ++fl) {
         const uint32_t slot = __ldg(a.cface + ((size_t)tile * NF + fl) * TILE + lane);
         const size_t fi = slot >> 1;
         const unsigned side = slot & 1u;
+        const float4* t4 = a.phi_tab4 + ((code >> (3 * fl)) & 7u) * GT;
+        float phi[GT * 4];
+#pragma unroll
+        for (int g = 0; g < GT; ++g) {
+            const float4 p4 = __ldg(t4 + g);
+            phi[g * 4] = p4.x;
+            phi[g * 4 + 1] = p4.y;
+            phi[g * 4 + 2] = p4.z;
+            phi[g * 4 + 3] = p4.w;
+        }
 #pragma unroll
         for (int q = 0; q < NQ; ++q) {
             float out = uc;
 #pragma unroll
-            for (int k = 0; k < KR; ++k) out = fmaf(c[k], phi[(fl * NQ + q) * KR + k], out);
+            for (int k = 0; k < KR; ++k) out = fmaf(c[k], phi[q * KR + k], out);
             fv[((ix.f(fi) * NQ + q) * 2 + side) * NC + v] = out;
         }
     }
@@ -293,10 +297,10 @@ template <int K, int M, int NQ, int NSLOT>
 struct StageLayout {
     using B = TileBlocks<K, M, NQ>;
     static constexpr unsigned SLOT = B::PB + B::NBB;                // pseudo-inverse, then neighbour ids
-    static constexpr unsigned PHI = NSLOT * SLOT;                   // face shapes
-    static constexpr unsigned BAR = PHI + B::FB;                    // NSLOT + 1 mbarriers
+    static constexpr unsigned PHI = NSLOT * SLOT;                   // face-shape codes of the tile
+    static constexpr unsigned BAR = PHI + B::CB;                    // NSLOT + 1 mbarriers
     static constexpr unsigned WARP = (BAR + 8 * (NSLOT + 1) + 127) / 128 * 128;
-    static_assert(B::PB % 128 == 0 && B::NBB % 16 == 0 && SLOT % 128 == 0 && B::FB % 16 == 0, "alignment");
+    static_assert(B::PB % 128 == 0 && B::NBB % 16 == 0 && SLOT % 128 == 0 && B::CB % 16 == 0, "alignment");
 };
 
 // Table source of teno32_cell: one warp's shared-memory stage.
@@ -356,13 +360,13 @@ struct StageSrc {
     __device__ __forceinline__ const float4* P(int s) const {
         return reinterpret_cast<const float4*>(base + (index(s) % NSLOT) * L::SLOT);
     }
-    __device__ __forceinline__ const float4* phi() {
+    __device__ __forceinline__ const uint16_t* codes() {
         if (!phi_ready) {
             const bool done = mbar_wait(bar(NSLOT), 0u);
             ok = __all_sync(0xffffffffu, done) && ok;
             phi_ready = true;
         }
-        return ok ? reinterpret_cast<const float4*>(base + L::PHI) : nullptr;
+        return ok ? reinterpret_cast<const uint16_t*>(base + L::PHI) : nullptr;
     }
     template <class T>
     __device__ __forceinline__ T ld(const T* p) const { return *p; }
@@ -385,9 +389,9 @@ __global__ void __launch_bounds__(WARPS * 32, MINB) teno32_staged_kernel(const T
     if (lane32 == 0) {
         for (int i = 0; i <= NSLOT; ++i) mbar_init(src.bar(i), 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        // the face shapes first: needed last, by every cell
-        mbar_expect_tx(src.bar(NSLOT), B::FB);
-        bulk_g2s(src.base + L::PHI, reinterpret_cast<const char*>(a.phi4) + (size_t)tile * B::FB, B::FB, src.bar(NSLOT));
+        // the face-shape codes first: needed last, by every cell
+        mbar_expect_tx(src.bar(NSLOT), B::CB);
+        bulk_g2s(src.base + L::PHI, reinterpret_cast<const char*>(a.fcode) + (size_t)tile * B::CB, B::CB, src.bar(NSLOT));
     }
     __syncwarp();
     const int cell = tile * 8 + (lane32 >> 2), v = lane32 & 3;
@@ -765,8 +769,8 @@ __global__ void __launch_bounds__(WARPS * 32, MINB) teno32_batch_staged_kernel(c
     if (lane32 == 0) {
         for (int i = 0; i <= NSLOT; ++i) mbar_init(src.bar(i), 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        mbar_expect_tx(src.bar(NSLOT), B::FB);
-        bulk_g2s(src.base + L::PHI, reinterpret_cast<const char*>(a.phi4) + (size_t)tile * B::FB, B::FB, src.bar(NSLOT));
+        mbar_expect_tx(src.bar(NSLOT), B::CB);
+        bulk_g2s(src.base + L::PHI, reinterpret_cast<const char*>(a.fcode) + (size_t)tile * B::CB, B::CB, src.bar(NSLOT));
     }
     __syncwarp();
     const int cell = tile * 8 + (lane32 >> 2), v = lane32 & 3;
@@ -796,7 +800,7 @@ struct ResidentSrc {
         return reinterpret_cast<const uint4*>(base + s * L::SLOT + B::PB);
     }
     __device__ __forceinline__ const float4* P(int s) const { return reinterpret_cast<const float4*>(base + s * L::SLOT); }
-    __device__ __forceinline__ const float4* phi() { return reinterpret_cast<const float4*>(base + L::PHI); }
+    __device__ __forceinline__ const uint16_t* codes() { return reinterpret_cast<const uint16_t*>(base + L::PHI); }
     template <class T>
     __device__ __forceinline__ T ld(const T* p) const { return *p; }
 };
@@ -829,11 +833,11 @@ __global__ void __launch_bounds__(WARPS * 32, MINB) teno32_batch_resident_kernel
     if (threadIdx.x == 0) {
         mbar_init(bar, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        unsigned bytes = B::FB;
+        unsigned bytes = B::CB;
         for (int s = 0; s < B::S; ++s)
             if ((need_all >> s) & 1u) bytes += L::SLOT;
         mbar_expect_tx(bar, bytes);
-        bulk_g2s(stage_smem + L::PHI, reinterpret_cast<const char*>(a.phi4) + (size_t)tile * B::FB, B::FB, bar);
+        bulk_g2s(stage_smem + L::PHI, reinterpret_cast<const char*>(a.fcode) + (size_t)tile * B::CB, B::CB, bar);
         for (int s = 0; s < B::S; ++s) {
             if (!((need_all >> s) & 1u)) continue;
             bulk_g2s(stage_smem + s * L::SLOT, reinterpret_cast<const char*>(a.P4) + (size_t)(tile * B::S + s) * B::PB,

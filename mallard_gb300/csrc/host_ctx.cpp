@@ -288,21 +288,42 @@ void mgpu_ctx::build() {
             throw Unsupported("GPU TENO kernels exist for p = 1..3 with stencil factor 2 and default face quadrature");
         const int KR = K - 1, MR = M - 1, S = 4, NF = 3;
         // FP32-bulk form: FP32 tables only, in groups of four for 16-byte
-        // loads (flat index j*(K-1)+k for P, (face*n_q+q)*(K-1)+k for phi),
-        // with the transformed areas folded into P
+        // loads (flat index j*(K-1)+k for P), with the transformed areas
+        // folded into P; face shapes as a per-cell code into one shared table
         const bool f32 = single();
         // least squares on the GPU (teno_tables.cu) unless asked for the host
         // build or the basis is monomial (std::pow)
         const bool gpu_lsq = cfg.table_build == MGPU_TABLES_GPU && cfg.basis == MGPU_BASIS_LEGENDRE;
-        const size_t GJ = (MR + 3) / 4, GP = ((size_t)MR * KR + 3) / 4, GF = ((size_t)NF * nq * KR + 3) / 4;
+        const size_t GJ = (MR + 3) / 4, GP = ((size_t)MR * KR + 3) / 4, GT = ((size_t)nq * KR + 3) / 4;
         auto at4 = [](size_t group, size_t lane, size_t e) { return (group * TILE + lane) * 4 + e; };
         std::vector<uint32_t> h_cface(tiles * NF * TILE, 0), h_nb, h_nb4;
         std::vector<double> h_ar, h_P, h_phi;
-        std::vector<float> h_P4, h_phi4;
+        std::vector<float> h_P4, h_tab;
+        std::vector<uint16_t> h_fcode;
+        // The FP32 form's face shapes.  In a triangle's reference frame (its
+        // nodes 0, 1, 2 at (0,0), (1,0), (0,1)) the face from node i0 to node
+        // i1 is a reference edge: code 2 i0 for i1 = i0 + 1 (mod 3), 2 i0 + 1
+        // for i1 = i0 + 2, so six shape sets serve every cell (codes 6 and 7
+        // stay zero).  Each cell's own shapes are still evaluated below and
+        // must equal its codes' entries.
+        const double ref[3][2] = {{0.0, 0.0}, {1.0, 0.0}, {0.0, 1.0}};
+        auto edge_point = [&](int code, int q, double* x) {
+            const int i0 = code / 2, i1 = (code & 1) ? (i0 + 2) % 3 : (i0 + 1) % 3;
+            for (int i = 0; i < 2; i++) x[i] = (qf.pts[q] + 1.0) * 0.5 * (ref[i1][i] - ref[i0][i]) + ref[i0][i];
+        };
         if (f32) {
             h_nb4.assign(tiles * S * GJ * TILE * 4, 0);
             if (!gpu_lsq) h_P4.assign(tiles * S * GP * TILE * 4, 0.0f);
-            h_phi4.assign(tiles * GF * TILE * 4, 0.0f);
+            h_fcode.assign(tiles * TILE, 0x1ff);  // code 7 (zero shapes) until the cell's faces are seen
+            h_tab.assign(8 * GT * 4, 0.0f);
+            for (int code = 0; code < 6; ++code)
+                for (int q = 0; q < nq; ++q) {
+                    double xq[2];
+                    edge_point(code, q, xq);
+                    for (int k = 1; k < K; ++k)
+                        h_tab[(size_t)code * GT * 4 + (size_t)q * KR + (k - 1)] =
+                            (float)(basis_2d(t.basis, t.pidx[2 * k], t.pidx[2 * k + 1], xq[0], xq[1]) - t.ipt[k]);
+                }
         } else {
             h_nb.assign(tiles * S * MR * TILE, 0);
             if (!gpu_lsq) {
@@ -374,10 +395,23 @@ void mgpu_ctx::build() {
                             double J[4], Ji[4];
                             tri_jacobian(w0, mv.node_coords + 2 * (size_t)nc[1], mv.node_coords + 2 * (size_t)nc[2], J);
                             mat2_inverse(J, Ji);
+                            uint32_t fcode = 0;
                             for (int fl = 0; fl < NF; ++fl) {
                                 const uint32_t f = mv.faces_of_cell[mv.offsets_faces_of_cell[o] + fl];
                                 const int side = mv.cells_of_face[2 * (size_t)f] == (int32_t)o ? 0 : 1;
                                 h_cface[(tile * NF + fl) * TILE + lane] = (uint32_t)face_new[f] * 2u + (uint32_t)side;
+                                int code = 0;
+                                if (f32) {
+                                    const uint32_t* fn = mv.nodes_of_face + mv.offsets_nodes_of_face[f];
+                                    int i0 = -1, i1 = -1;
+                                    for (int i = 0; i < 3; ++i) {
+                                        if (nc[i] == fn[0]) i0 = i;
+                                        if (nc[i] == fn[1]) i1 = i;
+                                    }
+                                    if (i0 < 0 || i1 < 0 || i0 == i1) throw Unsupported("a face is not an edge of its cell");
+                                    code = i1 == (i0 + 1) % 3 ? 2 * i0 : 2 * i0 + 1;
+                                    fcode |= (uint32_t)code << (3 * fl);
+                                }
                                 const double* p0 = mv.node_coords + 2 * (size_t)mv.nodes_of_face[mv.offsets_nodes_of_face[f]];
                                 const double* p1 = mv.node_coords + 2 * (size_t)mv.nodes_of_face[mv.offsets_nodes_of_face[f] + 1];
                                 double x0[2], x1[2];
@@ -395,14 +429,18 @@ void mgpu_ctx::build() {
                                         const double shape = cfg.teno_variant == MGPU_TENO_CORRECTED ? b - t.ipt[k]
                                                                                                    : b + (t.ipt[k] / area0);
                                         if (f32) {
-                                            const size_t e = ((size_t)fl * nq + q) * KR + (k - 1);
-                                            h_phi4[at4(tile * GF + e / 4, lane, e % 4)] = (float)shape;
+                                            // the cell's own shape against its code's table entry
+                                            const float own = (float)shape;
+                                            const float tab = h_tab[(size_t)code * GT * 4 + (size_t)q * KR + (k - 1)];
+                                            if (!(std::fabs(own - tab) <= 1e-5f * (1.0f + std::fabs(tab))))
+                                                throw Unsupported("face shapes of a cell differ from its reference edge's");
                                         } else {
                                             h_phi[(((tile * NF + fl) * nq + q) * KR + (k - 1)) * TILE + lane] = shape;
                                         }
                                     }
                                 }
                             }
+                            if (f32) h_fcode[c] = (uint16_t)fcode;
                         }
                     }
                     h_sm[c] = sm;
@@ -425,7 +463,10 @@ void mgpu_ctx::build() {
             nb4.upload(h_nb4);
             if (gpu_lsq) P4.alloc(tiles * S * GP * TILE * 4);
             else P4.upload(h_P4);
-            phi4.upload(h_phi4);
+            fcode.upload(h_fcode);
+            std::vector<float4> tab4(8 * GT);
+            std::memcpy(tab4.data(), h_tab.data(), h_tab.size() * sizeof(float));
+            phi_tab4.upload(tab4);
         } else {
             nb.upload(h_nb);
             if (gpu_lsq) {
@@ -448,15 +489,18 @@ void mgpu_ctx::build() {
         teno.phi = phi.p;
         teno.nb4 = nb4.p;
         teno.P4 = P4.p;
-        teno.phi4 = phi4.p;
+        teno.fcode = fcode.p;
+        teno.phi_tab4 = phi_tab4.p;
         teno.cface = cface.p;
         teno.smask = smask.p;
-        // compulsory bytes of one reconstruction launch: tables, shapes, face
-        // slots, the state gathered once per cell, face states written
+        // compulsory bytes of one reconstruction launch: tables, shapes (the
+        // FP32 form: a 2-byte code per cell), face slots, the state gathered
+        // once per cell, face states written
         double tb = 0;
         const double per_row = f32 ? 4 + 4.0 * KR : 4 + 8 + 8.0 * KR, fw = f32 ? 4 : 8;
         for (uint32_t c = 0; c < N; ++c) tb += __builtin_popcount(h_sm[c]) * (double)MR * per_row;
-        recon_bytes = tb + (double)N * (NF * nq * KR * fw + NF * 4 + 1 + 32) + (double)N * NF * nq * 4 * fw;
+        const double shapes = f32 ? 2.0 : NF * nq * KR * fw;
+        recon_bytes = tb + (double)N * (shapes + NF * 4 + 1 + 32) + (double)N * NF * nq * 4 * fw;
     } else {
         recon_bytes = (double)F_flux * (8 + 64) + (double)N * 32;
     }
@@ -1053,7 +1097,7 @@ int mgpu_get_table(mgpu_ctx* ctx, int field, void* dst, uint64_t* bytes) {
             case MGPU_TABLE_NB: src = ctx->nb.p; n = ctx->nb.bytes(); break;
             case MGPU_TABLE_NB32: src = ctx->nb4.p; n = ctx->nb4.bytes(); break;
             case MGPU_TABLE_PHI: src = ctx->phi.p; n = ctx->phi.bytes(); break;
-            case MGPU_TABLE_PHI32: src = ctx->phi4.p; n = ctx->phi4.bytes(); break;
+            case MGPU_TABLE_PHI32: src = ctx->fcode.p; n = ctx->fcode.bytes(); break;
             default: throw ArgFail("unknown table");
         }
         if (!src) throw ArgFail("this form holds no such table");

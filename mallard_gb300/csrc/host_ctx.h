@@ -115,7 +115,9 @@ struct mgpu_ctx {
     DevArray<uint32_t> nb, cface;
     DevArray<double> ar, P, phi;
     DevArray<uint32_t> nb4;
-    DevArray<float> P4, phi4;
+    DevArray<float> P4;
+    DevArray<uint16_t> fcode;   // FP32 form: face-shape code per cell (3 bits per face slot)
+    DevArray<float4> phi_tab4;  // FP32 form: the 8 code slots' shape sets
     DevArray<uint8_t> smask, masks;
     DevArray<double> staging;      // caller-order rows for state transfers
     DevArray<uint32_t> perm_old;   // internal cell -> caller cell

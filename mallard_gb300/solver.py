@@ -316,7 +316,7 @@ class Solver:
         return dict(zip(self.BUILD_PHASES, t.tolist()))
 
     TABLES = {"P": (0, np.float64), "areas": (1, np.float64), "P32": (2, np.float32), "nb": (3, np.uint32),
-              "nb32": (4, np.uint32), "phi": (5, np.float64), "phi32": (6, np.float32)}
+              "nb32": (4, np.uint32), "phi": (5, np.float64), "phi32": (6, np.uint16)}
 
     def get_table(self, name):
         """One reconstruction table as the kernels read it (tiled layout,
