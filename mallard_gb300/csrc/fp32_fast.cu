@@ -2,15 +2,15 @@
 //
 // Arithmetic split (everything else stays FP64):
 //  * FP32: TENO coefficients, smoothness indicators, stencil selection, face
-//    evaluation, face states, primitive recovery, Riemann flux;
+//    evaluation, face states, primitive recovery, Riemann flux, viscous
+//    terms (and, in spectral32.cuh, the time step's spectral radius);
 //  * FP64: the table build (least squares, face shapes; the tables are
-//    rounded to FP32 once, on upload), geometry (normals, areas,
-//    volumes), the conserved state and its accumulation across RK stages
-//    (the update kernel also writes an FP32 copy of each stage's state,
-//    which the reconstruction gathers)
-//    (the FP64 update kernel), and primitive recovery near vacuum: when the
-//    internal energy is under 1e-3 of the total the face state is recovered
-//    in FP64.
+//    rounded to FP32 once, on upload), geometry (normals, areas, volumes),
+//    the conserved state and its accumulation across RK stages in the
+//    update kernel (which also writes an FP32 copy of each stage's state for
+//    the reconstruction to gather), and primitive recovery near vacuum: when
+//    the internal energy is under 1e-3 of the total the face state is
+//    recovered in FP64.
 // Stencil selection uses ratios of smoothness indicators: (SI+eps)^-6 itself
 // overflows FP32, but w_s / sum w = 1 / sum_d ((SI_s+eps)/(SI_d+eps))^6 does
 // not.  Only the corrected weighting is built in this form.
@@ -260,7 +260,8 @@ __global__ void __launch_bounds__(BS, MINB) teno32_kernel(const TenoArgs a, cons
 // Staged form: each warp (one 8-cell tile) copies the table blocks of the
 // stencils its cells evaluate into shared memory with cp.async.bulk, NSLOT
 // stencils at a time (a slot is refilled with the next stencil as soon as
-// the warp is done with it), and the face shapes into a slot of their own;
+// the warp is done with it), and the tile's face-shape codes (16 bytes)
+// into a slot of their own;
 // an mbarrier per slot tracks the bytes.  One bulk copy replaces the dozens
 // of dependent table loads of the direct form, so the warp's table traffic
 // is in flight at once while it gathers the neighbours' states.
