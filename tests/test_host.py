@@ -239,3 +239,42 @@ def test_initial_state_matches_reference_formulas():
     assert np.allclose(Uc[:, 1] / Uc[:, 0], 600.0)
     with pytest.raises(RuntimeError, match="Missing T"):
         initial_state(m, {"type": "constant", "u": [1.0, 0.0], "p": 1.0}, gas)
+
+
+@pytest.mark.parametrize("which", ["cartesian_tri", "permuted", "ramp"])
+def test_face_points_sit_on_reference_edges(which):
+    """The FP32 form stores a 3-bit code per face slot instead of per-cell
+    face shapes: mapped into its triangle's reference frame (nodes 0, 1, 2 at
+    (0,0), (1,0), (0,1)), a face's Gauss points are those of the reference
+    edge from node i0 to node i1, so six shape sets serve every cell.  Check
+    that premise on the meshes the tests and benchmark use: every face of a
+    cell joins two of its nodes, and the mapped points match the edge's."""
+    if which == "ramp":
+        m = mg.Mesh.ramp_channel(45, 15, 3.0, 1.0, 0.5, 15.0, 0.2, seed=7)
+    else:
+        m = mg.Mesh.generate("cartesian_tri", 17, 13, 1.0, 1.0)
+        if which == "permuted":
+            m.permute_cells(5)
+    ref = np.array([[0.0, 0.0], [1.0, 0.0], [0.0, 1.0]])
+    gl = np.array([-1.0, 1.0]) / np.sqrt(3.0)  # two-point Gauss-Legendre on [-1, 1]
+    X = m.node_coords
+    codes = np.zeros(6, dtype=int)
+    worst = 0.0
+    for c in range(m.n_cells):
+        nc = m.nodes_of_cell[m.offsets_nodes_of_cell[c]:m.offsets_nodes_of_cell[c + 1]]
+        assert len(nc) == 3
+        J = np.column_stack((X[nc[1]] - X[nc[0]], X[nc[2]] - X[nc[0]]))
+        Ji = np.linalg.inv(J)
+        for f in m.faces_of_cell[m.offsets_faces_of_cell[c]:m.offsets_faces_of_cell[c + 1]]:
+            fn = m.nodes_of_face[m.offsets_nodes_of_face[f]:m.offsets_nodes_of_face[f + 1]]
+            i0, i1 = int(np.flatnonzero(nc == fn[0])[0]), int(np.flatnonzero(nc == fn[1])[0])
+            assert i0 != i1
+            code = 2 * i0 if i1 == (i0 + 1) % 3 else 2 * i0 + 1
+            codes[code] += 1
+            x0, x1 = Ji @ (X[fn[0]] - X[nc[0]]), Ji @ (X[fn[1]] - X[nc[0]])
+            for t in (gl + 1.0) * 0.5:
+                mapped = x0 + t * (x1 - x0)
+                edge = ref[i0] + t * (ref[i1] - ref[i0])
+                worst = max(worst, np.abs(mapped - edge).max())
+    assert worst < 1e-12, worst
+    assert codes.sum() == 3 * m.n_cells
