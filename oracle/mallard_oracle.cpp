@@ -877,9 +877,17 @@ void star_anrs(const double* L, const double* R, double& ps, double& rls, double
     else star_tsrs(L, R, ps, rls, rrs);
 }
 
-// Rusanov / HLL / HLLC ::calc_flux (riemann_solver.h:331-519)
+// Rusanov / HLL / HLLC ::calc_flux (riemann_solver.h:331-519).
+// guard (the robust TENO variant): a star pressure that is not a number
+// counts as zero.  The reference's two-rarefaction estimate raises a
+// negative base to the power 2 gamma / (gamma - 1), which is not an exact
+// integer in floating point, when a strong expansion meets a near-vacuum
+// pressure; its NaN then reaches the wave speeds and the flux.  A zero star
+// pressure gives the same wave speeds as any star pressure below both
+// pressures, so the guard changes no flux that the reference computes as a
+// number.
 void riemann(int kind, double* F, const double* n, double rl, const double* ul, double pl, double gl, double hl,
-             double rr, const double* ur, double pr, double gr, double hr) {
+             double rr, const double* ur, double pr, double gr, double hr, bool guard = false) {
     double unl = ul[0] * n[0] + ul[1] * n[1];
     double unr = ur[0] * n[0] + ur[1] * n[1];
     double qql = ul[0] * ul[0] + ul[1] * ul[1];
@@ -900,6 +908,7 @@ void riemann(int kind, double* F, const double* n, double rl, const double* ul, 
     double Wl[4] = {rl, unl, pl, gl}, Wr[4] = {rr, unr, pr, gr};
     double ps, rls, rrs;
     star_anrs(Wl, Wr, ps, rls, rrs);
+    if (guard && !(ps == ps)) ps = 0.0;
     double ql = (ps <= pl) ? 1.0 : std::sqrt(1.0 + (gl + 1.0) / (2.0 * gl) * (ps / pl - 1.0));
     double qr = (ps <= pr) ? 1.0 : std::sqrt(1.0 + (gr + 1.0) / (2.0 * gr) * (ps / pr - 1.0));
     double Sl = unl - al * ql;
@@ -966,6 +975,13 @@ struct Case {
     //    Same decisions and same work per cell as variant 0.  The face flux
     //    then replaces a reconstructed face state whose density or pressure
     //    is not positive by the owning cell's average (first-order fallback).
+    // 2: robust: variant 1, then per cell (robust_cell below):
+    //    a cell with a boundary face takes its average at all its face
+    //    points; otherwise each variable's polynomial is scaled toward the
+    //    cell average so that its face values stay within the range of the
+    //    cell's central stencil, and if a face state is still not admissible
+    //    the cell takes its average at all its face points.  HLL/HLLC count a
+    //    star pressure that is not a number as zero (riemann, guard).
     int teno_variant = 0;
     int integrator = 0;  // 0 SSPRK3, 1 FE, 2 RK4 (time_integrator.h)
     std::vector<Bc> bcs;
@@ -994,6 +1010,62 @@ void recon_fo(Case& cs, const double* U, double* face) {
     }
 }
 
+bool admissible(const Gas& g, const double* W);
+
+// The robust variant's per-cell step after the TENO face values of all four
+// variables are known (no reference counterpart):
+//  1. a cell with a boundary face takes its average at every face point
+//     (its one-sided stencils, extrapolated onto transmissive boundaries,
+//     let a boundary mode grow);
+//  2. otherwise, per variable, the face-point deviations from the average
+//     d_p = w_p - u are scaled by one theta = min over the points of
+//     dhi / d_p (d_p > dhi) or dlo / d_p (d_p < dlo), where [dlo, dhi] is
+//     the range of the central stencil's averages minus u;
+//  3. if a face state is then not admissible (density and pressure
+//     positive), the cell takes its average at every face point.
+void robust_cell(Case& cs, uint32_t c, const double* U, double* face, const double* dlo, const double* dhi) {
+    const OMesh& m = *cs.mesh;
+    const int nq = cs.nq;
+    const uint32_t fo = m.off_foc[c];
+    const int nf = (int)(m.off_foc[c + 1] - fo);
+    auto at = [&](int fl, int q) -> double* {
+        const uint32_t f = m.foc[fo + fl];
+        const int side = m.cof[2 * (size_t)f] == (int32_t)c ? 0 : 1;
+        return &face[(((size_t)f * nq + q) * 2 + side) * NC];
+    };
+    bool first_order = false;
+    for (int fl = 0; fl < nf; fl++)
+        if (m.cof[2 * (size_t)m.foc[fo + fl] + 1] < 0) first_order = true;
+    if (!first_order) {
+        for (int v = 0; v < NC; ++v) {
+            const double u = U[(size_t)c * NC + v];
+            double th = 1.0;
+            for (int fl = 0; fl < nf; fl++)
+                for (int q = 0; q < nq; q++) {
+                    const double d = at(fl, q)[v] - u;
+                    if (d > dhi[v]) th = std::fmin(th, dhi[v] / d);
+                    else if (d < dlo[v]) th = std::fmin(th, dlo[v] / d);
+                }
+            if (th < 1.0)
+                for (int fl = 0; fl < nf; fl++)
+                    for (int q = 0; q < nq; q++) {
+                        double& w = at(fl, q)[v];
+                        w = u + th * (w - u);
+                    }
+        }
+        for (int fl = 0; fl < nf && !first_order; fl++)
+            for (int q = 0; q < nq; q++)
+                if (!admissible(cs.gas, at(fl, q))) {
+                    first_order = true;
+                    break;
+                }
+    }
+    if (first_order)
+        for (int fl = 0; fl < nf; fl++)
+            for (int q = 0; q < nq; q++)
+                for (int v = 0; v < NC; ++v) at(fl, q)[v] = U[(size_t)c * NC + v];
+}
+
 // TENOFunctor::operator() (face_reconstruction.cpp:866-1039)
 void recon_teno_cell(Case& cs, uint32_t c, const double* U, double* face) {
     const OMesh& m = *cs.mesh;
@@ -1004,6 +1076,9 @@ void recon_teno_cell(Case& cs, uint32_t c, const double* U, double* face) {
     uint32_t g0 = t.off_groups[c];
     int gs = (int)(t.off_groups[c + 1] - g0);
     std::vector<double> sw((size_t)gs * NC), dw((size_t)gs * K * NC);
+    // range of the central stencil around the cell average, per variable
+    // (the robust variant's bounds; the target cell itself gives 0)
+    double dlo[NC] = {0.0, 0.0, 0.0, 0.0}, dhi[NC] = {0.0, 0.0, 0.0, 0.0};
     const double* w0 = m.nc(m.node_of_cell(c, 0));
     double J[4], Ji[4];
     tri_jac(w0, m.nc(m.node_of_cell(c, 1)), m.nc(m.node_of_cell(c, 2)), J);
@@ -1020,8 +1095,14 @@ void recon_teno_cell(Case& cs, uint32_t c, const double* U, double* face) {
         std::vector<double> b((size_t)M * NC);
         for (int j = 0; j < M; ++j) {
             uint32_t nb = t.stencils[so + j];
-            for (int v = 0; v < NC; ++v)
-                b[(size_t)j * NC + v] = t.areas[so + j] * (U[(size_t)nb * NC + v] - U[(size_t)c * NC + v]);
+            for (int v = 0; v < NC; ++v) {
+                const double d = U[(size_t)nb * NC + v] - U[(size_t)c * NC + v];
+                b[(size_t)j * NC + v] = t.areas[so + j] * d;
+                if (sl == 0) {
+                    dlo[v] = std::fmin(dlo[v], d);
+                    dhi[v] = std::fmax(dhi[v], d);
+                }
+            }
         }
         double* a = &dw[(size_t)sl * K * NC];
         mm(&t.mats[mo], b.data(), a, K, M, NC);
@@ -1047,7 +1128,7 @@ void recon_teno_cell(Case& cs, uint32_t c, const double* U, double* face) {
                     sw[(size_t)sl * NC + v] = (1.0 / K);
                     mask |= (uint8_t)(1u << sl);
                 }
-            if (cs.teno_variant == 1) {
+            if (cs.teno_variant >= 1) {
                 sw[v] = 0.0;
                 for (int sl = 1; sl < gs; ++sl)
                     if (!(mask & (1u << sl))) sw[(size_t)sl * NC + v] = 0.0;
@@ -1076,13 +1157,14 @@ void recon_teno_cell(Case& cs, uint32_t c, const double* U, double* face) {
                     uint32_t so = t.off_stencils[g0 + sl];
                     for (int k = 0; k < K; k++) {
                         double phi = basis2(t.basis, t.pidx[2 * k], t.pidx[2 * k + 1], xq[0], xq[1]);
-                        double shape = cs.teno_variant == 1 ? phi - t.ipt[k] : phi + (t.ipt[k] / t.areas[so]);
+                        double shape = cs.teno_variant >= 1 ? phi - t.ipt[k] : phi + (t.ipt[k] / t.areas[so]);
                         out += sw[(size_t)sl * NC + v] * dw[(size_t)sl * K * NC + (size_t)k * NC + v] * shape;
                     }
                 }
             }
         }
     }
+    if (cs.teno_variant == 2) robust_cell(cs, c, U, face, dlo, dhi);
 }
 
 void recon(Case& cs, const double* U, double* face) {
@@ -1161,7 +1243,7 @@ void lr_states(const Case& cs, int bc, const Bc* b, const double* face_q, const 
 // WallAdiabaticFluxFunctor::call_impl (boundary_wall_adiabatic.cpp:38-70).
 // Positivity fallback of the corrected TENO variant: a face state whose
 // density or pressure is not positive reverts to the cell average.
-inline bool admissible(const Gas& g, const double* W) {
+bool admissible(const Gas& g, const double* W) {
     double rho = W[0];
     if (!(rho > 0.0)) return false;
     double u0 = W[1] / rho, u1 = W[2] / rho;
@@ -1283,7 +1365,7 @@ void face_flux(Case& cs, uint32_t f, int bc, const Bc* b, const double* U, const
     for (int q = 0; q < cs.nq; q++) {
         const double* fq = &face[((size_t)f * cs.nq + q) * 2 * NC];
         double fix[2 * NC];
-        if (cs.recon == RECON_TENO && cs.teno_variant == 1) {
+        if (cs.recon == RECON_TENO && cs.teno_variant >= 1) {
             for (int i = 0; i < 2 * NC; i++) fix[i] = fq[i];
             for (int sd = 0; sd < 2; sd++) {
                 int32_t c = m.cof[2 * (size_t)f + sd];
@@ -1302,7 +1384,8 @@ void face_flux(Case& cs, uint32_t f, int bc, const Bc* b, const double* U, const
             Ft[3] = 0.0;
         } else {
             lr_states(cs, bc, b, fq, n, cl, cr, pl, pr);
-            riemann(cs.rsolver, Ft, n, cl[0], pl, pl[2], cs.gas.gamma, pl[4], cr[0], pr, pr[2], cs.gas.gamma, pr[4]);
+            riemann(cs.rsolver, Ft, n, cl[0], pl, pl[2], cs.gas.gamma, pl[4], cr[0], pr, pr[2], cs.gas.gamma, pr[4],
+                    cs.teno_variant == 2);
         }
         for (int i = 0; i < NC; i++) F[i] += cs.qface.wts[q] * Ft[i];
     }

@@ -181,7 +181,9 @@ class OracleCase:
             raise RuntimeError(_err(self._lib))
 
     def set_teno_variant(self, variant):
-        """0: the reference's weighting; 1: cut-off weighting (see the C source)."""
+        """0: the reference's weighting; 1: cut-off weighting; 2: robust (cut-off
+        weighting, first-order boundary cells, range scaling and positivity
+        fallback per cell, guarded star pressure); see the C source."""
         self._lib.orc_case_set_teno_variant(self.h, int(variant))
 
     def set_integrator(self, name):

@@ -104,7 +104,7 @@ def make_pair(mesh, recon="TENO", riemann="HLLC", variant="reference", bcs=None,
     om = OracleMesh.from_arrays(mesh)
     oc = OracleCase(om, recon=recon, basis="legendre", poly_order=poly_order, riemann=riemann, p_min=p_min,
                     p_max=p_max, **GAS)
-    oc.set_teno_variant(0 if variant == "reference" else 1)
+    oc.set_teno_variant({"reference": 0, "corrected": 1, "robust": 2}[variant])
     oc.set_integrator(integrator)
     for b in blist:
         data = ()
