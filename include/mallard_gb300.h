@@ -254,21 +254,28 @@ int mgpu_run(mgpu_ctx* ctx, double cfl, uint32_t n_steps, double* t_out);
  * a bounded device wait ran out (MGPU_ERR_TIMEOUT). */
 int mgpu_status(mgpu_ctx* ctx, uint32_t* flags);
 
-/* The CFL time step of the resident state (as mgpu_calc_dt) for callers
- * that cannot allocate device memory while they step: code that captures its
- * time loop into a CUDA graph (no allocation during capture), code whose
- * device memory comes from its own allocator or a fixed pool, real-time
- * loops.  This entry point has no counterpart in the reference.
+/* The CFL time step of the resident state, as mgpu_calc_dt computes it, for
+ * callers that must not allocate device memory once they are stepping: a
+ * host application whose device memory all comes from its own pool or
+ * arena, or a real-time loop that cannot afford the device-wide
+ * synchronisation of cudaMalloc/cudaFree.  This entry point has no
+ * counterpart in the reference.
  *   dt_device               device pointer to one double (caller-owned): dt
  *   spectral_radius_device  optional device array [n_cells] in the caller's
  *                           cell order: per-cell spectral radius (the
  *                           reference's cfl_local before its scaling by dt)
  * Enqueued on the context's stream; it does not synchronise.  It calls no
  * cudaMalloc/cudaFree: its reduction scratch is a static device array of
- * 512 KiB (one partial per 256 cells), so meshes above 16,777,216 cells are
- * rejected with MGPU_ERR_ARG.  The first call on each device looks up that
- * array's address, so make it before any stream capture.  Calls share the
- * array: calls that overlap on the GPU race. */
+ * 512 KiB (one partial per 256 cells), so empty meshes and meshes above
+ * 16,777,216 cells are rejected with MGPU_ERR_ARG.  The first call on each
+ * device looks up that array's device address (with the context's device
+ * current), so make that first call before any stream capture.  The
+ * caller's current device is restored on return.  Calls share the array:
+ * calls that overlap on the GPU race.  A dt that is not finite and
+ * non-negative sets bit 1 of mgpu_status.  The plain FP64 and the FP32 forms
+ * give mgpu_calc_dt's values bit for bit; on the FP64-fast form (which
+ * mgpu_calc_dt evaluates with reciprocals and FMA) they agree to 1e-12
+ * relative. */
 int mgpu_calc_dt_noalloc(mgpu_ctx* ctx, double cfl, double* dt_device, double* spectral_radius_device);
 
 /* ---- learned TENO stencil selector ------------------------------------

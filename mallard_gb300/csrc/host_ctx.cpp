@@ -1182,8 +1182,9 @@ namespace mgpu {
 
 // The spectral-radius inputs of a finalized context, for entry points that
 // live in other translation units (noalloc.cu).  Allocates nothing.
-bool ctx_spectral_view(mgpu_ctx* ctx, SpecArgs* s, const uint32_t** cell_old, cudaStream_t* stream, int* device) {
-    if (!ctx || !ctx->finalized || !s || !cell_old || !stream || !device) return false;
+bool ctx_spectral_view(mgpu_ctx* ctx, SpecArgs* s, const uint32_t** cell_old, cudaStream_t* stream, int* device,
+                       unsigned** flags) {
+    if (!ctx || !ctx->finalized || !s || !cell_old || !stream || !device || !flags) return false;
     *s = SpecArgs{};
     s->n_cells = (int)ctx->N;
     s->cfaces = ctx->cfaces.p;
@@ -1196,6 +1197,7 @@ bool ctx_spectral_view(mgpu_ctx* ctx, SpecArgs* s, const uint32_t** cell_old, cu
     *cell_old = ctx->perm_old.p;
     *stream = ctx->stream;
     *device = ctx->cfg.device;
+    *flags = ctx->flags.p;
     return true;
 }
 

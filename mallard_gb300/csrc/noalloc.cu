@@ -1,11 +1,12 @@
 // noalloc.cu -- the CFL time step (spectral radius -> dt) without any device
 // allocation at call time.
 //
-// Who needs it: callers that cannot call cudaMalloc while they step, e.g.
-// code that records the whole time loop into a CUDA graph (allocation is not
-// allowed during stream capture), callers whose device memory belongs to
-// another allocator or a pre-sized pool, and real-time loops that must not
-// touch the allocator.  Such callers create their context once at start-up
+// Who needs it: callers that must not call cudaMalloc/cudaFree once they are
+// stepping.  A host application that owns all device memory through its own
+// pool or arena (so that a library allocating on its own would fragment the
+// pool or overrun the budget it planned), and real-time loops, where the
+// implicit device synchronisation of cudaMalloc/cudaFree would stall every
+// stream, are two such callers.  They create their context once at start-up
 // (which does allocate) and then call mgpu_calc_dt_noalloc every step with
 // their own output buffers.
 //
@@ -24,7 +25,8 @@
 
 namespace mgpu {
 // Defined in host_ctx.cpp: the context's spectral-radius inputs.
-bool ctx_spectral_view(mgpu_ctx* ctx, SpecArgs* a, const uint32_t** cell_old, cudaStream_t* stream, int* device);
+bool ctx_spectral_view(mgpu_ctx* ctx, SpecArgs* a, const uint32_t** cell_old, cudaStream_t* stream, int* device,
+                       unsigned** flags);
 }  // namespace mgpu
 
 namespace {
@@ -108,10 +110,13 @@ __global__ void __launch_bounds__(kBlock) spectral_partial_kernel(const mgpu::Sp
     }
 }
 
-// One block: the maximum over the used partial slots, then dt = cfl / max.
+// One block: the maximum over the used partial slots, then dt = cfl / max;
+// a dt that is not a finite non-negative number sets bit 1 of the context's
+// status word, as the main path's time-step kernel does.
 __global__ void __launch_bounds__(1024) dt_from_partials_kernel(const unsigned long long* __restrict__ partial,
                                                                 int n_partials, double cfl,
-                                                                double* __restrict__ dt_out) {
+                                                                double* __restrict__ dt_out,
+                                                                unsigned* __restrict__ flags) {
     unsigned long long bits = 0ull;
     for (int i = threadIdx.x; i < n_partials; i += blockDim.x) {
         const unsigned long long v = partial[i];
@@ -132,7 +137,11 @@ __global__ void __launch_bounds__(1024) dt_from_partials_kernel(const unsigned l
             const unsigned long long other = __shfl_xor_sync(0xffffffffu, bits, o);
             bits = other > bits ? other : bits;
         }
-        if (threadIdx.x == 0) *dt_out = cfl / __longlong_as_double((long long)bits);
+        if (threadIdx.x == 0) {
+            const double d = cfl / __longlong_as_double((long long)bits);
+            *dt_out = d;
+            if (!(d >= 0.0) || !isfinite(d)) atomicOr(flags, 2u);
+        }
     }
 }
 
@@ -157,14 +166,19 @@ extern "C" int mgpu_calc_dt_noalloc(mgpu_ctx* ctx, double cfl, double* dt_device
     mgpu::SpecArgs a{};
     const uint32_t* cell_old = nullptr;
     cudaStream_t stream = nullptr;
+    unsigned* flags = nullptr;
     int device = 0;
     if (!ctx || !dt_device) {
         mgpu::set_error("mgpu_calc_dt_noalloc: null argument");
         return MGPU_ERR_ARG;
     }
-    if (!mgpu::ctx_spectral_view(ctx, &a, &cell_old, &stream, &device)) {
+    if (!mgpu::ctx_spectral_view(ctx, &a, &cell_old, &stream, &device, &flags)) {
         mgpu::set_error("mgpu_calc_dt_noalloc: context not finalized");
         return MGPU_ERR_STATE;
+    }
+    if (a.n_cells <= 0) {
+        mgpu::set_error("mgpu_calc_dt_noalloc: the mesh has no cells");
+        return MGPU_ERR_ARG;
     }
     const long long blocks = ((long long)a.n_cells + kBlock - 1) / kBlock;
     if (blocks > kMaxBlocks) {
@@ -173,10 +187,13 @@ extern "C" int mgpu_calc_dt_noalloc(mgpu_ctx* ctx, double cfl, double* dt_device
                         " (use mgpu_calc_dt)");
         return MGPU_ERR_ARG;
     }
-    cudaError_t e = cudaSetDevice(device);
+    // work on the context's device, then give the caller back its own
+    int caller_device = -1;
+    cudaError_t e = cudaGetDevice(&caller_device);
+    if (e == cudaSuccess) e = cudaSetDevice(device);
     unsigned long long* partial = nullptr;
     if (e == cudaSuccess) e = partial_scratch(device, &partial);
-    if (e == cudaSuccess && blocks > 0) {
+    if (e == cudaSuccess) {
         if (a.u32)
             spectral_partial_kernel<true><<<(unsigned)blocks, kBlock, 0, stream>>>(a, partial, spectral_radius_device,
                                                                                   cell_old);
@@ -185,9 +202,13 @@ extern "C" int mgpu_calc_dt_noalloc(mgpu_ctx* ctx, double cfl, double* dt_device
                                                                                    cell_old);
         e = cudaGetLastError();
         if (e == cudaSuccess) {
-            dt_from_partials_kernel<<<1, 1024, 0, stream>>>(partial, (int)blocks, cfl, dt_device);
+            dt_from_partials_kernel<<<1, 1024, 0, stream>>>(partial, (int)blocks, cfl, dt_device, flags);
             e = cudaGetLastError();
         }
+    }
+    if (caller_device >= 0 && caller_device != device) {
+        const cudaError_t r = cudaSetDevice(caller_device);
+        if (e == cudaSuccess) e = r;
     }
     if (e != cudaSuccess) {
         mgpu::set_error(std::string("mgpu_calc_dt_noalloc: ") + cudaGetErrorString(e));

@@ -85,3 +85,46 @@ def test_calc_dt_noalloc_after_a_larger_mesh():
         s.synchronize()
         assert abs(float(dt_dev.cpu().numpy()[0]) - dt_ref) <= TOL * abs(dt_ref)
         s.close()
+
+
+def test_calc_dt_noalloc_fp64_fast_form():
+    """The FP64-fast form: mgpu_calc_dt uses reciprocals and FMA there, this
+    entry point the plain divisions, so the two agree to 1e-12, not bit for
+    bit."""
+    torch = pytest.importorskip("torch")
+    m = mg.Mesh.generate("cartesian_tri", 40, 40, 1.0, 1.0)
+    m.permute_cells(5)
+    s = mg.Solver(m, teno_variant="corrected", precision="fp64_fast",
+                  boundaries=[{"name": z, "type": "extrapolation"} for z in ("right", "top", "left", "bottom")])
+    U, W = four_quadrant(m)
+    s.set_state(U, W)
+    lib = N.lib()
+    dt_dev = torch.full((1,), -1.0, dtype=torch.float64, device="cuda")
+    for call in range(2):
+        dt_ref, _ = s.calc_dt(0.5)
+        N.check(lib.mgpu_calc_dt_noalloc(s._h, 0.5, _dev_ptr(dt_dev), None))
+        s.synchronize()
+        dt = float(dt_dev.cpu().numpy()[0])
+        assert abs(dt - dt_ref) <= TOL * abs(dt_ref), (call, dt, dt_ref)
+        s.take_step(dt_ref)
+    s.close()
+
+
+def test_calc_dt_noalloc_flags_a_nan_state():
+    """A non-finite cell gives a non-finite dt, which the status word reports
+    (bit 1), as it does for the main path's time step."""
+    torch = pytest.importorskip("torch")
+    m = mg.Mesh.generate("cartesian_tri", 16, 16, 1.0, 1.0)
+    s = mg.Solver(m, teno_variant="corrected",
+                  boundaries=[{"name": z, "type": "extrapolation"} for z in ("right", "top", "left", "bottom")])
+    U, W = four_quadrant(m)
+    U[7, :] = np.nan
+    W[7, :] = np.nan
+    s.set_state(U, W)
+    assert s.status() == 0
+    dt_dev = torch.zeros(1, dtype=torch.float64, device="cuda")
+    N.check(N.lib().mgpu_calc_dt_noalloc(s._h, 0.5, _dev_ptr(dt_dev), None))
+    s.synchronize()
+    assert not np.isfinite(float(dt_dev.cpu().numpy()[0])) or float(dt_dev.cpu().numpy()[0]) < 0
+    assert s.status() & 2
+    s.close()
