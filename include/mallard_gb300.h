@@ -78,8 +78,18 @@ enum {
 };
 /* TENO weighting: 0 = the reference's arithmetic, quirks included;
  * 1 = corrected cut-off weights, zero-mean evaluation basis and a
- * positivity fallback in the face flux (same work per cell). */
-enum { MGPU_TENO_REFERENCE = 0, MGPU_TENO_CORRECTED = 1 };
+ * positivity fallback in the face flux (same work per cell);
+ * 2 = robust: the corrected weighting, then per cell: a cell with a
+ * boundary face takes its average at all its face points; otherwise each
+ * variable's face values are scaled toward the cell average into the range
+ * of the cell's central stencil, and a cell whose face states are then not
+ * all admissible (density and pressure positive) takes its average at all
+ * its face points.  HLL and HLLC count a star pressure that is not a
+ * number (the reference's two-rarefaction estimate under a strong
+ * expansion next to near-vacuum pressure) as zero.  No reference
+ * counterpart; it runs the four-quadrant and random-ensemble workloads to
+ * their end times. */
+enum { MGPU_TENO_REFERENCE = 0, MGPU_TENO_CORRECTED = 1, MGPU_TENO_ROBUST = 2 };
 /* Arithmetic of the GPU path.
  * FP64      : FP64 with the reference's rounding (no FMA contraction, the
  *             reference's operation order); bit-identical to the reference's
@@ -87,7 +97,7 @@ enum { MGPU_TENO_REFERENCE = 0, MGPU_TENO_CORRECTED = 1 };
  * FP64_FAST : FP64 with FMA contraction and reduced-instruction forms of the
  *             smoothness indicator and x^6; agrees to ~1e-15 relative.
  * FP32      : reconstruction and face flux in FP32 (TENO with the corrected
- *             weighting only); tables, geometry, the conserved state and its
+ *             or robust weighting only); tables, geometry, the conserved state and its
  *             RK accumulation stay FP64, and face states near vacuum are
  *             recovered in FP64. */
 enum { MGPU_PREC_FP64 = 0, MGPU_PREC_FP64_FAST = 1, MGPU_PREC_FP32 = 2 };
@@ -447,7 +457,10 @@ uint32_t mgpu_n_cells(const mgpu_ctx* ctx);
 
 /* ---- unit-level GPU entry points (known-answer tests) ------------------ */
 /* n independent Riemann problems; arrays: n_unit [n][2], u_l/u_r [n][2],
- * scalars [n]; flux [n][4].  Host buffers. */
+ * scalars [n]; flux [n][4].  Host buffers.  solver: MGPU_RIEMANN_*, with
+ * MGPU_RIEMANN_GUARD or'ed in for the robust variant's guarded star
+ * pressure (a NaN star pressure counts as zero). */
+#define MGPU_RIEMANN_GUARD 16
 int mgpu_riemann_flux_batch(int solver, uint32_t n, const double* n_unit, const double* rho_l, const double* u_l,
                             const double* p_l, const double* gamma_l, const double* h_l, const double* rho_r,
                             const double* u_r, const double* p_r, const double* gamma_r, const double* h_r,

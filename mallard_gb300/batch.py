@@ -9,7 +9,8 @@ together by one launch per kernel (no counterpart in the reference).
     U, W = b.get_state(0, 5)
 
 Each mesh's TENO tables and face geometry are built once and shared by its
-cases; every case has its own time step.  FP32 form of corrected TENO, p = 3.
+cases; every case has its own time step.  FP32 form of corrected (or
+robust) TENO, p = 3.
 """
 
 import ctypes as C
@@ -21,7 +22,7 @@ from . import _native as N
 
 class Batch:
     def __init__(self, meshes, cases_per_group, boundaries=(), riemann_solver="HLLC", gamma=1.4, p_ref=101325.0,
-                 T_ref=298.15, rho_ref=1.225, device=0):
+                 T_ref=298.15, rho_ref=1.225, device=0, teno_variant="corrected"):
         self._lib = N.lib()
         self.meshes = list(meshes)
         self.C = [int(c) for c in cases_per_group]
@@ -29,7 +30,7 @@ class Batch:
         self._lib.mgpu_config_defaults(C.byref(cfg))
         cfg.riemann_solver = N.RIEMANN[riemann_solver]
         cfg.gamma, cfg.p_ref, cfg.T_ref, cfg.rho_ref = gamma, p_ref, T_ref, rho_ref
-        cfg.teno_variant = N.TENO_VARIANTS["corrected"]
+        cfg.teno_variant = N.TENO_VARIANTS[teno_variant]
         cfg.precision = N.PRECISIONS["fp32"]
         cfg.device = int(device)
         self._views = [m.view() for m in self.meshes]

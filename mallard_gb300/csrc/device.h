@@ -65,6 +65,10 @@ struct TenoArgs {
     double oi2[KR_MAX * KR_MAX];  // same, upper triangle with doubled off-diagonals (fast form)
     float oi2f[KR_MAX * KR_MAX];  // oi2 in FP32 (FP32-bulk form)
     unsigned* err;                // status word: bit 2 when a bounded wait ran out (staged FP32 form)
+    // robust TENO variant: per cell 1 if it has a boundary face; gamma - 1
+    const uint8_t* bcell;         // null unless the variant is MGPU_TENO_ROBUST
+    double gm1;
+    float gm1f;
 };
 
 struct FluxArgs {
@@ -78,6 +82,7 @@ struct FluxArgs {
     const double* U;        // stage input, for the positivity fallback
     double qw[4];           // face quadrature weights
     float qw_f[4];          // the same rounded to FP32 (FP32 form)
+    int guard;              // robust TENO variant: a NaN star pressure counts as zero (HLL, HLLC)
 };
 
 struct UpdateArgs {

@@ -79,6 +79,52 @@ struct GlobalSrc {
     __device__ __forceinline__ T ld(const T* p) const { return __ldg(p); }
 };
 
+// The robust variant's per-cell step in FP32 (teno_flux.cuh's robust_cell):
+// a cell with a boundary face takes its average at every face point;
+// otherwise each variable's deviations are scaled into the central
+// stencil's range [dlo, dhi] (when that stencil was evaluated), and a cell
+// with a face state that is then not admissible takes its average at every
+// face point.  Every lane of live calls it (the cell's four lanes exchange
+// their variables).
+template <int NF, int NQ>
+__device__ __forceinline__ void robust_cell32(const TenoArgs& a, bool boundary, bool have_range, unsigned live,
+                                              float uc, float dlo, float dhi, float (&out)[NF][NQ]) {
+    if (!boundary && have_range) {
+        float th = 1.0f;
+#pragma unroll
+        for (int fl = 0; fl < NF; ++fl)
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) {
+                const float d = out[fl][q] - uc;
+                if (d > dhi) th = fminf(th, dhi / d);
+                else if (d < dlo) th = fminf(th, dlo / d);
+            }
+        if (th < 1.0f)
+#pragma unroll
+            for (int fl = 0; fl < NF; ++fl)
+#pragma unroll
+                for (int q = 0; q < NQ; ++q) out[fl][q] = fmaf(th, out[fl][q] - uc, uc);
+    }
+    bool bad = boundary;
+#pragma unroll
+    for (int fl = 0; fl < NF; ++fl)
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+            const float rho = __shfl_sync(live, out[fl][q], 0, 4);
+            const float m0 = __shfl_sync(live, out[fl][q], 1, 4);
+            const float m1 = __shfl_sync(live, out[fl][q], 2, 4);
+            const float E = __shfl_sync(live, out[fl][q], 3, 4);
+            const float ir = 1.0f / rho;
+            const float ke = 0.5f * (m0 * m0 + m1 * m1) * ir;
+            if (!(rho > 0.0f) || !(a.gm1f * (E - ke) > 0.0f)) bad = true;
+        }
+    if (bad)
+#pragma unroll
+        for (int fl = 0; fl < NF; ++fl)
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) out[fl][q] = uc;
+}
+
 // Reconstruction of variable v of one cell.  live: lanes of the warp whose
 // cells exist (the four lanes of a cell share its fate).  src: where the
 // tile's table blocks are read (GlobalSrc, or shared memory filled by bulk
@@ -111,6 +157,8 @@ __device__ __forceinline__ bool teno32_cell(const TenoArgs& a, const float* __re
     bool ok = true;
     float coef[S][KR];
     float x[S];
+    float dlo = 0.0f, dhi = 0.0f;  // robust variant: central-stencil range around uc
+    bool have_range = false;
 #pragma unroll
     for (int s = 0; s < S; ++s) {
 #pragma unroll
@@ -129,6 +177,14 @@ __device__ __forceinline__ bool teno32_cell(const TenoArgs& a, const float* __re
 #pragma unroll
                 for (int e = 0; e < 4; ++e)
                     if (g * 4 + e < MR) d[g * 4 + e] = __ldg(U + ix.u(id[e]) * NC + v) - uc;
+            }
+            if (s == 0 && a.bcell) {
+#pragma unroll
+                for (int j = 0; j < MR; ++j) {
+                    dlo = fminf(dlo, d[j]);
+                    dhi = fmaxf(dhi, d[j]);
+                }
+                have_range = true;
             }
             // coefficients = (P x areas) . d, accumulated over the stencil in order
             const float4* Pp = src.P(s) + lane;
@@ -215,15 +271,20 @@ __device__ __forceinline__ bool teno32_cell(const TenoArgs& a, const float* __re
     }
 
     // face values: the shapes of each face slot's code (a 3-bit index into
-    // the shared table: always in bounds), then one dot product per point
+    // the shared table: always in bounds), then one dot product per point.
+    // The robust variant's per-cell step needs every lane of the live mask
+    // (its four lanes per cell exchange their variables), so a lane with
+    // nothing to write still computes (on code 0) and takes part.
     const uint16_t* codes = src.codes();
-    if (!codes || !ok || !alive) return false;
-    const unsigned code = src.ld(codes + lane);
+    const bool fine = codes && ok && alive;
+    const bool robust = a.bcell != nullptr;
+    if (!fine && !robust) return false;
+    const unsigned code = fine ? src.ld(codes + lane) : 0u;
+    float outv[NF][NQ];
+    uint32_t slots[NF];
 #pragma unroll
     for (int fl = 0; fl < NF; ++fl) {
-        const uint32_t slot = __ldg(a.cface + ((size_t)tile * NF + fl) * TILE + lane);
-        const size_t fi = slot >> 1;
-        const unsigned side = slot & 1u;
+        slots[fl] = fine ? __ldg(a.cface + ((size_t)tile * NF + fl) * TILE + lane) : 0u;
         const float4* t4 = a.phi_tab4 + ((code >> (3 * fl)) & 7u) * GT;
         float phi[GT * 4];
 #pragma unroll
@@ -239,8 +300,17 @@ __device__ __forceinline__ bool teno32_cell(const TenoArgs& a, const float* __re
             float out = uc;
 #pragma unroll
             for (int k = 0; k < KR; ++k) out = fmaf(c[k], phi[q * KR + k], out);
-            fv[((ix.f(fi) * NQ + q) * 2 + side) * NC + v] = out;
+            outv[fl][q] = out;
         }
+    }
+    if (robust) robust_cell32<NF, NQ>(a, fine && a.bcell[cell] != 0, have_range, live, uc, dlo, dhi, outv);
+    if (!fine) return false;
+#pragma unroll
+    for (int fl = 0; fl < NF; ++fl) {
+        const size_t fi = slots[fl] >> 1;
+        const unsigned side = slots[fl] & 1u;
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) fv[((ix.f(fi) * NQ + q) * 2 + side) * NC + v] = outv[fl][q];
     }
     return true;
 }
@@ -604,7 +674,7 @@ __device__ __forceinline__ void flux32_face(const FluxArgs& a, const float* __re
                 pr[3] = T;
                 pr[4] = e + po / rho;
             }
-            riemann<RS>(Ft, n, cl[0], pl, pl[2], gam, pl[4], cr[0], pr, pr[2], gam, pr[4]);
+            riemann<RS>(Ft, n, cl[0], pl, pl[2], gam, pl[4], cr[0], pr, pr[2], gam, pr[4], a.guard != 0);
         }
 #pragma unroll
         for (int i = 0; i < 4; i++) F[i] = fmaf(a.qw_f[q], Ft[i], F[i]);

@@ -97,8 +97,8 @@ int mgpu_batch_create(uint32_t n_groups, const mgpu_mesh* const* meshes, const u
         if (!meshes || !cases_per_group || !cfg) throw ArgFail("null argument");
         if (n_groups == 0 || n_groups > (uint32_t)MAX_GROUPS) throw ArgFail("1 to 8 mesh groups");
         if (cfg->precision != MGPU_PREC_FP32 || cfg->recon != MGPU_RECON_TENO || cfg->poly_order != 3 ||
-            cfg->teno_variant != MGPU_TENO_CORRECTED)
-            throw Unsupported("the batched form runs the FP32 form of corrected TENO at p = 3");
+            cfg->teno_variant == MGPU_TENO_REFERENCE)
+            throw Unsupported("the batched form runs the FP32 form of corrected or robust TENO at p = 3");
         if (cfg->time_integrator != MGPU_INTEGRATOR_SSPRK3) throw Unsupported("the batched form integrates with SSPRK3");
         if (cfg->viscous) throw Unsupported("the batched form is inviscid");
         std::unique_ptr<mgpu_batch> b(new mgpu_batch());
@@ -184,6 +184,7 @@ int mgpu_batch_finalize(mgpu_batch* b) {
             fa.nrm = c->nrm.p;
             fa.area = c->area.p;
             fa.bc = c->bcidx.p;
+            fa.guard = c->cfg.teno_variant == MGPU_TENO_ROBUST;
             for (int i = 0; i < 4; ++i) {
                 fa.qw[i] = c->qw[i];
                 fa.qw_f[i] = (float)c->qw[i];

@@ -426,7 +426,7 @@ void mgpu_ctx::build() {
                                     for (int i = 0; i < 2; i++) xq[i] = (qf.pts[q] + 1.0) * 0.5 * (x1[i] - x0[i]) + x0[i];
                                     for (int k = 1; k < K; ++k) {
                                         const double b = basis_2d(t.basis, t.pidx[2 * k], t.pidx[2 * k + 1], xq[0], xq[1]);
-                                        const double shape = cfg.teno_variant == MGPU_TENO_CORRECTED ? b - t.ipt[k]
+                                        const double shape = cfg.teno_variant != MGPU_TENO_REFERENCE ? b - t.ipt[k]
                                                                                                    : b + (t.ipt[k] / area0);
                                         if (f32) {
                                             // the cell's own shape against its code's table entry
@@ -483,6 +483,19 @@ void mgpu_ctx::build() {
         lap(4);
         cface.upload(h_cface);
         smask.upload(h_sm);
+        if (cfg.teno_variant == MGPU_TENO_ROBUST) {
+            // the robust variant's first-order cells: those with a boundary face
+            std::vector<uint8_t> h_bc(N, 0);
+            for (uint32_t c = 0; c < N; ++c) {
+                const uint32_t o = cell_old[c];
+                for (uint32_t k = mv.offsets_faces_of_cell[o]; k < mv.offsets_faces_of_cell[o + 1]; ++k)
+                    if (mv.cells_of_face[2 * (size_t)mv.faces_of_cell[k] + 1] < 0) h_bc[c] = 1;
+            }
+            bcell.upload(h_bc);
+            teno.bcell = bcell.p;
+        }
+        teno.gm1 = cfg.gamma - 1.0;
+        teno.gm1f = (float)(cfg.gamma - 1.0);
         teno.nb = nb.p;
         teno.ar = ar.p;
         teno.P = P.p;
@@ -675,9 +688,10 @@ int mgpu_create(const mgpu_mesh* mesh, const mgpu_config* cfg, mgpu_ctx** out) {
         if (cfg->viscous && !(cfg->mu_ref >= 0.0 && cfg->prandtl > 0.0 && (cfg->sutherland_S <= 0.0 || cfg->T_mu_ref > 0.0)))
             throw ArgFail("viscous flux: mu_ref >= 0, prandtl > 0 and, with Sutherland's law, T_mu_ref > 0");
         if (cfg->precision == MGPU_PREC_FP32 &&
-            (cfg->recon != MGPU_RECON_TENO || cfg->teno_variant != MGPU_TENO_CORRECTED))
-            throw Unsupported("the FP32 form implements TENO with the corrected weighting");
-        if (cfg->teno_variant != MGPU_TENO_REFERENCE && cfg->teno_variant != MGPU_TENO_CORRECTED)
+            (cfg->recon != MGPU_RECON_TENO || cfg->teno_variant == MGPU_TENO_REFERENCE))
+            throw Unsupported("the FP32 form implements TENO with the corrected or robust weighting");
+        if (cfg->teno_variant != MGPU_TENO_REFERENCE && cfg->teno_variant != MGPU_TENO_CORRECTED &&
+            cfg->teno_variant != MGPU_TENO_ROBUST)
             throw ArgFail("unknown TENO variant");
         if (cfg->basis != MGPU_BASIS_LEGENDRE && cfg->basis != MGPU_BASIS_MONOMIAL) throw ArgFail("Unknown basis type.");
         if (!(cfg->gamma > 1.0) || !(cfg->p_ref > 0) || !(cfg->T_ref > 0) || !(cfg->rho_ref > 0))
@@ -1117,7 +1131,8 @@ int mgpu_riemann_flux_batch(int solver, uint32_t n, const double* n_unit, const 
                             const double* u_r, const double* p_r, const double* gamma_r, const double* h_r,
                             double* flux) {
     return guarded([&] {
-        if (solver < 0 || solver > 2) throw ArgFail("Unknown Riemann solver type.");
+        if ((solver & ~MGPU_RIEMANN_GUARD) < 0 || (solver & ~MGPU_RIEMANN_GUARD) > 2)
+            throw ArgFail("Unknown Riemann solver type.");
         if (n == 0) return MGPU_OK;
         if (!n_unit || !rho_l || !u_l || !p_l || !gamma_l || !h_l || !rho_r || !u_r || !p_r || !gamma_r || !h_r || !flux)
             throw ArgFail("null argument");

@@ -118,7 +118,7 @@ struct mgpu_ctx {
     DevArray<float> P4;
     DevArray<uint16_t> fcode;   // FP32 form: face-shape code per cell (3 bits per face slot)
     DevArray<float4> phi_tab4;  // FP32 form: the 8 code slots' shape sets
-    DevArray<uint8_t> smask, masks;
+    DevArray<uint8_t> smask, masks, bcell;
     DevArray<double> staging;      // caller-order rows for state transfers
     DevArray<uint32_t> perm_old;   // internal cell -> caller cell
     TenoArgs teno{};
@@ -234,7 +234,8 @@ struct mgpu_ctx {
             a.qw[i] = qw[i];
             a.qw_f[i] = (float)qw[i];
         }
-        const bool pos = cfg.recon == MGPU_RECON_TENO && cfg.teno_variant == MGPU_TENO_CORRECTED;
+        const bool pos = cfg.recon == MGPU_RECON_TENO && cfg.teno_variant != MGPU_TENO_REFERENCE;
+        a.guard = cfg.recon == MGPU_RECON_TENO && cfg.teno_variant == MGPU_TENO_ROBUST;
         if (single()) {
             viscous_gradients32(Uin == U.p ? U32.p : Ut32.p);
             const Visc32Args* v = cfg.viscous ? &visc32 : nullptr;

@@ -315,9 +315,9 @@ int mgpu_selector_harvest(mgpu_selector* s, mgpu_ctx* ctx, double keep_central, 
     if (int rc = need_sel(s)) return rc;
     if (int rc = need_ready(ctx)) return rc;
     return guarded([&] {
-        if (ctx->cfg.recon != MGPU_RECON_TENO || ctx->K != 10 || ctx->cfg.teno_variant != MGPU_TENO_CORRECTED ||
+        if (ctx->cfg.recon != MGPU_RECON_TENO || ctx->K != 10 || ctx->cfg.teno_variant == MGPU_TENO_REFERENCE ||
             ctx->single())
-            throw Unsupported("harvest needs an FP64 context with corrected TENO at p = 3");
+            throw Unsupported("harvest needs an FP64 context with corrected or robust TENO at p = 3");
         if (ctx->cfg.device != s->device) throw ArgFail("selector and context are on different devices");
         DeviceGuard g(s->device);
         // TENO decisions of the current state

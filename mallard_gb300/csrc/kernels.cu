@@ -267,7 +267,7 @@ __global__ void permute_column_kernel(int n, int stride, const uint32_t* __restr
 
 // buf: per problem 13 doubles: n0 n1 rho_l ul0 ul1 p_l gamma_l h_l rho_r ur0 ur1 p_r gamma_r h_r ... (14)
 template <int RS>
-__global__ void riemann_batch_kernel(uint32_t n, const double* __restrict__ in, double* __restrict__ flux) {
+__global__ void riemann_batch_kernel(uint32_t n, const double* __restrict__ in, double* __restrict__ flux, int guard) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double* b = in + (size_t)i * 14;
@@ -275,7 +275,7 @@ __global__ void riemann_batch_kernel(uint32_t n, const double* __restrict__ in, 
     const double ul[2] = {b[3], b[4]};
     const double ur[2] = {b[9], b[10]};
     double F[4];
-    riemann<RS>(F, nn, b[2], ul, b[5], b[6], b[7], b[8], ur, b[11], b[12], b[13]);
+    riemann<RS>(F, nn, b[2], ul, b[5], b[6], b[7], b[8], ur, b[11], b[12], b[13], guard != 0);
 #pragma unroll
     for (int k = 0; k < 4; k++) flux[(size_t)i * 4 + k] = F[k];
 }
@@ -398,10 +398,11 @@ cudaError_t launch_permute_column(int n, int stride, const uint32_t* idx, const 
 cudaError_t launch_riemann_batch(int rsolver, uint32_t n, const double* in, double* flux, cudaStream_t s) {
     const unsigned blocks = (n + 127) / 128;
     if (blocks == 0) return cudaSuccess;
-    switch (rsolver) {
-        case MGPU_RIEMANN_RUSANOV: riemann_batch_kernel<MGPU_RIEMANN_RUSANOV><<<blocks, 128, 0, s>>>(n, in, flux); break;
-        case MGPU_RIEMANN_HLL: riemann_batch_kernel<MGPU_RIEMANN_HLL><<<blocks, 128, 0, s>>>(n, in, flux); break;
-        case MGPU_RIEMANN_HLLC: riemann_batch_kernel<MGPU_RIEMANN_HLLC><<<blocks, 128, 0, s>>>(n, in, flux); break;
+    const int guard = (rsolver & MGPU_RIEMANN_GUARD) ? 1 : 0;
+    switch (rsolver & ~MGPU_RIEMANN_GUARD) {
+        case MGPU_RIEMANN_RUSANOV: riemann_batch_kernel<MGPU_RIEMANN_RUSANOV><<<blocks, 128, 0, s>>>(n, in, flux, guard); break;
+        case MGPU_RIEMANN_HLL: riemann_batch_kernel<MGPU_RIEMANN_HLL><<<blocks, 128, 0, s>>>(n, in, flux, guard); break;
+        case MGPU_RIEMANN_HLLC: riemann_batch_kernel<MGPU_RIEMANN_HLLC><<<blocks, 128, 0, s>>>(n, in, flux, guard); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

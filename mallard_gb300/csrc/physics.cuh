@@ -108,9 +108,15 @@ __device__ __forceinline__ T anrs(const T* L, const T* R) {
     return ps;
 }
 
+// guard: a star pressure that is not a number counts as zero (the robust
+// TENO variant).  The two-rarefaction estimate raises a negative base to
+// the power 2 gamma / (gamma - 1), not an exact integer in floating point,
+// when a strong expansion meets near-vacuum pressure; zero gives the wave
+// speeds of every star pressure below both sides' pressures, so no flux the
+// reference computes as a number changes.
 template <int RS, class T>
 __device__ __forceinline__ void riemann(T* F, const T* n, T rl, const T* ul, T pl, T gl, T hl, T rr, const T* ur, T pr,
-                                        T gr, T hr) {
+                                        T gr, T hr, bool guard = false) {
     const T unl = ul[0] * n[0] + ul[1] * n[1];
     const T unr = ur[0] * n[0] + ur[1] * n[1];
     const T qql = ul[0] * ul[0] + ul[1] * ul[1];
@@ -130,7 +136,8 @@ __device__ __forceinline__ void riemann(T* F, const T* n, T rl, const T* ul, T p
         return;
     }
     const T Wl[4] = {rl, unl, pl, gl}, Wr[4] = {rr, unr, pr, gr};
-    const T ps = anrs(Wl, Wr);
+    T ps = anrs(Wl, Wr);
+    if (guard && !(ps == ps)) ps = T(0.0);
     const T ql = (ps <= pl) ? T(1.0) : sqrt(T(1.0) + (gl + T(1.0)) / (T(2.0) * gl) * (ps / pl - T(1.0)));
     const T qr = (ps <= pr) ? T(1.0) : sqrt(T(1.0) + (gr + T(1.0)) / (T(2.0) * gr) * (ps / pr - T(1.0)));
     const T Sl = unl - al * ql;

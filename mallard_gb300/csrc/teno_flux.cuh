@@ -25,12 +25,65 @@ namespace {
 // registers until the weights are known, then writes its variable at the
 // quadrature points of the cell's three faces.
 
+// The robust variant's per-cell step (after the face values of all four
+// variables are known): a cell with a boundary face takes its average at
+// every face point; otherwise each variable's deviations from the average
+// are scaled by one factor into the central stencil's range [dlo, dhi]
+// (around the average), and a cell with a face state that is then not
+// admissible takes its average at every face point.  live: the warp's lanes
+// whose cells exist; the four lanes of a cell exchange their variables.
+template <int NF, int NQ>
+__device__ __forceinline__ void robust_cell(const TenoArgs& a, int cell, unsigned live, double uc, double dlo,
+                                            double dhi, double (&out)[NF][NQ]) {
+    const bool boundary = a.bcell[cell] != 0;
+    if (!boundary) {
+        double th = 1.0;
+#pragma unroll
+        for (int fl = 0; fl < NF; ++fl)
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) {
+                const double d = out[fl][q] - uc;
+                if (d > dhi) th = fmin(th, dhi / d);
+                else if (d < dlo) th = fmin(th, dlo / d);
+            }
+        if (th < 1.0)
+#pragma unroll
+            for (int fl = 0; fl < NF; ++fl)
+#pragma unroll
+                for (int q = 0; q < NQ; ++q) out[fl][q] = uc + th * (out[fl][q] - uc);
+    }
+    bool bad = boundary;
+#pragma unroll
+    for (int fl = 0; fl < NF; ++fl)
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+            const double rho = __shfl_sync(live, out[fl][q], 0, 4);
+            const double m0 = __shfl_sync(live, out[fl][q], 1, 4);
+            const double m1 = __shfl_sync(live, out[fl][q], 2, 4);
+            const double E = __shfl_sync(live, out[fl][q], 3, 4);
+            if (!(rho > 0.0)) {
+                bad = true;
+            } else {
+                const double u0 = m0 / rho, u1 = m1 / rho;
+                const double e = E / rho - 0.5 * (u0 * u0 + u1 * u1);
+                if (!(a.gm1 * rho * e > 0.0)) bad = true;
+            }
+        }
+    if (bad)
+#pragma unroll
+        for (int fl = 0; fl < NF; ++fl)
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) out[fl][q] = uc;
+}
+
 template <int K, int M, int NQ, int VARIANT>
 __global__ void __launch_bounds__(128) teno_kernel(const TenoArgs a, const double* __restrict__ U,
                                                    double* __restrict__ fv, uint8_t* __restrict__ masks) {
     constexpr int KR = K - 1, MR = M - 1, NF = 3, S = 4;
+    constexpr bool ROBUST = VARIANT == MGPU_TENO_ROBUST;
     const int gt = blockIdx.x * blockDim.x + threadIdx.x;
     const int cell = gt >> 2, v = gt & 3;
+    const unsigned live = ROBUST ? __ballot_sync(0xffffffffu, cell < a.n_cells) : 0u;
     if (cell >= a.n_cells) return;
     const int tile = cell >> 3, lane = cell & 7;
     const double uc = U[(size_t)cell * NC + v];
@@ -38,6 +91,7 @@ __global__ void __launch_bounds__(128) teno_kernel(const TenoArgs a, const doubl
 
     double coef[S][KR];
     double w[S];
+    double dlo = 0.0, dhi = 0.0;  // the robust variant's central-stencil range around uc
 #pragma unroll
     for (int s = 0; s < S; ++s) {
 #pragma unroll
@@ -51,7 +105,12 @@ __global__ void __launch_bounds__(128) teno_kernel(const TenoArgs a, const doubl
 #pragma unroll 4
         for (int j = 0; j < MR; ++j) {
             const uint32_t nbj = __ldg(nbp + j * TILE);
-            const double b = __ldg(arp + j * TILE) * (__ldg(U + (size_t)nbj * NC + v) - uc);
+            const double d = __ldg(U + (size_t)nbj * NC + v) - uc;
+            const double b = __ldg(arp + j * TILE) * d;
+            if (ROBUST && s == 0) {
+                dlo = fmin(dlo, d);
+                dhi = fmax(dhi, d);
+            }
 #pragma unroll
             for (int k = 0; k < KR; ++k) coef[s][k] = coef[s][k] + __ldg(Pp + (j * KR + k) * TILE) * b;
         }
@@ -97,7 +156,7 @@ __global__ void __launch_bounds__(128) teno_kernel(const TenoArgs a, const doubl
                 w[s] = (1.0 / K);
                 mask |= 1u << s;
             }
-        if (VARIANT == MGPU_TENO_CORRECTED) {
+        if (VARIANT != MGPU_TENO_REFERENCE) {
             w[0] = 0.0;
 #pragma unroll
             for (int s = 1; s < S; ++s)
@@ -119,11 +178,11 @@ __global__ void __launch_bounds__(128) teno_kernel(const TenoArgs a, const doubl
 #endif
 
     // face states at the quadrature points
+    double outv[NF][NQ];
+    uint32_t slots[NF];
 #pragma unroll
     for (int fl = 0; fl < NF; ++fl) {
-        const uint32_t slot = __ldg(a.cface + ((size_t)tile * NF + fl) * TILE + lane);
-        const size_t f = slot >> 1;
-        const unsigned side = slot & 1u;
+        slots[fl] = __ldg(a.cface + ((size_t)tile * NF + fl) * TILE + lane);
 #pragma unroll
         for (int q = 0; q < NQ; ++q) {
             const double* php = a.phi + (((size_t)tile * NF + fl) * NQ + q) * KR * TILE + lane;
@@ -141,8 +200,16 @@ __global__ void __launch_bounds__(128) teno_kernel(const TenoArgs a, const doubl
                 for (int k = 0; k < KR; ++k) out = out + (w[s] * coef[s][k]) * phi[k];
 #endif
             }
-            fv[((f * NQ + q) * 2 + side) * NC + v] = out;
+            outv[fl][q] = out;
         }
+    }
+    if (ROBUST) robust_cell<NF, NQ>(a, cell, live, uc, dlo, dhi, outv);
+#pragma unroll
+    for (int fl = 0; fl < NF; ++fl) {
+        const size_t f = slots[fl] >> 1;
+        const unsigned side = slots[fl] & 1u;
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) fv[((f * NQ + q) * 2 + side) * NC + v] = outv[fl][q];
     }
 }
 
@@ -223,7 +290,7 @@ __global__ void __launch_bounds__(128) flux_kernel(const FluxArgs a, const GasPa
                 pr[3] = T;
                 pr[4] = e + po / rho;
             }
-            riemann<RS>(Ft, n, cl[0], pl, pl[2], g.gamma, pl[4], cr[0], pr, pr[2], g.gamma, pr[4]);
+            riemann<RS>(Ft, n, cl[0], pl, pl[2], g.gamma, pl[4], cr[0], pr, pr[2], g.gamma, pr[4], a.guard != 0);
         }
 #pragma unroll
         for (int i = 0; i < 4; i++) F[i] += a.qw[q] * Ft[i];
@@ -242,6 +309,8 @@ cudaError_t teno_dispatch_variant(const TenoArgs& a, int variant, const double* 
     if (blocks == 0) return cudaSuccess;
     if (variant == MGPU_TENO_CORRECTED)
         teno_kernel<K, M, NQ, MGPU_TENO_CORRECTED><<<blocks, 128, 0, s>>>(a, U, fv, masks);
+    else if (variant == MGPU_TENO_ROBUST)
+        teno_kernel<K, M, NQ, MGPU_TENO_ROBUST><<<blocks, 128, 0, s>>>(a, U, fv, masks);
     else
         teno_kernel<K, M, NQ, MGPU_TENO_REFERENCE><<<blocks, 128, 0, s>>>(a, U, fv, masks);
     return cudaGetLastError();

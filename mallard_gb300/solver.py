@@ -443,8 +443,9 @@ def initial_state(mesh, init, gas):
     return np.ascontiguousarray(U), np.ascontiguousarray(W)
 
 
-def riemann_flux(solver, n_unit, rho_l, u_l, p_l, gamma_l, h_l, rho_r, u_r, p_r, gamma_r, h_r):
-    """RiemannSolver::calc_flux on the GPU for arrays of problems."""
+def riemann_flux(solver, n_unit, rho_l, u_l, p_l, gamma_l, h_l, rho_r, u_r, p_r, gamma_r, h_r, guard=False):
+    """RiemannSolver::calc_flux on the GPU for arrays of problems; guard: the
+    robust variant's star pressure (a NaN star pressure counts as zero)."""
     arrs = [np.ascontiguousarray(np.atleast_1d(np.asarray(a, dtype=np.float64)))
             for a in (n_unit, rho_l, u_l, p_l, gamma_l, h_l, rho_r, u_r, p_r, gamma_r, h_r)]
     n = arrs[1].size
@@ -452,7 +453,7 @@ def riemann_flux(solver, n_unit, rho_l, u_l, p_l, gamma_l, h_l, rho_r, u_r, p_r,
     arrs[2] = arrs[2].reshape(n, 2)
     arrs[7] = arrs[7].reshape(n, 2)
     F = np.empty((n, 4))
-    N.check(N.lib().mgpu_riemann_flux_batch(N.RIEMANN[solver], n, *[N.ptr(a) for a in arrs], N.ptr(F)))
+    N.check(N.lib().mgpu_riemann_flux_batch(N.RIEMANN[solver] | (16 if guard else 0), n, *[N.ptr(a) for a in arrs], N.ptr(F)))
     return F
 
 

@@ -29,6 +29,7 @@
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <random>
 #include <utility>
 #include <vector>
 
@@ -670,15 +671,31 @@ void teno_sizes(Teno& t, double factor) {
     }
 }
 
-// TENO::compute_stencils (face_reconstruction.cpp:406-475)
+// TENO::compute_stencils (face_reconstruction.cpp:406-475).  Each cell's
+// stencils depend on the mesh alone, so with more than one oracle thread
+// they are searched in parallel and then concatenated in cell order (the
+// same tables as the serial loop).
 void teno_stencils(Teno& t, const OMesh& m) {
     t.off_groups = {0};
     t.off_stencils = {0};
     t.stencils.clear();
+    std::vector<std::vector<std::vector<uint32_t>>> per(m.n_cells);
+    std::string err;
+#pragma omp parallel for schedule(dynamic, 256) if (g_threads > 1) num_threads(g_threads)
+    for (int64_t ci = 0; ci < (int64_t)m.n_cells; ++ci) {
+        try {
+            const uint32_t c = (uint32_t)ci;
+            per[c].push_back(stencil_central(m, t.M, c));
+            for (auto& s : stencils_directional(m, t.M, c)) per[c].push_back(std::move(s));
+        } catch (const std::exception& e) {
+#pragma omp critical
+            err = e.what();
+        }
+    }
+    if (!err.empty()) throw std::runtime_error(err);
     for (uint32_t c = 0; c < m.n_cells; ++c) {
         std::vector<std::vector<uint32_t>> all;
-        all.push_back(stencil_central(m, t.M, c));
-        for (auto& s : stencils_directional(m, t.M, c)) all.push_back(s);
+        all.swap(per[c]);
         for (auto& s : all) {
             if ((int)s.size() < t.M && s.size() > 0) throw std::runtime_error("Stencil is not full.");
             t.stencils.insert(t.stencils.end(), s.begin(), s.end());
@@ -688,95 +705,123 @@ void teno_stencils(Teno& t, const OMesh& m) {
     }
 }
 
-// TENO::compute_reconstruction_matrices (face_reconstruction.cpp:477-741)
-void teno_matrices(Teno& t, const OMesh& m) {
+// TENO::compute_reconstruction_matrices (face_reconstruction.cpp:477-741),
+// one stencil: its transformed areas and pseudo-inverse into at/A.  set_ipt:
+// the basis means of the target (from cell 0, stencil 0, :598-602) are
+// taken from this stencil first.
+void stencil_matrix(Teno& t, const OMesh& m, uint32_t c, int sl, bool set_ipt, double* at, double* A) {
     const int K = t.K;
-    t.off_mats = {0};
-    t.mats.clear();
-    t.areas.clear();
-    t.ipt.assign(K, 0.0);
     const int nq = t.qcell.n();
-    for (uint32_t c = 0; c < m.n_cells; ++c) {
-        if (m.n_nodes_of_cell(c) != 3) throw std::runtime_error("TENO has only been implemented for triangular cells.");
-        const double* w0 = m.nc(m.node_of_cell(c, 0));
-        double J[4], Ji[4];
-        tri_jac(w0, m.nc(m.node_of_cell(c, 1)), m.nc(m.node_of_cell(c, 2)), J);
-        inv2(J, Ji);
-        uint32_t g0 = t.off_groups[c];
-        int gs = (int)(t.off_groups[c + 1] - g0);
-        for (int sl = 0; sl < gs; ++sl) {
-            uint32_t s = g0 + sl;
-            uint32_t so = t.off_stencils[s];
-            int M = (int)(t.off_stencils[s + 1] - so);
-            if (M == 0) {
-                if (sl == 0) throw std::runtime_error("Central stencil is empty for cell " + std::to_string(c) + ".");
-                t.off_mats.push_back((uint32_t)t.mats.size());
-                continue;
-            }
-            std::vector<double> at(M), A((size_t)M * K), R((size_t)M * K), Y((size_t)K * M);
-            for (int j = 0; j < M; ++j) {
-                uint32_t nb = t.stencils[so + j];
-                double v[3][2];
-                for (int k = 0; k < 3; ++k) {
-                    v[k][0] = m.nc(m.node_of_cell(nb, k))[0];
-                    v[k][1] = m.nc(m.node_of_cell(nb, k))[1];
-                }
-                double Jn[4];
-                tri_jac(v[0], v[1], v[2], Jn);
-                double vt[3][2];
-                for (int k = 0; k < 3; ++k) {
-                    vt[k][0] = v[k][0] - w0[0];
-                    vt[k][1] = v[k][1] - w0[1];
-                    mv2(Ji, vt[k], vt[k]);
-                }
-                at[j] = tri_area(vt[0], vt[1], vt[2]);
-                std::vector<double> qp(2 * (size_t)nq);
-                for (int q = 0; q < nq; ++q) {
-                    double x[2] = {t.qcell.pts[2 * q], t.qcell.pts[2 * q + 1]};
-                    mv2(Jn, x, x);
-                    x[0] += v[0][0];
-                    x[1] += v[0][1];
-                    x[0] -= w0[0];
-                    x[1] -= w0[1];
-                    mv2(Ji, x, x);
-                    qp[2 * q] = x[0];
-                    qp[2 * q + 1] = x[1];
-                }
-                for (int k = 0; k < K; ++k) {
-                    double& a = A[(size_t)j * K + k];
-                    a = 0.0;
-                    for (int q = 0; q < nq; ++q)
-                        a += t.qcell.wts[q] * basis2(t.basis, t.pidx[2 * k], t.pidx[2 * k + 1], qp[2 * q], qp[2 * q + 1]);
-                    a *= at[j];
-                }
-            }
-            if (c == 0 && sl == 0)
-                for (int k = 0; k < K; ++k) t.ipt[k] = A[k] / at[0];
-            for (int j = 0; j < M; ++j)
-                for (int k = 0; k < K; ++k) A[(size_t)j * K + k] -= at[j] * t.ipt[k];
-            bool col0_zero = true;
-            for (int j = 0; j < M; ++j)
-                if (A[(size_t)j * K] > 1.0e-12) { col0_zero = false; break; }
-            if (col0_zero) {
-                std::vector<double> B((size_t)(M - 1) * (K - 1));
-                for (int j = 1; j < M; ++j)
-                    for (int k = 1; k < K; ++k) B[(size_t)(j - 1) * (K - 1) + (k - 1)] = A[(size_t)j * K + k];
-                householder_r(B.data(), R.data(), M - 1, K - 1);
-                fwd_subst(R.data(), B.data(), Y.data(), K - 1, K - 1, M - 1, true, true);
-                back_subst(R.data(), Y.data(), B.data(), K - 1, K - 1, M - 1, false, false);
-                for (int k = 0; k < K; ++k)
-                    for (int j = 0; j < M; ++j)
-                        A[(size_t)k * M + j] = (k == 0 || j == 0) ? 0.0 : B[(size_t)(k - 1) * (M - 1) + (j - 1)];
-            } else {
-                householder_r(A.data(), R.data(), M, K);
-                fwd_subst(R.data(), A.data(), Y.data(), K, K, M, true, true);
-                back_subst(R.data(), Y.data(), A.data(), K, K, M, false, false);
-            }
-            t.mats.insert(t.mats.end(), A.begin(), A.end());
-            t.off_mats.push_back((uint32_t)t.mats.size());
-            t.areas.insert(t.areas.end(), at.begin(), at.end());
+    const double* w0 = m.nc(m.node_of_cell(c, 0));
+    double J[4], Ji[4];
+    tri_jac(w0, m.nc(m.node_of_cell(c, 1)), m.nc(m.node_of_cell(c, 2)), J);
+    inv2(J, Ji);
+    const uint32_t s = t.off_groups[c] + sl;
+    const uint32_t so = t.off_stencils[s];
+    const int M = (int)(t.off_stencils[s + 1] - so);
+    std::vector<double> R((size_t)M * K), Y((size_t)K * M);
+    for (int j = 0; j < M; ++j) {
+        uint32_t nb = t.stencils[so + j];
+        double v[3][2];
+        for (int k = 0; k < 3; ++k) {
+            v[k][0] = m.nc(m.node_of_cell(nb, k))[0];
+            v[k][1] = m.nc(m.node_of_cell(nb, k))[1];
+        }
+        double Jn[4];
+        tri_jac(v[0], v[1], v[2], Jn);
+        double vt[3][2];
+        for (int k = 0; k < 3; ++k) {
+            vt[k][0] = v[k][0] - w0[0];
+            vt[k][1] = v[k][1] - w0[1];
+            mv2(Ji, vt[k], vt[k]);
+        }
+        at[j] = tri_area(vt[0], vt[1], vt[2]);
+        std::vector<double> qp(2 * (size_t)nq);
+        for (int q = 0; q < nq; ++q) {
+            double x[2] = {t.qcell.pts[2 * q], t.qcell.pts[2 * q + 1]};
+            mv2(Jn, x, x);
+            x[0] += v[0][0];
+            x[1] += v[0][1];
+            x[0] -= w0[0];
+            x[1] -= w0[1];
+            mv2(Ji, x, x);
+            qp[2 * q] = x[0];
+            qp[2 * q + 1] = x[1];
+        }
+        for (int k = 0; k < K; ++k) {
+            double& a = A[(size_t)j * K + k];
+            a = 0.0;
+            for (int q = 0; q < nq; ++q)
+                a += t.qcell.wts[q] * basis2(t.basis, t.pidx[2 * k], t.pidx[2 * k + 1], qp[2 * q], qp[2 * q + 1]);
+            a *= at[j];
         }
     }
+    if (set_ipt)
+        for (int k = 0; k < K; ++k) t.ipt[k] = A[k] / at[0];
+    for (int j = 0; j < M; ++j)
+        for (int k = 0; k < K; ++k) A[(size_t)j * K + k] -= at[j] * t.ipt[k];
+    bool col0_zero = true;
+    for (int j = 0; j < M; ++j)
+        if (A[(size_t)j * K] > 1.0e-12) { col0_zero = false; break; }
+    if (col0_zero) {
+        std::vector<double> B((size_t)(M - 1) * (K - 1));
+        for (int j = 1; j < M; ++j)
+            for (int k = 1; k < K; ++k) B[(size_t)(j - 1) * (K - 1) + (k - 1)] = A[(size_t)j * K + k];
+        householder_r(B.data(), R.data(), M - 1, K - 1);
+        fwd_subst(R.data(), B.data(), Y.data(), K - 1, K - 1, M - 1, true, true);
+        back_subst(R.data(), Y.data(), B.data(), K - 1, K - 1, M - 1, false, false);
+        for (int k = 0; k < K; ++k)
+            for (int j = 0; j < M; ++j)
+                A[(size_t)k * M + j] = (k == 0 || j == 0) ? 0.0 : B[(size_t)(k - 1) * (M - 1) + (j - 1)];
+    } else {
+        householder_r(A, R.data(), M, K);
+        fwd_subst(R.data(), A, Y.data(), K, K, M, true, true);
+        back_subst(R.data(), Y.data(), A, K, K, M, false, false);
+    }
+}
+
+// All stencils: offsets first, then every stencil's matrix in place (in
+// parallel with more than one oracle thread; each stencil's arithmetic is
+// its own, so the tables equal the serial build's).
+void teno_matrices(Teno& t, const OMesh& m) {
+    const int K = t.K;
+    t.ipt.assign(K, 0.0);
+    std::vector<size_t> mo(t.off_stencils.size()), ao(t.off_stencils.size());
+    size_t nm = 0, na = 0;
+    t.off_mats = {0};
+    for (uint32_t c = 0; c < m.n_cells; ++c) {
+        if (m.n_nodes_of_cell(c) != 3) throw std::runtime_error("TENO has only been implemented for triangular cells.");
+        for (uint32_t s = t.off_groups[c]; s < t.off_groups[c + 1]; ++s) {
+            const size_t M = t.off_stencils[s + 1] - t.off_stencils[s];
+            if (M == 0 && s == t.off_groups[c])
+                throw std::runtime_error("Central stencil is empty for cell " + std::to_string(c) + ".");
+            mo[s] = nm;
+            ao[s] = na;
+            nm += (size_t)K * M;
+            na += M;
+            t.off_mats.push_back((uint32_t)nm);
+        }
+    }
+    t.mats.assign(nm, 0.0);
+    t.areas.assign(na, 0.0);
+    if (m.n_cells == 0) return;
+    stencil_matrix(t, m, 0, 0, true, &t.areas[ao[0]], &t.mats[mo[0]]);
+    std::string err;
+#pragma omp parallel for schedule(dynamic, 256) if (g_threads > 1) num_threads(g_threads)
+    for (int64_t ci = 0; ci < (int64_t)m.n_cells; ++ci) {
+        try {
+            const uint32_t c = (uint32_t)ci;
+            const uint32_t g0 = t.off_groups[c];
+            for (uint32_t s = g0; s < t.off_groups[c + 1]; ++s) {
+                if (t.off_stencils[s + 1] == t.off_stencils[s] || (c == 0 && s == g0)) continue;
+                stencil_matrix(t, m, c, (int)(s - g0), false, &t.areas[ao[s]], &t.mats[mo[s]]);
+            }
+        } catch (const std::exception& e) {
+#pragma omp critical
+            err = e.what();
+        }
+    }
+    if (!err.empty()) throw std::runtime_error(err);
 }
 
 // TENO::compute_oscillation_indicator (face_reconstruction.cpp:743-788)
@@ -1611,6 +1656,51 @@ void* orc_mesh_from_arrays(uint32_t n_nodes, const double* node_coords, uint32_t
 
 void orc_mesh_free(void* h) { delete static_cast<OMesh*>(h); }
 
+// Seeded relabelling of the cells (the benchmark meshes' random cell order),
+// the same permutation the GPU library's mesh helper applies: a Fisher-Yates
+// shuffle of new_of_old driven by std::mt19937_64(seed), position i - 1
+// swapped with rng() % i for i = n .. 2.  Cell lists, centroids and volumes
+// move with their cells; faces keep their numbers and only the cell ids on
+// the faces of the zones change.  new_of_old (optional) receives the map.
+int orc_mesh_permute_cells(void* h, uint64_t seed, uint32_t* new_of_old) {
+    return guarded([&] {
+        OMesh& m = *static_cast<OMesh*>(h);
+        const uint32_t n = m.n_cells;
+        std::vector<uint32_t> to_new(n), to_old(n);
+        for (uint32_t i = 0; i < n; ++i) to_new[i] = i;
+        std::mt19937_64 rng(seed);
+        for (uint32_t i = n; i > 1; --i) std::swap(to_new[i - 1], to_new[(uint32_t)(rng() % i)]);
+        for (uint32_t i = 0; i < n; ++i) to_old[to_new[i]] = i;
+        auto move_lists = [&](std::vector<uint32_t>& off, std::vector<uint32_t>& flat) {
+            std::vector<uint32_t> o2(1, 0), f2;
+            f2.reserve(flat.size());
+            for (uint32_t c = 0; c < n; ++c) {
+                const uint32_t old = to_old[c];
+                for (uint32_t k = off[old]; k < off[old + 1]; ++k) f2.push_back(flat[k]);
+                o2.push_back((uint32_t)f2.size());
+            }
+            off.swap(o2);
+            flat.swap(f2);
+        };
+        move_lists(m.off_noc, m.noc);
+        move_lists(m.off_foc, m.foc);
+        std::vector<double> cc(m.cell_coords.size()), vol(m.cell_volume.size());
+        for (uint32_t c = 0; c < n; ++c) {
+            cc[2 * (size_t)c] = m.cell_coords[2 * (size_t)to_old[c]];
+            cc[2 * (size_t)c + 1] = m.cell_coords[2 * (size_t)to_old[c] + 1];
+            vol[c] = m.cell_volume[to_old[c]];
+        }
+        m.cell_coords.swap(cc);
+        m.cell_volume.swap(vol);
+        for (uint32_t f : m.zone_faces)
+            for (int sd = 0; sd < 2; ++sd) {
+                int32_t& c = m.cof[2 * (size_t)f + sd];
+                if (c >= 0) c = (int32_t)to_new[(uint32_t)c];
+            }
+        if (new_of_old) std::copy(to_new.begin(), to_new.end(), new_of_old);
+    });
+}
+
 // field ids: 0 node_coords 1 cell_coords 2 cell_volume 3 face_area 4 face_normals
 // 5 off_noc 6 noc 7 off_foc 8 foc 9 off_nof 10 nof 11 cells_of_face 12 zone_off 13 zone_faces
 uint64_t orc_mesh_len(void* h, int field) {
@@ -1855,7 +1945,8 @@ void orc_teno_copy(void* h, int field, void* dst) {
 // Unit-level entry points used by the known-answer tests.
 void orc_riemann_flux(int kind, const double* n_unit, double rl, const double* ul, double pl, double gl, double hl,
                       double rr, const double* ur, double pr, double gr, double hr, double* flux) {
-    riemann(kind, flux, n_unit, rl, ul, pl, gl, hl, rr, ur, pr, gr, hr);
+    // kind | 16: the robust variant's guarded star pressure
+    riemann(kind & 15, flux, n_unit, rl, ul, pl, gl, hl, rr, ur, pr, gr, hr, (kind & 16) != 0);
 }
 
 void orc_gas_constants(double gamma, double p_ref, double T_ref, double rho_ref, double* R_cp_cv) {

@@ -69,6 +69,7 @@ def load():
         "orc_mesh_generate": (vp, [i32, u32, u32, f64, f64]),
         "orc_mesh_from_arrays": (vp, [u32, vp, u32, vp, vp, vp, vp, u32, vp, vp, vp, u32, vp, vp]),
         "orc_mesh_free": (None, [vp]),
+        "orc_mesh_permute_cells": (i32, [vp, u64, vp]),
         "orc_mesh_len": (u64, [vp, i32]),
         "orc_mesh_copy": (None, [vp, i32, vp]),
         "orc_mesh_counts": (u32, [vp, C.POINTER(u32), C.POINTER(u32), C.POINTER(u32)]),
@@ -120,6 +121,9 @@ class OracleMesh:
         if not handle:
             raise RuntimeError(_err(self._lib))
         self.h = handle
+        self._load()
+
+    def _load(self):
         nn, nc, nf = C.c_uint32(), C.c_uint32(), C.c_uint32()
         self.n_zones = self._lib.orc_mesh_counts(self.h, C.byref(nn), C.byref(nc), C.byref(nf))
         self.n_nodes, self.n_cells, self.n_faces = nn.value, nc.value, nf.value
@@ -131,6 +135,15 @@ class OracleMesh:
             if width > 1:
                 a = a.reshape(-1, width)
             setattr(self, name, a)
+
+    def permute_cells(self, seed):
+        """Relabel the cells by the seeded permutation the GPU library's mesh
+        helper applies (see the C source); returns new_of_old."""
+        perm = np.empty(self.n_cells, dtype=np.uint32)
+        if self._lib.orc_mesh_permute_cells(self.h, int(seed), _p(perm)) != 0:
+            raise RuntimeError(_err(self._lib))
+        self._load()
+        return perm
 
     @classmethod
     def generate(cls, mesh_type, nx, ny, Lx=1.0, Ly=1.0):
@@ -261,12 +274,12 @@ class Oracle:
     def max_threads(self):
         return self.lib.orc_max_threads()
 
-    def riemann_flux(self, kind, n_unit, rho_l, u_l, p_l, gamma_l, h_l, rho_r, u_r, p_r, gamma_r, h_r):
+    def riemann_flux(self, kind, n_unit, rho_l, u_l, p_l, gamma_l, h_l, rho_r, u_r, p_r, gamma_r, h_r, guard=False):
         n = np.asarray(n_unit, dtype=np.float64)
         ul = np.asarray(u_l, dtype=np.float64)
         ur = np.asarray(u_r, dtype=np.float64)
         F = np.empty(4)
-        self.lib.orc_riemann_flux(RIEMANN[kind], _p(n), rho_l, _p(ul), p_l, gamma_l, h_l, rho_r, _p(ur), p_r,
+        self.lib.orc_riemann_flux(RIEMANN[kind] | (16 if guard else 0), _p(n), rho_l, _p(ul), p_l, gamma_l, h_l, rho_r, _p(ur), p_r,
                                   gamma_r, h_r, _p(F))
         return F
 

@@ -90,8 +90,9 @@ BC_DATA = {
 
 
 def make_pair(mesh, recon="TENO", riemann="HLLC", variant="reference", bcs=None, poly_order=3, p_min=-1e20,
-              p_max=1e20, reorder=True, precision="fp64", integrator="SSPRK3"):
-    """A GPU solver and an oracle case on the same mesh and numerics."""
+              p_max=1e20, reorder=True, precision="fp64", integrator="SSPRK3", gpu=True):
+    """A GPU solver and an oracle case on the same mesh and numerics (gpu
+    False: the oracle case alone, the solver None)."""
     bcs = bcs or {name: "extrapolation" for name in mesh.zone_names[1:]}
     blist = []
     for name, typ in bcs.items():
@@ -100,7 +101,7 @@ def make_pair(mesh, recon="TENO", riemann="HLLC", variant="reference", bcs=None,
         blist.append(d)
     s = mg.Solver(mesh, face_reconstruction=recon, basis_type="legendre", basis_order=poly_order,
                   riemann_solver=riemann, boundaries=blist, teno_variant=variant, reorder=reorder, p_min=p_min,
-                  p_max=p_max, precision=precision, time_integrator=integrator, **GAS)
+                  p_max=p_max, precision=precision, time_integrator=integrator, **GAS) if gpu else None
     om = OracleMesh.from_arrays(mesh)
     oc = OracleCase(om, recon=recon, basis="legendre", poly_order=poly_order, riemann=riemann, p_min=p_min,
                     p_max=p_max, **GAS)

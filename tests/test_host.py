@@ -278,3 +278,19 @@ def test_face_points_sit_on_reference_edges(which):
                 worst = max(worst, np.abs(mapped - edge).max())
     assert worst < 1e-12, worst
     assert codes.sum() == 3 * m.n_cells
+
+
+def test_oracle_permutation_equals_the_library_mesh_helper():
+    """The oracle's seeded cell relabelling (used by the benchmark's CPU legs,
+    which build the benchmark mesh without the GPU library) gives the
+    library's permuted mesh array for array."""
+    from oracle import OracleMesh
+    for kind, nx, ny in (("cartesian_tri", 37, 23), ("cartesian", 20, 9), ("wedge", 30, 10)):
+        m = mg.Mesh.generate(kind, nx, ny, 1.0, 1.0)
+        p_lib = m.permute_cells(20261203)
+        om = OracleMesh.generate(kind, nx, ny, 1.0, 1.0)
+        p_ora = om.permute_cells(20261203)
+        np.testing.assert_array_equal(p_lib, p_ora)
+        for k in ("node_coords", "cell_coords", "cell_volume", "offsets_nodes_of_cell", "nodes_of_cell",
+                  "offsets_faces_of_cell", "faces_of_cell", "cells_of_face", "zone_offsets", "zone_faces"):
+            np.testing.assert_array_equal(np.asarray(getattr(m, k)), np.asarray(getattr(om, k)), err_msg=f"{kind} {k}")
