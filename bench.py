@@ -9,36 +9,45 @@ unit square, relabelled by a seeded random cell permutation (seed 20261203)
 and reverse-Cuthill-McKee ordered inside the library; TENO p = 3 (legendre),
 HLLC, SSPRK3 with CFL 0.5, extrapolation (transmissive) boundaries, gamma
 1.4, quadrant states split at x = y = 0.8.  Synthetic, seeded data.  The
-TENO weighting is the corrected variant (same work per cell as the
-reference's weighting, which turns this state non-finite within one step).
+TENO weighting is the robust variant (the corrected cut-off weighting with
+first-order boundary cells, a range scaling and a positivity fallback per
+cell, and a guarded HLLC star pressure): it runs this state to t = 0.3,
+which the reference's weighting (non-finite within one step) and the
+corrected one (within ~15 steps) do not.
 
 Forms (all on the GPU, same mesh, state and steps):
-  fp64          the plain path, the reference's arithmetic (the parity path)
+  fp64          the plain path, FP64 with the reference's operation order
   fp64_fast     FP64 with FMA contraction
   fp32          reconstruction and flux in FP32, state and accumulation FP64
   fp32_learned  fp32 + the learned stencil selector (the headline by default)
 The headline line carries the headline form's rate, and "forms" every
 form's rate, per-kernel times and its density L1 / L-infinity and mass /
-energy differences against the plain FP64 state after the same steps.
+energy differences against the plain FP64 state after the same steps.  A
+timed state that is not finite, or a non-zero status word, prints a
+"status" line without a value and exits 1.
 
 One step = spectral radius + dt + three stages of (reconstruction, face flux,
 residual gather + update), plus one selector inference every second step in
-the learned form (--sel-interval), all on the GPU, replayed as CUDA graphs.  Inputs (tables
-7-15 GB) are far larger than L2, so no explicit flush is done.
+the learned form (--sel-interval), all on the GPU, replayed as CUDA graphs.
+Inputs (tables 3.4-7 KB per cell, 7-15 GB) are far larger than L2, so no
+explicit flush is done.
 
 Metric: Mcell-updates/s = cells x steps / seconds / 1e6 (one cell-update =
 one cell advanced one full SSPRK3 step).
 
-A second section, "wedge", times the 4M-cell supersonic wedge workload:
-the supersonic ramp channel (Delaunay mesh, viscous at Re 1e5 with no-slip
-walls), plain FP64 against FP32 + learned selector, with the learned
-form's density error.  A third,
-"batched", times the ensemble workload: 256 four-quadrant cases of uneven mesh
-size stepped together by the batched FP32 form.
+Further sections of the line: "end_time" runs the four-quadrant problem to
+t = 0.3 (the learned form at the headline size; the plain FP64 path and the
+learned form at --end-time-n, with the error between them); "c5" times the
+learned form against the plain FP64 path on 2048^2 (8.4M cells); "wedge"
+times the 4M-cell supersonic wedge (Delaunay ramp channel, viscous at Re 1e5
+with no-slip walls), plain FP64 against FP32 + learned selector; "batched"
+runs the ensemble workload (256 four-quadrant cases of uneven mesh size) to
+its 500 steps with the batched FP32 form.
 
 --impl reference times the CPU oracle (the restatement of the reference's
-algorithm, FP64, all host threads) on a 256 x 256 sample of the same
-workload.
+algorithm, FP64, all host threads) on the same 1024^2 mesh, built by the
+oracle's own mesh generator and cell permutation (the GPU library is not
+loaded in that process).
 """
 
 import argparse
@@ -51,6 +60,8 @@ import threading
 import time
 from pathlib import Path
 
+import numpy as np
+
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 sys.path.insert(0, str(ROOT / "tests"))
@@ -59,9 +70,16 @@ METRIC = "Mcell-updates/s on 1 GB300: FP64 plain vs FP32+learned TENO at matched
 UNIT = "Mcell-updates/s"
 SEED = 20261203
 CFL = 0.5
+T_END = 0.3
 CPU_SAMPLE_N = 256
 SEL_THRESHOLD = 0.98
 WEDGE_CFL = 0.4
+GAS = dict(gamma=1.4, p_ref=101325.0, T_ref=298.15, rho_ref=1.225)
+# the four-quadrant states (rho, u, v, p) of UR, UL, LL, LR
+QUADRANTS = ((1.5, 0.0, 0.0, 1.5),
+             (0.532258064516129, 1.206045378311055, 0.0, 0.3),
+             (0.137992831541219, 1.206045378311055, 1.206045378311055, 0.029032258064516),
+             (0.532258064516129, 0.0, 1.206045378311055, 0.3))
 
 
 def parse():
@@ -71,21 +89,28 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=1024, help="quads per side (cells = 2 n^2)")
-    ap.add_argument("--variant", default="corrected", choices=["reference", "corrected"])
+    ap.add_argument("--variant", default="robust", choices=["reference", "corrected", "robust"])
     ap.add_argument("--form", default="fp32_learned", choices=["fp64", "fp64_fast", "fp32", "fp32_learned"],
                     help="headline form: fp64 = the reference's rounding (bit-faithful); fp64_fast = FMA-contracted "
                          "FP64; fp32 = FP32-bulk reconstruction and flux; fp32_learned = fp32 + learned selector")
     ap.add_argument("--forms", default="fp64,fp64_fast,fp32",
                     help="other forms timed on the same workload (comma list, '' for none); fp64 is also the "
                          "error reference")
+    ap.add_argument("--end-time-n", type=int, default=256,
+                    help="mesh size of the end-time accuracy run (plain FP64 and learned form to t = 0.3); 0 skips "
+                         "the end-time section")
+    ap.add_argument("--c5-n", type=int, default=2048, help="mesh size of the c5 section (0 skips it)")
     ap.add_argument("--wedge-n", type=int, default=816,
                     help="rows of the ramp-channel lattice (3n+1 columns; 816 -> 4.0M triangles); 0 skips it")
     ap.add_argument("--wedge-develop", type=int, default=300,
                     help="untimed steps of the wedge from its uniform start before the timed ones")
     ap.add_argument("--wedge-re", type=float, default=1e5,
                     help="Reynolds number of the wedge on the ramp length (viscous flux, no-slip walls); 0 = inviscid")
+    ap.add_argument("--wedge-variant", default="corrected", choices=["corrected", "robust"],
+                    help="TENO variant of the wedge (the corrected one keeps high order in the wall cells)")
     ap.add_argument("--batch-cases", type=int, default=256,
                     help="cases of the batched section (the four-quadrant ensemble); 0 skips it")
+    ap.add_argument("--batch-steps", type=int, default=500, help="total steps of the batched section")
     ap.add_argument("--sel-interval", type=int, default=2,
                     help="steps per selector prediction in the learned form (1 = every step; 2 keeps stale "
                          "predictions inside the neighbour check's one-cell margin at CFL <= 0.5)")
@@ -98,6 +123,28 @@ def parse():
 
 def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
+
+
+def four_quadrant_state(cell_coords, split=0.8):
+    """Conservatives and primitives of the four-quadrant state per cell, as
+    the reference's analytical initialisation computes them
+    (src/solver/solver_initialize.cpp:159-185, physics.cpp:69-73)."""
+    x, y = cell_coords[:, 0], cell_coords[:, 1]
+    right, top = x >= split, y >= split
+    prim = np.zeros((len(x), 4))
+    for sel, st in zip((right & top, ~right & top, ~right & ~top, right & ~top), QUADRANTS):
+        prim[sel] = st
+    g = GAS["gamma"]
+    R = GAS["p_ref"] / (GAS["T_ref"] * GAS["rho_ref"])
+    cp = R * g / (g - 1.0)
+    cv = cp / g
+    rho, u, v, p = prim.T
+    T = p / (rho * R)
+    e = cv * T
+    E = e + 0.5 * (u * u + v * v)
+    h = e + p / rho
+    return (np.ascontiguousarray(np.stack([rho, rho * u, rho * v, rho * E], 1)),
+            np.ascontiguousarray(np.stack([u, v, p, T, h], 1)))
 
 
 def case_mesh(n):
@@ -171,55 +218,55 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
-# CPU oracle leg
+# CPU oracle legs (no GPU library in these: the oracle's own mesh generator
+# and cell permutation build the same mesh)
 # ---------------------------------------------------------------------------
 
-def cpu_oracle_rate(n, steps, warmup, variant, reps=1):
-    """Cell-updates/s of the oracle on an n x n sample, all host threads:
-    reps x steps timed steps, each repetition from the initial state (the
-    state is reset outside the timed region; the four-quadrant state stays
-    finite over the first ~15 steps at this size)."""
-    import numpy as np  # noqa: F401
-    from cases import four_quadrant
+def oracle_case(n, variant, threads):
     from oracle import Oracle, OracleCase, OracleMesh
-    m = case_mesh(n)
-    o = Oracle()
-    threads = max(1, os.cpu_count() or 1)
-    o.set_threads(threads)
-    oc = OracleCase(OracleMesh.from_arrays(m), recon="TENO", basis="legendre", poly_order=3, riemann="HLLC")
-    oc.set_teno_variant(0 if variant == "reference" else 1)
+    Oracle().set_threads(threads)
+    om = OracleMesh.generate("cartesian_tri", n, n, 1.0, 1.0)
+    om.permute_cells(SEED)
+    oc = OracleCase(om, recon="TENO", basis="legendre", poly_order=3, riemann="HLLC", **GAS)
+    oc.set_teno_variant({"reference": 0, "corrected": 1, "robust": 2}[variant])
     for z in range(1, 5):
         oc.add_boundary(z, "extrapolation")
-    U, W = four_quadrant(m)
+    U, W = four_quadrant_state(om.cell_coords)
     oc.set_state(U, W)
+    return oc, om.n_cells
+
+
+def cpu_oracle_rate(n, steps, warmup, variant):
+    """Cell-updates/s of the oracle on the n x n workload, all host threads:
+    W untimed then K timed consecutive steps from the initial state."""
+    threads = max(1, os.cpu_count() or 1)
+    t0 = time.perf_counter()
+    oc, cells = oracle_case(n, variant, threads)
+    setup = time.perf_counter() - t0
     if warmup:
         oc.run(CFL, warmup)
-    dt = 0.0
-    for _ in range(reps):
-        oc.set_state(U, W)
-        t0 = time.perf_counter()
-        oc.run(CFL, steps)
-        dt += time.perf_counter() - t0
-    return m.n_cells * steps * reps / dt / 1e6, threads, dt, m.n_cells
+    t0 = time.perf_counter()
+    oc.run(CFL, steps)
+    secs = time.perf_counter() - t0
+    U, _ = oc.get_state()
+    return cells * steps / secs / 1e6, threads, secs, cells, setup, bool(np.isfinite(U).all())
 
 
 def run_reference(args):
     rank, _, world = dist_env()
     if rank != 0:
         return
-    # K timed steps as repetitions of at most 8 from the initial state (the
-    # four-quadrant state stays finite over its first ~15 steps at 256^2)
-    per = max(1, min(8, args.steps))
-    reps = (args.steps + per - 1) // per
-    rate, threads, secs, cells = cpu_oracle_rate(args.cpu_sample_n, per, args.warmup, args.variant, reps=reps)
-    sample = (f"cartesian_tri {args.cpu_sample_n}x{args.cpu_sample_n} ({cells} cells) of the same workload, "
-              f"{reps} x {per} timed steps from the initial state after {args.warmup} warm-up, "
-              f"{threads} OpenMP threads")
+    rate, threads, secs, cells, setup, finite = cpu_oracle_rate(args.n, args.steps, args.warmup, args.variant)
+    sample = (f"the full workload: cartesian_tri {args.n}x{args.n} ({cells} cells), {args.steps} timed steps after "
+              f"{args.warmup} warm-up, {threads} OpenMP threads (setup {setup:.1f} s untimed)")
     line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs * 1e3 / (reps * per),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs * 1e3 / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": dict(workload_config(args, args.n), form="reference CPU path (oracle port, FP64)",
-                           timed_steps=reps * per),
+            "config": workload_config(args, args.n),
+            "reference_path": "CPU oracle (oracle/mallard_oracle.cpp: the reference's algorithm restated, FP64, "
+                              "OpenMP with atomic scatter like Kokkos::OpenMP); the reference itself does not build "
+                              "here (its Kokkos, KokkosKernels and toml11 submodules are empty)",
+            "finite": finite,
             "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -284,23 +331,36 @@ def make_solver(m, args, form, device, selector):
     prec, learned = FORMS[form]
     s = mg.Solver(m, face_reconstruction="TENO", basis_type="legendre", basis_order=3, riemann_solver="HLLC",
                   boundaries=[{"name": z, "type": "extrapolation"} for z in ("right", "top", "left", "bottom")],
-                  teno_variant=args.variant, reorder=True, device=device, precision=prec)
+                  teno_variant=args.variant, reorder=True, device=device, precision=prec, **GAS)
     if learned:
         s.attach_selector(selector[0], threshold=SEL_THRESHOLD, interval=args.sel_interval)
     return s
 
 
 def errors_vs(m, U, U_ref):
-    import numpy as np
     vol = m.cell_volume
-    if not (np.isfinite(U).all() and np.isfinite(U_ref).all()):
-        return {"finite": bool(np.isfinite(U).all())}
+    fin = bool(np.isfinite(U).all() and np.isfinite(U_ref).all())
+    if not fin:
+        return {"finite": False, "density_l1_rel_err": None, "density_linf_rel_err": None}
     d = np.abs(U[:, 0] - U_ref[:, 0])
+    i = int(np.argmax(d))
     return {"density_l1_rel_err": float(np.sum(vol * d) / np.sum(vol * np.abs(U_ref[:, 0]))),
             "density_linf_rel_err": float(d.max() / np.abs(U_ref[:, 0]).max()),
+            "density_linf_at": [round(float(x), 4) for x in m.cell_coords[i]],
             "mass_rel_diff": float(abs(np.sum(vol * U[:, 0]) - np.sum(vol * U_ref[:, 0])) / np.sum(vol * U_ref[:, 0])),
             "energy_rel_diff": float(abs(np.sum(vol * U[:, 3]) - np.sum(vol * U_ref[:, 3])) /
                                      np.sum(vol * U_ref[:, 3]))}
+
+
+def autotune(s, args, U0, W0):
+    if args.shape >= 0:
+        s.set_launch_shape(args.shape)
+        return {"chosen_shape": args.shape, "ms_per_shape": None, "shapes": "fixed by --shape"}
+    shape, tms = s.autotune()
+    s.set_state(U0, W0)
+    return {"chosen_shape": shape, "ms_per_shape": [round(x, 4) for x in tms],
+            "shapes": "0: 128 thr/<=128 regs, 1: 128/<=80, 2: 128/<=64, 3: 256/<=64, "
+                      "4-6: staged (bulk copies to shared memory) 1 slot x 4 warps/<=80, 2 x 2/<=128, 1 x 4/<=128"}
 
 
 def time_form(m, args, form, U0, W0, device, selector, barrier=None, clocks=None):
@@ -313,17 +373,7 @@ def time_form(m, args, form, U0, W0, device, selector, barrier=None, clocks=None
     stream = torch.cuda.Stream()
     s.set_stream(stream.cuda_stream)
     s.set_state(U0, W0)
-    tune = None
-    if FORMS[form][0] == "fp32" and args.shape >= 0:
-        s.set_launch_shape(args.shape)
-        tune = {"chosen_shape": args.shape, "ms_per_shape": None, "shapes": "fixed by --shape"}
-    elif FORMS[form][0] == "fp32":
-        shape, tms = s.autotune()
-        tune = {"chosen_shape": shape, "ms_per_shape": [round(x, 4) for x in tms],
-                "shapes": "0: 128 thr/<=128 regs, 1: 128/<=80, 2: 128/<=64, 3: 256/<=64, "
-                          "4-6: staged (bulk copies to shared memory) 1 slot x 4 warps/<=80, 2 x 2/<=128, "
-                          "1 x 4/<=128"}
-        s.set_state(U0, W0)
+    tune = autotune(s, args, U0, W0) if FORMS[form][0] == "fp32" else None
     s.launch(CFL, args.warmup)
     s.synchronize()
     if clocks:
@@ -353,6 +403,136 @@ def time_form(m, args, form, U0, W0, device, selector, barrier=None, clocks=None
     return s, {"ms": ms, "U": U, "flags": flags, "stats": stats, "kt": kt, "clocks": clk, "tune": tune}
 
 
+def kernel_bytes(kind, precision, learned, cells, faces, solver, stats):
+    """Algorithmic (compulsory) bytes of one launch of a kernel class:
+    recon: the library's traffic model (tables of the stencils evaluated,
+    shapes, face slots, the state gathered once per cell, face states
+    written); flux: per flux face the face states of both sides, the flux x
+    area written and the face geometry; update: per cell the gather list,
+    1/volume and the state rows one SSPRK3 stage reads and writes (averaged
+    over the three), plus every face's flux once; cfl: per cell its faces,
+    its state row and the radius, per face its cells, normal and 1/distance;
+    selector: neighbour ids of all stencils, the state gathered once per
+    cell, predictions, the weight image per 128-cell CTA."""
+    fp32 = precision == "fp32"
+    fw = 4 if fp32 else 8
+    if kind == "recon":
+        full, _ = solver.traffic_model()
+        if learned and stats:
+            per_stencil = 19 * (4 + 4 * 9)
+            return stats["stencils_evaluated"] * per_stencil + full - stats["stencils_full"] * per_stencil + cells * 4
+        return full
+    if kind == "flux":
+        return faces * (2 * 2 * 4 * fw + 32 + 8 + 16 + 8 + 1)
+    if kind == "update":
+        rows = (96 + 160 + 64) / 3.0 + (16 if fp32 else 16.0)
+        return cells * (16 + 8 + rows) + faces * 32
+    if kind == "cfl":
+        return cells * (16 + (16 if fp32 else 32 + 48) + 8) + faces * (8 + 16 + 8)
+    if kind == "selector" and stats:
+        return stats["stencils_full"] * 19 * 4 + cells * (32 + 4) + (cells + 127) // 128 * 25216
+    return 0
+
+
+def run_until(s, t_end, chunk=50):
+    """Steps s until its simulated time reaches t_end (the last chunk ends
+    there or later); returns (time, steps, wall seconds)."""
+    t, steps = 0.0, 0
+    t0 = time.perf_counter()
+    while t < t_end:
+        k = 1 if t_end - t < 0.02 else chunk
+        t += s.run(CFL, k)
+        steps += k
+        if s.status() != 0:
+            break
+    return t, steps, time.perf_counter() - t0
+
+
+def run_end_time(args, device, selector):
+    """The four-quadrant problem to t = 0.3 (its end time): the learned form
+    on the headline mesh (finite, steps, wall time), and at --end-time-n the
+    plain FP64 path and the learned form, stepped to the same time with the
+    same number of steps, with the error between them."""
+    import mallard_gb300 as mg  # noqa: F401
+    out = {"t_end": T_END}
+    m = case_mesh(args.n)
+    U0, W0 = four_quadrant_state(m.cell_coords)
+    s = make_solver(m, args, "fp32_learned", device, selector)
+    s.set_state(U0, W0)
+    s.autotune()
+    s.set_state(U0, W0)
+    t, steps, wall = run_until(s, T_END)
+    U, _ = s.get_state()
+    vol = m.cell_volume
+    out[f"{args.n}x{args.n}"] = {"form": "fp32_learned", "t": t, "steps": steps, "wall_s": wall,
+                                 "finite": bool(np.isfinite(U).all()) and s.status() == 0,
+                                 "density_min": float(U[:, 0].min()), "density_max": float(U[:, 0].max()),
+                                 "mass": float(np.sum(vol * U[:, 0]))}
+    s.close()
+    n = args.end_time_n
+    if n > 0:
+        m = case_mesh(n)
+        U0, W0 = four_quadrant_state(m.cell_coords)
+        ref = make_solver(m, args, "fp64", device, selector)
+        ref.set_state(U0, W0)
+        t64, steps64, wall64 = 0.0, 0, time.perf_counter()
+        while t64 < T_END and ref.status() == 0:
+            t64 += ref.run(CFL, 1)
+            steps64 += 1
+        wall64 = time.perf_counter() - wall64
+        Ur, _ = ref.get_state()
+        ref.close()
+        s = make_solver(m, args, "fp32_learned", device, selector)
+        s.set_state(U0, W0)
+        tl = s.run(CFL, steps64)
+        Ul, _ = s.get_state()
+        rec = {"steps": steps64, "t_fp64": t64, "t_learned": tl, "fp64_wall_s": wall64,
+               "finite": bool(np.isfinite(Ul).all() and np.isfinite(Ur).all()) and s.status() == 0,
+               "selector": selector_summary(selector, s.selector_stats(), args.sel_interval)}
+        rec.update(errors_vs(m, Ul, Ur))
+        s.close()
+        out[f"{n}x{n}_learned_vs_fp64"] = rec
+    return out
+
+
+def run_c5(args, device, selector):
+    """The learned form against the plain FP64 path on the 2048^2
+    four-quadrant mesh (8,388,608 cells): W + K steps each, rates and the
+    density error after the same steps."""
+    import torch
+    n = args.c5_n
+    m = case_mesh(n)
+    U0, W0 = four_quadrant_state(m.cell_coords)
+    out = {"workload": f"four-quadrant Riemann, cartesian_tri {n}x{n} -> {m.n_cells} triangles, seeded permutation "
+                       f"+ RCM, TENO p3 ({args.variant}) + HLLC, CFL {CFL}", "cells": m.n_cells}
+    finals = {}
+    for form in ("fp64", "fp32_learned"):
+        s = make_solver(m, args, form, device, selector)
+        stream = torch.cuda.Stream()
+        s.set_stream(stream.cuda_stream)
+        s.set_state(U0, W0)
+        if form == "fp32_learned":
+            s.autotune()
+            s.set_state(U0, W0)
+        s.launch(CFL, args.warmup)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        s.launch(CFL, args.steps)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        finals[form] = s.get_state()[0]
+        out[form] = {"value": m.n_cells * args.steps / (ms * 1e-3) / 1e6, "ms_per_step": ms / args.steps,
+                     "finite": bool(np.isfinite(finals[form]).all()) and s.status() == 0}
+        if form == "fp32_learned":
+            out[form]["selector"] = selector_summary(selector, s.selector_stats(), args.sel_interval)
+        s.close()
+    out["fp32_learned"].update(errors_vs(m, finals["fp32_learned"], finals["fp64"]))
+    out["speedup_learned_vs_fp64"] = out["fp32_learned"]["value"] / out["fp64"]["value"]
+    return out
+
+
 def run_wedge(args, device, selector):
     """The supersonic ramp channel (15 degree ramp at x = 0.5 in a 3 x 1
     channel, jittered-lattice Delaunay mesh of 2 nx ny triangles, Mach 2.5
@@ -363,7 +543,6 @@ def run_wedge(args, device, selector):
     uniform flow, which flatters the selector), then runs W warm-up and K
     timed steps; the learned form's density error is taken against the
     plain one after all of them."""
-    import numpy as np
     import torch
 
     import mallard_gb300 as mg
@@ -376,13 +555,13 @@ def run_wedge(args, device, selector):
     flow = (f"viscous Re {re:g} on the ramp length, Pr 0.72, Sutherland, no-slip adiabatic walls" if re
             else "inviscid (slip walls)")
     out = {"workload": f"ramp channel {nx}x{ny} lattice -> {mesh.n_cells} Delaunay triangles, 15 deg ramp, "
-                       f"Mach 2.5, TENO p3 + Rusanov, SSPRK3 CFL {WEDGE_CFL}, {flow}; timed after "
-                       f"{args.wedge_develop} development steps",
+                       f"Mach 2.5, TENO p3 ({args.wedge_variant}) + Rusanov, SSPRK3 CFL {WEDGE_CFL}, {flow}; timed "
+                       f"after {args.wedge_develop} development steps",
            "cells": mesh.n_cells, "mesh_s": time.perf_counter() - t0, "develop_steps": args.wedge_develop}
     finals = {}
     for form, prec in (("fp64", "fp64"), ("fp32_learned", "fp32")):
         t1 = time.perf_counter()
-        s, U0, W0 = wedge_setup(mesh, precision=prec, reynolds=re)
+        s, U0, W0 = wedge_setup(mesh, precision=prec, reynolds=re, teno_variant=args.wedge_variant)
         if form == "fp32_learned":
             s.attach_selector(selector[0], threshold=SEL_THRESHOLD, interval=args.sel_interval)
         setup = time.perf_counter() - t1
@@ -422,8 +601,9 @@ def run_batched(args, device):
     squares, mesh size drawn per case from {64, 128, 256, 512}^2 quads
     (cartesian_tri, so twice as many triangles), quadrant states drawn per
     case (rho ~ U[0.1, 2], p ~ U[0.03, 2], u, v ~ U[-1.5, 1.5]); the
-    batched FP32 form with one launch per kernel over all cases, autotuned."""
-    import numpy as np
+    batched FP32 form with one launch per kernel over all cases, autotuned.
+    W warm-up and K timed steps, then the rest of --batch-steps untimed;
+    finite_cases counts the cases finite after all of them."""
     import torch
 
     import mallard_gb300 as mg
@@ -437,7 +617,7 @@ def run_batched(args, device):
     meshes = [mg.Mesh.generate("cartesian_tri", sizes[i], sizes[i], 1.0, 1.0) for i in used]
     b = Batch(meshes, [counts[i] for i in used],
               boundaries=[{"name": z, "type": "extrapolation"} for z in ("right", "top", "left", "bottom")],
-              riemann_solver="HLLC")
+              riemann_solver="HLLC", teno_variant=args.variant, **GAS)
     cells = 0
     for g, i in enumerate(used):
         m = meshes[g]
@@ -448,7 +628,7 @@ def run_batched(args, device):
             sx, sy = r.uniform(0.3, 0.7, 2)
             quad = np.where(x >= sx, np.where(y >= sy, 0, 3), np.where(y >= sy, 1, 2))
             pr = q[quad]
-            U, W = mg.state_from_primitives(pr[:, 0], pr[:, 1], pr[:, 2], pr[:, 3])
+            U, W = mg.state_from_primitives(pr[:, 0], pr[:, 1], pr[:, 2], pr[:, 3], **GAS)
             b.set_state(g, k, U, W)
             cells += m.n_cells
     setup = time.perf_counter() - t0
@@ -465,48 +645,34 @@ def run_batched(args, device):
     e1.record(stream)
     e1.synchronize()
     secs = e0.elapsed_time(e1) * 1e-3
-    per_step = []
-    for _ in range(2):  # two more steps one by one, to see whether the step time changes as cases fail
-        e0.record(stream)
-        b.run(CFL, 1)
-        e1.record(stream)
-        e1.synchronize()
-        per_step.append(e0.elapsed_time(e1))
+    flags_timed, _ = b.status()
+    rest = max(0, args.batch_steps - args.warmup - args.steps)
+    t1 = time.perf_counter()
+    if rest:
+        b.run(CFL, rest)
+        b.synchronize()
+    rest_s = time.perf_counter() - t1
     flags, times = b.status()
     b.close()
     case_cells = np.concatenate([np.full(counts[i], meshes[g].n_cells) for g, i in enumerate(used)])
-    live = int(case_cells[flags == 0].sum())
+    live = int(case_cells[flags_timed == 0].sum())
     return {"workload": f"{args.batch_cases} four-quadrant cases, cartesian_tri sizes {{64,128,256,512}}^2 quads "
-                        f"drawn per case (seed {SEED}), random quadrant states, TENO p3 + HLLC, SSPRK3 CFL {CFL}, "
-                        f"FP32 form, one launch per kernel over all cases",
+                        f"drawn per case (seed {SEED}), random quadrant states, TENO p3 ({args.variant}) + HLLC, "
+                        f"SSPRK3 CFL {CFL}, FP32 form, one launch per kernel over all cases",
             "cases_per_size": {f"{sizes[i]}x{sizes[i]}": counts[i] for i in range(4)}, "cells": cells,
             "value": live * args.steps / secs / 1e6, "unit": UNIT, "ms_per_step": secs * 1e3 / args.steps,
-            "value_counts": "cells of the cases still finite after the timed steps (a failed case is frozen and "
-                            "does no further work)",
-            "live_cells": live,
+            "value_counts": "cells of the cases finite after the timed steps", "live_cells": live,
             "timing": "CUDA events on the batch's stream around the graph replays",
-            "ms_next_steps": per_step,
             "autotune": {"shape": shape, "ctas_per_sm": bps, "ms": np.round(ms, 4).tolist()},
-            "finite_cases": int((flags == 0).sum()), "setup_s": setup}
-
-
-def recon_bytes_selected(solver, stats, cells):
-    """Compulsory bytes of one selector-driven reconstruction launch: the
-    tables of the stencils actually evaluated plus the per-cell constants
-    (shapes, face slots, stencil mask, prediction, state, face states)."""
-    full_bytes, _ = solver.traffic_model()
-    per_stencil = 19 * (4 + 4 * 9)
-    fixed = full_bytes - stats["stencils_full"] * per_stencil
-    return stats["stencils_evaluated"] * per_stencil + fixed + cells * 4
+            "total_steps": args.warmup + args.steps + rest, "rest_wall_s": rest_s,
+            "finite_cases": int((flags == 0).sum()), "case_time_min": float(times.min()),
+            "case_time_max": float(times.max()), "setup_s": setup}
 
 
 def run_ours(args):
-    import numpy as np
-    import torch
+    import torch  # noqa: F401
 
     import mallard_gb300 as mg
-    from cases import four_quadrant
-
     from mallard_gb300.replicas import Replicas
 
     reps = Replicas("nccl")
@@ -515,10 +681,12 @@ def run_ours(args):
 
     t_setup = time.perf_counter()
     m = case_mesh(args.n)
-    U0, W0 = four_quadrant(m)
+    U0, W0 = four_quadrant_state(m.cell_coords)
     cells = m.n_cells
+    faces = int(m.zone_offsets[-1])
     head = args.form
-    selector = load_selector(local) if FORMS[head][1] or "fp32_learned" in args.forms.split(",") else None
+    need_sel = FORMS[head][1] or "fp32_learned" in args.forms.split(",") or args.end_time_n or args.c5_n
+    selector = load_selector(local) if need_sel else None
     setup_s = time.perf_counter() - t_setup
 
     # ---- the other forms (the plain FP64 path's final state is the error reference)
@@ -543,6 +711,14 @@ def run_ours(args):
     Uend, flags, kt, clk, stats = r["U"], r["flags"], r["kt"], r["clocks"], r["stats"]
     finite = bool(np.isfinite(Uend).all()) and flags == 0
     finals[head] = Uend
+    if not finite:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                              "warmup": args.warmup, "status": "invalid: the timed state is not finite "
+                                                               f"(status flags {flags}); no value is reported",
+                              "config": workload_config(args, args.n)}), flush=True)
+        reps.close()
+        sys.exit(1)
 
     # ---- end to end through the public API with host buffers: each step
     # uploads the conserved state from pinned memory (the primitives are
@@ -563,7 +739,7 @@ def run_ours(args):
     d2h = cells * 4 * 8
 
     # ---- roofline of the dominant kernel
-    recon_bytes, stage_bytes = solver.traffic_model()
+    _, stage_bytes = solver.traffic_model()
     peaks = {}
     pk = ROOT / "MEASURED_PEAKS.json"
     if pk.exists():
@@ -574,33 +750,30 @@ def run_ours(args):
               for k, v in kt.items() if v[1]}
     dom = max(kshare, key=lambda k: kshare[k]["share"])
     learned = FORMS[head][1]
+    prec = FORMS[head][0]
     staged = bool(r["tune"]) and r["tune"]["chosen_shape"] >= 4
     fp32_name = "teno32_staged_kernel" if staged else "teno32_kernel"
     kernel_names = {"recon": (f"{fp32_name}<10,20,2,SEL>" if learned else
-                              (f"{fp32_name}<10,20,2>" if FORMS[head][0] == "fp32" else "teno_kernel<10,20,2>")),
-                    "selector": "mlp_kernel<1> (tcgen05)", "flux": "flux kernel", "update": "update_kernel",
-                    "cfl": "spectral_kernel"}
-    dom_ms, dom_n = kt[dom]
-    dom_s = dom_ms / max(dom_n, 1) * 1e-3
-    if dom == "recon":
-        algo = recon_bytes_selected(solver, stats, cells) if learned else recon_bytes
-    elif dom == "selector":
-        # nb4 indices of all stencils, the state gathered once per cell, predictions, weight image per CTA
-        algo = (stats["stencils_full"] * 19 * 4 + cells * (32 + 4) + (cells + 127) // 128 * 25216) if stats else 0
-    else:
-        algo = 0
-    achieved = algo / dom_s / 1e9 if algo else None
+                              (f"{fp32_name}<10,20,2>" if prec == "fp32" else "teno_kernel<10,20,2>")),
+                    "selector": "mlp_kernel<1> (tcgen05)", "flux": "flux32_kernel" if prec == "fp32" else "flux_kernel",
+                    "update": "update_kernel", "cfl": "spectral_kernel"}
+    for k in kshare:
+        kshare[k]["algorithmic_bytes_per_launch"] = kernel_bytes(k, prec, learned, cells, faces, solver, stats)
+        kshare[k]["achieved_gbs"] = kshare[k]["algorithmic_bytes_per_launch"] / (kshare[k]["ms_per_launch"] * 1e-3) / 1e9
+    algo = kshare[dom]["algorithmic_bytes_per_launch"]
+    achieved = kshare[dom]["achieved_gbs"]
     traffic = None
     tf = ROOT / "profiles" / "teno_recon_traffic.json"
     if tf.exists() and dom == "recon":
         t = json.loads(tf.read_text())
-        key = "fp32_learned" if learned else FORMS[head][0]
+        key = "fp32_learned" if learned else prec
         per_cell = t.get("dram_bytes_per_cell_by_form", {}).get(key)
         traffic = per_cell * cells if per_cell else None
     roofline = {"bound": "hbm", "kernel": kernel_names.get(dom, dom), "achieved": achieved, "peak": hbm_peak,
-                "unit": "GB/s", "frac": achieved / hbm_peak if achieved else None,
+                "unit": "GB/s", "frac": achieved / hbm_peak,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if pk.exists() else "fallback 6800 GB/s",
-                "traffic": traffic, "algorithmic_bytes_per_launch": algo}
+                "traffic": traffic, "algorithmic_bytes_per_launch": algo,
+                "timing": "CUDA events around every launch on the solver's stream (a second pass of W + K steps)"}
     # 11 per step; the selector's inference and neighbour check on the
     # prediction steps (the first of the timed call, then every interval)
     pred_steps = -(-args.steps // max(args.sel_interval, 1)) if learned else 0
@@ -620,37 +793,43 @@ def run_ours(args):
                 forms[form].update(errors_vs(m, U, finals["fp64"]))
         if head != "fp64":
             accuracy = {k: forms[head].get(k) for k in ("density_l1_rel_err", "density_linf_rel_err",
-                                                        "mass_rel_diff", "energy_rel_diff")}
-            accuracy["against"] = "plain FP64 GPU path (bit-faithful to the reference's arithmetic), same steps"
+                                                        "density_linf_at", "mass_rel_diff", "energy_rel_diff")}
+            accuracy["against"] = "plain FP64 GPU path (the reference's operation order), same steps"
             accuracy["bar"] = "density L1 <= 1e-3"
+    # the plain FP64 path's binding roof is the FP64 unit: its reconstruction's flops per second
     fp64_roof = None
-    if FORMS[head][0].startswith("fp64"):
-        flops_cell = teno_flops_per_cell(FORMS[head][0])
+    fp64_kt = forms.get("fp64", {}).get("kernel_ms_per_launch", {})
+    if "recon" in fp64_kt:
+        flops_cell = teno_flops_per_cell("fp64")
         fp64_peak = mg.fp64_peak_gflops(local)
-        rs = kt["recon"][0] / max(kt["recon"][1], 1) * 1e-3
-        fp64_roof = {"achieved_gflops": flops_cell * cells / rs / 1e9, "peak_gflops": fp64_peak,
+        rs = fp64_kt["recon"] * 1e-3
+        fp64_roof = {"form": "fp64", "kernel": "teno_kernel<10,20,2>",
+                     "achieved_gflops": flops_cell * cells / rs / 1e9, "peak_gflops": fp64_peak,
                      "frac": flops_cell * cells / rs / 1e9 / fp64_peak, "flops_per_cell": flops_cell,
                      "peak_source": "measured FMA-chain probe on this GPU"}
 
+    end_time = run_end_time(args, local, selector) if args.end_time_n >= 0 else None
+    c5 = run_c5(args, local, selector) if args.c5_n > 0 else None
     wedge = run_wedge(args, local, selector or load_selector(local)) if args.wedge_n > 0 else None
     batched = run_batched(args, local) if args.batch_cases > 0 else None
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        rate, threads, secs, ccells = cpu_oracle_rate(args.cpu_sample_n, 8, 1, args.variant, reps=12)
+        rate, threads, secs, ccells, csetup, cfin = cpu_oracle_rate(args.cpu_sample_n, 64, 1, args.variant)
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"cartesian_tri {args.cpu_sample_n}x{args.cpu_sample_n} ({ccells} cells) of the same "
-                         f"workload, FP64 plain, 12 x 8 steps from the initial state after 1 warm-up, "
-                         f"{threads} OpenMP threads, {secs:.1f} s timed"}
+                         f"workload, FP64 plain, 64 steps after 1 warm-up, {threads} OpenMP threads, "
+                         f"{secs:.1f} s timed (bench.py --impl reference times the full 1024x1024 mesh)",
+               "finite": cfin}
 
     if rank == 0:
         cfg = workload_config(args, args.n)
         cfg["form"] = head
-        cfg["precision"] = FORMS[head][0] + (" + learned stencil selector" if learned else "")
+        cfg["precision"] = prec + (" + learned stencil selector" if learned else "")
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None,
-                "dtype": "f32 (reconstruction, flux) + f64 (state, accumulation)" if FORMS[head][0] == "fp32" else "f64",
+                "dtype": "f32 (reconstruction, flux) + f64 (state, accumulation)" if prec == "fp32" else "f64",
                 "data": "synthetic", "config": cfg,
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
                 "gpu_launches": gpu_launches, "clocks": clk, "roofline": roofline,
@@ -660,10 +839,9 @@ def run_ours(args):
             line["fp64_roof"] = fp64_roof
         if accuracy:
             line["accuracy_vs_fp64"] = accuracy
-        if wedge:
-            line["wedge"] = wedge
-        if batched:
-            line["batched"] = batched
+        for key, sec in (("end_time", end_time), ("c5", c5), ("wedge", wedge), ("batched", batched)):
+            if sec:
+                line[key] = sec
         print(json.dumps(line), flush=True)
     reps.close()
 

@@ -114,7 +114,8 @@ def wedge_viscosity(mach=2.5, rho=1.4, p=1.0, reynolds=1e5, length=1.0, prandtl=
             "prandtl": prandtl}
 
 
-def wedge_setup(mesh, mach=2.5, rho=1.4, p=1.0, riemann="Rusanov", precision="fp64_fast", reynolds=None):
+def wedge_setup(mesh, mach=2.5, rho=1.4, p=1.0, riemann="Rusanov", precision="fp64_fast", reynolds=None,
+                teno_variant="corrected"):
     """Solver and initial state of the supersonic ramp channel: uniform inflow
     state everywhere, "upt" inflow, "p_out" outflow, walls (slip; no-slip
     and viscous when a Reynolds number is given)."""
@@ -126,7 +127,7 @@ def wedge_setup(mesh, mach=2.5, rho=1.4, p=1.0, riemann="Rusanov", precision="fp
              {"name": "wall", "type": "wall_adiabatic"}, {"name": "top", "type": "wall_adiabatic"}]
     visc = wedge_viscosity(mach, rho, p, reynolds) if reynolds else None
     s = Solver(mesh, face_reconstruction="TENO", basis_type="legendre", basis_order=3, riemann_solver=riemann,
-               boundaries=blist, teno_variant="corrected", precision=precision, viscous=visc, **GAS)
+               boundaries=blist, teno_variant=teno_variant, precision=precision, viscous=visc, **GAS)
     n = mesh.n_cells
     U, W = state_from_primitives(np.full(n, rho), np.full(n, u), np.zeros(n), np.full(n, p), **GAS)
     return s, U, W
