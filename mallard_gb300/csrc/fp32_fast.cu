@@ -603,6 +603,94 @@ __device__ __forceinline__ void visc32_face(const Visc32Args& a, int fi, int2 lr
 }
 
 // Flux of one face (local index fi) into G; VISC: minus the viscous flux.
+// One quadrature point q of face fi: its flux Ft before the weight (the
+// face states, the positivity fallback to the cell averages, the boundary
+// condition's right state, the Riemann flux).
+template <int RS, int NQ, class IX>
+__device__ __forceinline__ void flux32_point(const FluxArgs& a, const float* __restrict__ fv, const GasParams& g,
+                                             const BcTable& bct, int fi, int q, int2 lr, const float* n, int bi,
+                                             int type, const IX& ix, const double* __restrict__ Ust, float* Ft) {
+    const float gam = g.gamma_f;
+    const float4* fq = reinterpret_cast<const float4*>(fv + (ix.f(fi) * NQ + q) * 8);
+    float cl[4], cr[4], pl[5], pr[5];
+    {
+        const float4 x = fq[0];
+        cl[0] = x.x; cl[1] = x.y; cl[2] = x.z; cl[3] = x.w;
+    }
+    if (type < 0) {
+        const float4 x = fq[1];
+        cr[0] = x.x; cr[1] = x.y; cr[2] = x.z; cr[3] = x.w;
+    }
+    if (!admissible(g, cl))
+#pragma unroll
+        for (int i = 0; i < 4; i++) cl[i] = f(Ust[ix.u(lr.x) * NC + i]);
+    if (type < 0 && !admissible(g, cr))
+#pragma unroll
+        for (int i = 0; i < 4; i++) cr[i] = f(Ust[ix.u(lr.y) * NC + i]);
+    primitives_guarded(g, cl, pl);
+    if (type == MGPU_BC_WALL_ADIABATIC) {
+        Ft[0] = 0.0f;
+        Ft[1] = pl[2] * n[0];
+        Ft[2] = pl[2] * n[1];
+        Ft[3] = 0.0f;
+        return;
+    }
+    if (type < 0) {
+        primitives_guarded(g, cr, pr);
+    } else if (type == MGPU_BC_SYMMETRY) {
+#pragma unroll
+        for (int i = 0; i < 4; i++) cr[i] = cl[i];
+#pragma unroll
+        for (int i = 0; i < NPR; i++) pr[i] = pl[i];
+        const float un = pl[0] * n[0] + pl[1] * n[1];
+        pr[0] = pl[0] - 2.0f * un * n[0];
+        pr[1] = pl[1] - 2.0f * un * n[1];
+    } else if (type == MGPU_BC_EXTRAPOLATION) {
+#pragma unroll
+        for (int i = 0; i < 4; i++) cr[i] = cl[i];
+#pragma unroll
+        for (int i = 0; i < NPR; i++) pr[i] = pl[i];
+    } else if (type == MGPU_BC_UPT) {
+        const double* d = bct.bc[bi].data;
+        cr[0] = f(d[0]);
+#pragma unroll
+        for (int i = 0; i < NPR; i++) pr[i] = f(d[i + 1]);
+    } else {  // MGPU_BC_P_OUT
+        const float rho_l = cl[0];
+        const float um = sqrtf(pl[0] * pl[0] + pl[1] * pl[1]);
+        const float sos = sqrtf(gam * pl[2] / rho_l);
+        const float po = (um < sos) ? f(bct.bc[bi].data[0]) : pl[2];
+        const float T = pl[3];
+        const float rho = po / (g.R_f * T);
+        const float e = g.cv_f * T;
+        cr[0] = rho;
+        pr[0] = pl[0];
+        pr[1] = pl[1];
+        pr[2] = po;
+        pr[3] = T;
+        pr[4] = e + po / rho;
+    }
+    riemann<RS>(Ft, n, cl[0], pl, pl[2], gam, pl[4], cr[0], pr, pr[2], gam, pr[4], a.guard != 0);
+}
+
+// G of face fi from its weighted point sum F (times 1/2: the Gauss weights
+// sum to 2) and, on viscous faces, the viscous flux.  half: 0 writes
+// G[0..1], 1 writes G[2..3], 2 writes all four.  FP32 -> FP64 exactly on the
+// integer pipe (f64_of), products in FP64.
+__device__ __forceinline__ void store_G32(double* Gf4, double area, const float* F, const float* Fv, int half) {
+    double2* Gf = reinterpret_cast<double2*>(Gf4);
+    const double v1 = Fv ? area * f64_of(Fv[1]) : 0.0, v2 = Fv ? area * f64_of(Fv[2]) : 0.0,
+                 v3 = Fv ? area * f64_of(Fv[3]) : 0.0;
+    if (half != 1) {
+        const double g1 = area * f64_of(F[1] * 0.5f);
+        Gf[0] = make_double2(area * f64_of(F[0] * 0.5f), Fv ? g1 - v1 : g1);
+    }
+    if (half != 0) {
+        const double g2 = area * f64_of(F[2] * 0.5f), g3 = area * f64_of(F[3] * 0.5f);
+        Gf[1] = make_double2(Fv ? g2 - v2 : g2, Fv ? g3 - v3 : g3);
+    }
+}
+
 template <int RS, int NQ, bool VISC, class IX>
 __device__ __forceinline__ void flux32_face(const FluxArgs& a, const float* __restrict__ fv, const GasParams& g,
                                             const BcTable& bct, int fi, const IX& ix, const double* __restrict__ Ust,
@@ -612,86 +700,22 @@ __device__ __forceinline__ void flux32_face(const FluxArgs& a, const float* __re
     const float n[2] = {f(nn.x), f(nn.y)};
     const int bi = a.bc[fi];
     const int type = bi < 0 ? -1 : bct.bc[bi].type;
-    const float gam = g.gamma_f;
     float F[4] = {0.0f, 0.0f, 0.0f, 0.0f};
 #pragma unroll
     for (int q = 0; q < NQ; ++q) {
-        const float4* fq = reinterpret_cast<const float4*>(fv + (ix.f(fi) * NQ + q) * 8);
-        float cl[4], cr[4], pl[5], pr[5], Ft[4];
-        {
-            const float4 x = fq[0];
-            cl[0] = x.x; cl[1] = x.y; cl[2] = x.z; cl[3] = x.w;
-        }
-        if (type < 0) {
-            const float4 x = fq[1];
-            cr[0] = x.x; cr[1] = x.y; cr[2] = x.z; cr[3] = x.w;
-        }
-        if (!admissible(g, cl))
-#pragma unroll
-            for (int i = 0; i < 4; i++) cl[i] = f(Ust[ix.u(lr.x) * NC + i]);
-        if (type < 0 && !admissible(g, cr))
-#pragma unroll
-            for (int i = 0; i < 4; i++) cr[i] = f(Ust[ix.u(lr.y) * NC + i]);
-        primitives_guarded(g, cl, pl);
-        if (type == MGPU_BC_WALL_ADIABATIC) {
-            Ft[0] = 0.0f;
-            Ft[1] = pl[2] * n[0];
-            Ft[2] = pl[2] * n[1];
-            Ft[3] = 0.0f;
-        } else {
-            if (type < 0) {
-                primitives_guarded(g, cr, pr);
-            } else if (type == MGPU_BC_SYMMETRY) {
-#pragma unroll
-                for (int i = 0; i < 4; i++) cr[i] = cl[i];
-#pragma unroll
-                for (int i = 0; i < NPR; i++) pr[i] = pl[i];
-                const float un = pl[0] * n[0] + pl[1] * n[1];
-                pr[0] = pl[0] - 2.0f * un * n[0];
-                pr[1] = pl[1] - 2.0f * un * n[1];
-            } else if (type == MGPU_BC_EXTRAPOLATION) {
-#pragma unroll
-                for (int i = 0; i < 4; i++) cr[i] = cl[i];
-#pragma unroll
-                for (int i = 0; i < NPR; i++) pr[i] = pl[i];
-            } else if (type == MGPU_BC_UPT) {
-                const double* d = bct.bc[bi].data;
-                cr[0] = f(d[0]);
-#pragma unroll
-                for (int i = 0; i < NPR; i++) pr[i] = f(d[i + 1]);
-            } else {  // MGPU_BC_P_OUT
-                const float rho_l = cl[0];
-                const float um = sqrtf(pl[0] * pl[0] + pl[1] * pl[1]);
-                const float sos = sqrtf(gam * pl[2] / rho_l);
-                const float po = (um < sos) ? f(bct.bc[bi].data[0]) : pl[2];
-                const float T = pl[3];
-                const float rho = po / (g.R_f * T);
-                const float e = g.cv_f * T;
-                cr[0] = rho;
-                pr[0] = pl[0];
-                pr[1] = pl[1];
-                pr[2] = po;
-                pr[3] = T;
-                pr[4] = e + po / rho;
-            }
-            riemann<RS>(Ft, n, cl[0], pl, pl[2], gam, pl[4], cr[0], pr, pr[2], gam, pr[4], a.guard != 0);
-        }
+        float Ft[4];
+        flux32_point<RS, NQ>(a, fv, g, bct, fi, q, lr, n, bi, type, ix, Ust, Ft);
 #pragma unroll
         for (int i = 0; i < 4; i++) F[i] = fmaf(a.qw_f[q], Ft[i], F[i]);
     }
     const double area = a.area[fi];
-    double2* Gf = reinterpret_cast<double2*>(Gout + ix.f(fi) * 4);
-    // FP32 -> FP64 exactly on the integer pipe (f64_of), products in FP64
     if (VISC && (type < 0 || type == MGPU_BC_WALL_ADIABATIC)) {
         float Fv[4];
         visc32_face(*va, fi, lr, type == MGPU_BC_WALL_ADIABATIC, n, Fv);
-        Gf[0] = make_double2(area * f64_of(F[0] * 0.5f), area * f64_of(F[1] * 0.5f) - area * f64_of(Fv[1]));
-        Gf[1] = make_double2(area * f64_of(F[2] * 0.5f) - area * f64_of(Fv[2]),
-                             area * f64_of(F[3] * 0.5f) - area * f64_of(Fv[3]));
+        store_G32(Gout + ix.f(fi) * 4, area, F, Fv, 2);
         return;
     }
-    Gf[0] = make_double2(area * f64_of(F[0] * 0.5f), area * f64_of(F[1] * 0.5f));
-    Gf[1] = make_double2(area * f64_of(F[2] * 0.5f), area * f64_of(F[3] * 0.5f));
+    store_G32(Gout + ix.f(fi) * 4, area, F, nullptr, 2);
 }
 
 template <int RS, int NQ, bool VISC>
@@ -702,11 +726,52 @@ __global__ void __launch_bounds__(128) flux32_kernel(const FluxArgs a, const flo
     flux32_face<RS, NQ, VISC>(a, fv, g, bct, fi, Ix1{}, a.U, a.G, &v);
 }
 
+// Two lanes per face (two Gauss points): lane q computes point q's flux, the
+// pair swaps them and both sum in the one-lane kernel's order (point 0
+// first), so G is bit for bit flux32_kernel's; lane 0 stores the first half
+// of the face's G, lane 1 the second.  Half the dependent work per thread,
+// twice the faces in flight.
+template <int RS, bool VISC>
+__global__ void __launch_bounds__(128) flux32_pair_kernel(const FluxArgs a, const float* __restrict__ fv,
+                                                          const GasParams g, const BcTable bct, const Visc32Args v) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int fi = t >> 1, q = t & 1;
+    const unsigned live = __ballot_sync(0xffffffffu, fi < a.n_faces);
+    if (fi >= a.n_faces) return;
+    const int2 lr = a.lr[fi];
+    const double2 nn = a.nrm[fi];
+    const float n[2] = {f(nn.x), f(nn.y)};
+    const int bi = a.bc[fi];
+    const int type = bi < 0 ? -1 : bct.bc[bi].type;
+    float Ft[4], F[4];
+    flux32_point<RS, 2>(a, fv, g, bct, fi, q, lr, n, bi, type, Ix1{}, a.U, Ft);
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const float o = __shfl_xor_sync(live, Ft[i], 1);
+        const float f0 = q == 0 ? Ft[i] : o, f1 = q == 0 ? o : Ft[i];
+        F[i] = fmaf(a.qw_f[1], f1, fmaf(a.qw_f[0], f0, 0.0f));
+    }
+    const double area = a.area[fi];
+    if (VISC && (type < 0 || type == MGPU_BC_WALL_ADIABATIC)) {
+        float Fv[4];
+        visc32_face(v, fi, lr, type == MGPU_BC_WALL_ADIABATIC, n, Fv);
+        store_G32(a.G + (size_t)fi * 4, area, F, Fv, q);
+        return;
+    }
+    store_G32(a.G + (size_t)fi * 4, area, F, nullptr, q);
+}
+
 template <int RS, int NQ>
 cudaError_t flux_go(const FluxArgs& a, const float* fv, const GasParams& g, const BcTable& bct,
                     const Visc32Args* v, cudaStream_t s) {
     const unsigned blocks = (unsigned)((a.n_faces + 127) / 128);
     if (!blocks) return cudaSuccess;
+    if constexpr (NQ == 2) {
+        const unsigned pblocks = (unsigned)((2ll * a.n_faces + 127) / 128);
+        if (v) flux32_pair_kernel<RS, true><<<pblocks, 128, 0, s>>>(a, fv, g, bct, *v);
+        else flux32_pair_kernel<RS, false><<<pblocks, 128, 0, s>>>(a, fv, g, bct, Visc32Args{});
+        return cudaGetLastError();
+    }
     if (v) flux32_kernel<RS, NQ, true><<<blocks, 128, 0, s>>>(a, fv, g, bct, *v);
     else flux32_kernel<RS, NQ, false><<<blocks, 128, 0, s>>>(a, fv, g, bct, Visc32Args{});
     return cudaGetLastError();
