@@ -128,4 +128,7 @@ def main(root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path of the reference checkout> > "
+                 "tests/golden/reference_unit_vectors.json")
+    main(sys.argv[1])
