@@ -413,7 +413,7 @@ def kernel_bytes(kind, precision, learned, cells, faces, solver, stats):
     over the three), plus every face's flux once; cfl: per cell its faces,
     its state row and the radius, per face its cells, normal and 1/distance;
     selector: neighbour ids of all stencils, the state gathered once per
-    cell, predictions, the weight image per 128-cell CTA."""
+    cell, predictions, the weight image once."""
     fp32 = precision == "fp32"
     fw = 4 if fp32 else 8
     if kind == "recon":
@@ -430,30 +430,39 @@ def kernel_bytes(kind, precision, learned, cells, faces, solver, stats):
     if kind == "cfl":
         return cells * (16 + (16 if fp32 else 32 + 48) + 8) + faces * (8 + 16 + 8)
     if kind == "selector" and stats:
-        return stats["stencils_full"] * 19 * 4 + cells * (32 + 4) + (cells + 127) // 128 * 25216
+        return stats["stencils_full"] * 19 * 4 + cells * (32 + 4) + 25216
     return 0
 
 
-def run_until(s, t_end, chunk=50):
-    """Steps s until its simulated time reaches t_end (the last chunk ends
-    there or later); returns (time, steps, wall seconds)."""
+def run_to_time(s, t_end, chunk=50):
+    """Steps s to exactly t_end: CFL steps (in chunks while far from it), and
+    a last step shortened to end on t_end.  Returns (steps, wall seconds,
+    status ok)."""
     t, steps = 0.0, 0
     t0 = time.perf_counter()
-    while t < t_end:
-        k = 1 if t_end - t < 0.02 else chunk
-        t += s.run(CFL, k)
-        steps += k
-        if s.status() != 0:
-            break
-    return t, steps, time.perf_counter() - t0
+    while t < t_end and s.status() == 0:
+        if t_end - t > 0.02:
+            t += s.run(CFL, chunk)
+            steps += chunk
+            continue
+        dt, _ = s.calc_dt(CFL)
+        if t + dt >= t_end:
+            s.take_step(t_end - t)
+            t = t_end
+        else:
+            s.take_step(dt)
+            t += dt
+        steps += 1
+    s.synchronize()
+    return steps, time.perf_counter() - t0, s.status() == 0
 
 
 def run_end_time(args, device, selector):
-    """The four-quadrant problem to t = 0.3 (its end time): the learned form
-    on the headline mesh (finite, steps, wall time), and at --end-time-n the
-    plain FP64 path and the learned form, stepped to the same time with the
-    same number of steps, with the error between them."""
-    import mallard_gb300 as mg  # noqa: F401
+    """The four-quadrant problem to its end time t = 0.3: the learned form on
+    the headline mesh (finite, steps, wall time), and at --end-time-n the
+    plain FP64 path, the FP32 form and the learned form, each stepped at its
+    own CFL time step to exactly t = 0.3, with the FP32 forms' errors against
+    the FP64 state."""
     out = {"t_end": T_END}
     m = case_mesh(args.n)
     U0, W0 = four_quadrant_state(m.cell_coords)
@@ -461,11 +470,11 @@ def run_end_time(args, device, selector):
     s.set_state(U0, W0)
     s.autotune()
     s.set_state(U0, W0)
-    t, steps, wall = run_until(s, T_END)
+    steps, wall, ok = run_to_time(s, T_END)
     U, _ = s.get_state()
     vol = m.cell_volume
-    out[f"{args.n}x{args.n}"] = {"form": "fp32_learned", "t": t, "steps": steps, "wall_s": wall,
-                                 "finite": bool(np.isfinite(U).all()) and s.status() == 0,
+    out[f"{args.n}x{args.n}"] = {"form": "fp32_learned", "steps": steps, "wall_s": wall,
+                                 "finite": bool(np.isfinite(U).all()) and ok,
                                  "density_min": float(U[:, 0].min()), "density_max": float(U[:, 0].max()),
                                  "mass": float(np.sum(vol * U[:, 0]))}
     s.close()
@@ -473,25 +482,19 @@ def run_end_time(args, device, selector):
     if n > 0:
         m = case_mesh(n)
         U0, W0 = four_quadrant_state(m.cell_coords)
-        ref = make_solver(m, args, "fp64", device, selector)
-        ref.set_state(U0, W0)
-        t64, steps64, wall64 = 0.0, 0, time.perf_counter()
-        while t64 < T_END and ref.status() == 0:
-            t64 += ref.run(CFL, 1)
-            steps64 += 1
-        wall64 = time.perf_counter() - wall64
-        Ur, _ = ref.get_state()
-        ref.close()
-        s = make_solver(m, args, "fp32_learned", device, selector)
-        s.set_state(U0, W0)
-        tl = s.run(CFL, steps64)
-        Ul, _ = s.get_state()
-        rec = {"steps": steps64, "t_fp64": t64, "t_learned": tl, "fp64_wall_s": wall64,
-               "finite": bool(np.isfinite(Ul).all() and np.isfinite(Ur).all()) and s.status() == 0,
-               "selector": selector_summary(selector, s.selector_stats(), args.sel_interval)}
-        rec.update(errors_vs(m, Ul, Ur))
-        s.close()
-        out[f"{n}x{n}_learned_vs_fp64"] = rec
+        finals, rec = {}, {}
+        for form in ("fp64", "fp32", "fp32_learned"):
+            s = make_solver(m, args, form, device, selector)
+            s.set_state(U0, W0)
+            steps, wall, ok = run_to_time(s, T_END)
+            finals[form] = s.get_state()[0]
+            rec[form] = {"steps": steps, "wall_s": wall, "finite": bool(np.isfinite(finals[form]).all()) and ok}
+            if form == "fp32_learned":
+                rec[form]["selector"] = selector_summary(selector, s.selector_stats(), args.sel_interval)
+            s.close()
+        for form in ("fp32", "fp32_learned"):
+            rec[form].update(errors_vs(m, finals[form], finals["fp64"]))
+        out[f"{n}x{n}_vs_fp64"] = rec
     return out
 
 
@@ -824,9 +827,8 @@ def run_ours(args):
 
     if rank == 0:
         cfg = workload_config(args, args.n)
-        cfg["form"] = head
-        cfg["precision"] = prec + (" + learned stencil selector" if learned else "")
-        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        line = {"form": head, "precision": prec + (" + learned stencil selector" if learned else ""),
+                "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32 (reconstruction, flux) + f64 (state, accumulation)" if prec == "fp32" else "f64",

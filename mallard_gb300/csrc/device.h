@@ -65,10 +65,8 @@ struct TenoArgs {
     double oi2[KR_MAX * KR_MAX];  // same, upper triangle with doubled off-diagonals (fast form)
     float oi2f[KR_MAX * KR_MAX];  // oi2 in FP32 (FP32-bulk form)
     unsigned* err;                // status word: bit 2 when a bounded wait ran out (staged FP32 form)
-    // robust TENO variant: per cell 1 if it has a boundary face; gamma - 1
+    // robust TENO variant: per cell 1 if it has a boundary face
     const uint8_t* bcell;         // null unless the variant is MGPU_TENO_ROBUST
-    double gm1;
-    float gm1f;
 };
 
 struct FluxArgs {

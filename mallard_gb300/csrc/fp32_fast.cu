@@ -114,9 +114,8 @@ __device__ __forceinline__ void robust_cell32(const TenoArgs& a, bool boundary, 
             const float m0 = __shfl_sync(live, out[fl][q], 1, 4);
             const float m1 = __shfl_sync(live, out[fl][q], 2, 4);
             const float E = __shfl_sync(live, out[fl][q], 3, 4);
-            const float ir = 1.0f / rho;
-            const float ke = 0.5f * (m0 * m0 + m1 * m1) * ir;
-            if (!(rho > 0.0f) || !(a.gm1f * (E - ke) > 0.0f)) bad = true;
+            const float m2 = fmaf(m0, m0, m1 * m1);
+            if (!(rho > 0.0f && 2.0f * rho * E > m2)) bad = true;
         }
     if (bad)
 #pragma unroll

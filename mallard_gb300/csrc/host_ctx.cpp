@@ -494,8 +494,6 @@ void mgpu_ctx::build() {
             bcell.upload(h_bc);
             teno.bcell = bcell.p;
         }
-        teno.gm1 = cfg.gamma - 1.0;
-        teno.gm1f = (float)(cfg.gamma - 1.0);
         teno.nb = nb.p;
         teno.ar = ar.p;
         teno.P = P.p;

@@ -30,7 +30,8 @@ namespace {
 // every face point; otherwise each variable's deviations from the average
 // are scaled by one factor into the central stencil's range [dlo, dhi]
 // (around the average), and a cell with a face state that is then not
-// admissible takes its average at every face point.  live: the warp's lanes
+// admissible (density positive and 2 rho E > |rho u|^2) takes its average
+// at every face point.  live: the warp's lanes
 // whose cells exist; the four lanes of a cell exchange their variables.
 template <int NF, int NQ>
 __device__ __forceinline__ void robust_cell(const TenoArgs& a, int cell, unsigned live, double uc, double dlo,
@@ -61,13 +62,9 @@ __device__ __forceinline__ void robust_cell(const TenoArgs& a, int cell, unsigne
             const double m0 = __shfl_sync(live, out[fl][q], 1, 4);
             const double m1 = __shfl_sync(live, out[fl][q], 2, 4);
             const double E = __shfl_sync(live, out[fl][q], 3, 4);
-            if (!(rho > 0.0)) {
-                bad = true;
-            } else {
-                const double u0 = m0 / rho, u1 = m1 / rho;
-                const double e = E / rho - 0.5 * (u0 * u0 + u1 * u1);
-                if (!(a.gm1 * rho * e > 0.0)) bad = true;
-            }
+            // density positive and 2 rho E > |rho u|^2 (pressure positive), no division
+            const double m2 = m0 * m0 + m1 * m1;
+            if (!(rho > 0.0 && 2.0 * rho * E > m2)) bad = true;
         }
     if (bad)
 #pragma unroll

@@ -1066,8 +1066,17 @@ bool admissible(const Gas& g, const double* W);
 //     d_p = w_p - u are scaled by one theta = min over the points of
 //     dhi / d_p (d_p > dhi) or dlo / d_p (d_p < dlo), where [dlo, dhi] is
 //     the range of the central stencil's averages minus u;
-//  3. if a face state is then not admissible (density and pressure
-//     positive), the cell takes its average at every face point.
+//  3. if a face state is then not admissible (density positive and
+//     2 rho E > |rho u|^2, i.e. pressure positive), the cell takes its
+//     average at every face point.
+// Admissible face state for the robust variant's fallback: density
+// positive and 2 rho E > |rho u|^2, which for rho > 0 is pressure positive
+// (gamma > 1), without divisions.
+inline bool robust_admissible(const double* W) {
+    const double m2 = W[1] * W[1] + W[2] * W[2];
+    return W[0] > 0.0 && 2.0 * W[0] * W[3] > m2;
+}
+
 void robust_cell(Case& cs, uint32_t c, const double* U, double* face, const double* dlo, const double* dhi) {
     const OMesh& m = *cs.mesh;
     const int nq = cs.nq;
@@ -1100,7 +1109,7 @@ void robust_cell(Case& cs, uint32_t c, const double* U, double* face, const doub
         }
         for (int fl = 0; fl < nf && !first_order; fl++)
             for (int q = 0; q < nq; q++)
-                if (!admissible(cs.gas, at(fl, q))) {
+                if (!robust_admissible(at(fl, q))) {
                     first_order = true;
                     break;
                 }
