@@ -865,18 +865,49 @@ __global__ void __launch_bounds__(BS, MINB) teno32_batch_kernel(const BatchLaunc
     }
 }
 
-// Batched face flux: thread (case, flux face).
-template <int RS, int NQ>
-__global__ void __launch_bounds__(128) flux32_batch_kernel(const BatchLaunch b, const GasParams g, const BcTable bct,
-                                                           const double* __restrict__ U) {
-    const long long total = b.face0[b.n_groups];
-    for (long long gt = (long long)blockIdx.x * 128 + threadIdx.x; gt < total; gt += (long long)gridDim.x * 128) {
-        const int gi = batch_group(b.face0, b.n_groups, gt);
-        const unsigned t = (unsigned)(gt - b.face0[gi]);
-        const unsigned tc = t >> 3, C = b.C[gi], cs = tc % C;
-        const int fi = (int)(tc / C) * 8 + (int)(t & 7);
-        if (fi >= b.n_faces[gi] || b.flags[b.case0[gi] + cs] != 0u) continue;
-        flux32_face<RS, NQ, false>(b.flux[gi], b.fv, g, bct, fi, IxB{b.ubase[gi], b.fbase[gi], C, cs}, U, b.G);
+// Batched face flux, two lanes per (case, face) item (flux32_pair_kernel's
+// scheme): the grid-stride loop runs whole warps, so every lane of a warp
+// takes part in the pair exchange of each pass.
+template <int RS>
+__global__ void __launch_bounds__(128) flux32_pair_batch_kernel(const BatchLaunch b, const GasParams g,
+                                                               const BcTable bct, const double* __restrict__ U) {
+    const long long total = 2 * b.face0[b.n_groups];
+    const int lane = threadIdx.x & 31;
+    for (long long base = (long long)blockIdx.x * 128 + (threadIdx.x & ~31); base < total;
+         base += (long long)gridDim.x * 128) {
+        const long long gt = base + lane;
+        bool on = gt < total;
+        int gi = 0, fi = 0;
+        unsigned C = 1, cs = 0;
+        if (on) {
+            const long long item = gt >> 1;
+            gi = batch_group(b.face0, b.n_groups, item);
+            const unsigned t = (unsigned)(item - b.face0[gi]);
+            const unsigned tc = t >> 3;
+            C = b.C[gi];
+            cs = tc % C;
+            fi = (int)(tc / C) * 8 + (int)(t & 7);
+            on = fi < b.n_faces[gi] && b.flags[b.case0[gi] + cs] == 0u;
+        }
+        const unsigned live = __ballot_sync(0xffffffffu, on);
+        if (!on) continue;
+        const int q = (int)(gt & 1);
+        const FluxArgs& a = b.flux[gi];
+        const IxB ix{b.ubase[gi], b.fbase[gi], C, cs};
+        const int2 lr = a.lr[fi];
+        const double2 nn = a.nrm[fi];
+        const float n[2] = {f(nn.x), f(nn.y)};
+        const int bi = a.bc[fi];
+        const int type = bi < 0 ? -1 : bct.bc[bi].type;
+        float Ft[4], F[4];
+        flux32_point<RS, 2>(a, b.fv, g, bct, fi, q, lr, n, bi, type, ix, U, Ft);
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const float o = __shfl_xor_sync(live, Ft[i], 1);
+            const float f0 = q == 0 ? Ft[i] : o, f1 = q == 0 ? o : Ft[i];
+            F[i] = fmaf(a.qw_f[1], f1, fmaf(a.qw_f[0], f0, 0.0f));
+        }
+        store_G32(b.G + ix.f(fi) * 4, a.area[fi], F, nullptr, q);
     }
 }
 
@@ -1065,15 +1096,15 @@ cudaError_t launch_teno_batch(const BatchLaunch& b, const float* U, int shape, i
 cudaError_t launch_flux_batch(const BatchLaunch& b, const GasParams& g, const BcTable& bct, int rsolver, int nq,
                               const double* U, cudaStream_t s) {
     if (nq != 2) return cudaErrorInvalidValue;
-    const long long blocks = (b.face0[b.n_groups] + 127) / 128;
+    const long long blocks = (2 * b.face0[b.n_groups] + 127) / 128;
     if (blocks == 0) return cudaSuccess;
     switch (rsolver) {
         case MGPU_RIEMANN_RUSANOV:
-            flux32_batch_kernel<MGPU_RIEMANN_RUSANOV, 2><<<(unsigned)blocks, 128, 0, s>>>(b, g, bct, U);
+            flux32_pair_batch_kernel<MGPU_RIEMANN_RUSANOV><<<(unsigned)blocks, 128, 0, s>>>(b, g, bct, U);
             break;
-        case MGPU_RIEMANN_HLL: flux32_batch_kernel<MGPU_RIEMANN_HLL, 2><<<(unsigned)blocks, 128, 0, s>>>(b, g, bct, U); break;
+        case MGPU_RIEMANN_HLL: flux32_pair_batch_kernel<MGPU_RIEMANN_HLL><<<(unsigned)blocks, 128, 0, s>>>(b, g, bct, U); break;
         case MGPU_RIEMANN_HLLC:
-            flux32_batch_kernel<MGPU_RIEMANN_HLLC, 2><<<(unsigned)blocks, 128, 0, s>>>(b, g, bct, U);
+            flux32_pair_batch_kernel<MGPU_RIEMANN_HLLC><<<(unsigned)blocks, 128, 0, s>>>(b, g, bct, U);
             break;
         default: return cudaErrorInvalidValue;
     }
