@@ -112,10 +112,12 @@ def test_fast_forms_to_the_end_time(precision):
     assert l1 <= 1e-3, l1
 
 
-def test_learned_form_four_quadrant():
+@pytest.mark.parametrize("interval", [2, 4])
+def test_learned_form_four_quadrant(interval):
     """FP32 + the shipped selector with the robust variant on the
-    four-quadrant problem at 128 x 128 for 300 steps: density L1 against the
-    plain FP64 run within the spec bar."""
+    four-quadrant problem at 128 x 128 for 300 steps, predicting every 2nd
+    or 4th step: density L1 against the plain FP64 run within the
+    spec bar."""
     from mallard_gb300.selector import Selector, default_weights_path
     path = default_weights_path()
     if not path.exists():
@@ -130,7 +132,7 @@ def test_learned_form_four_quadrant():
     with Selector() as sel:
         sel.load(path)
         f32, _ = make_pair(m, variant="robust", precision="fp32")
-        f32.attach_selector(sel, threshold=0.98, interval=2)
+        f32.attach_selector(sel, threshold=0.98, interval=interval)
         f32.set_state(U, W)
         f32.run(0.5, 300)
         Ug, _ = f32.get_state()
@@ -139,7 +141,8 @@ def test_learned_form_four_quadrant():
         f32.close()
     l1 = _l1(m, Ug, Ur)
     frac = st["stencils_evaluated"] / st["stencils_full"]
-    print(f"robust learned form, four-quadrant 128^2, 300 steps: L1 {l1:.2e}, stencils {frac:.3f}")
+    print(f"robust learned form, four-quadrant 128^2, 300 steps, interval {interval}: L1 {l1:.2e}, "
+          f"stencils {frac:.3f}")
     assert st["error"] == 0 and np.isfinite(l1) and l1 <= 1e-3
     assert frac < 0.8
 
