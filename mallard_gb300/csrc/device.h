@@ -31,6 +31,7 @@ struct GasParams {
     double gamma, R, cv, p_min, p_max;
     double icv;  // 1 / cv (fast forms)
     float gamma_f, R_f, cv_f, p_min_f, p_max_f;  // the same rounded to FP32 on the host (FP32 form)
+    float icv_f, gm1_f;                          // 1 / cv and gamma - 1, rounded once (FP32 form)
 };
 
 struct BcEntry {

@@ -479,13 +479,21 @@ __global__ void __launch_bounds__(WARPS * 32, MINB) teno32_staged_kernel(const T
     }
 }
 
-// Primitive recovery of a face state: FP32, or FP64 when the internal energy
-// is a small remainder of the total (near vacuum pressure).
+// Primitive recovery of a face state in FP32 with one correctly rounded
+// reciprocal of the density (instead of five divisions), or in FP64 when
+// the internal energy is a small remainder of the total (near vacuum
+// pressure).
 __device__ __forceinline__ void primitives_guarded(const GasParams& g, const float* U, float* W) {
-    primitives(g, U, W);
-    const float rho = U[0];
-    const float E = U[3] / rho;
-    const float e = W[3] * g.cv_f;
+    const float rho = U[0], ir = __frcp_rn(rho);
+    const float u0 = U[1] * ir, u1 = U[2] * ir;
+    const float E = U[3] * ir;
+    const float e = E - 0.5f * (u0 * u0 + u1 * u1);
+    const float p = fmaxf(g.p_min_f, fminf(g.p_max_f, g.gm1_f * rho * e));
+    W[0] = u0;
+    W[1] = u1;
+    W[2] = p;
+    W[3] = e * g.icv_f;
+    W[4] = e + p * ir;
     if (!(e > 1.0e-3f * E)) {
         const double Ud[4] = {U[0], U[1], U[2], U[3]};
         double Wd[5];
@@ -602,6 +610,13 @@ __device__ __forceinline__ void visc32_face(const Visc32Args& a, int fi, int2 lr
 }
 
 // Flux of one face (local index fi) into G; VISC: minus the viscous flux.
+// Positivity test of the face-state fallback in FP32 without divisions:
+// density positive and 2 rho E > |rho u|^2 (pressure positive).
+__device__ __forceinline__ bool admissible32(const float* W) {
+    const float m2 = fmaf(W[1], W[1], W[2] * W[2]);
+    return W[0] > 0.0f && 2.0f * W[0] * W[3] > m2;
+}
+
 // One quadrature point q of face fi: its flux Ft before the weight (the
 // face states, the positivity fallback to the cell averages, the boundary
 // condition's right state, the Riemann flux).
@@ -620,10 +635,10 @@ __device__ __forceinline__ void flux32_point(const FluxArgs& a, const float* __r
         const float4 x = fq[1];
         cr[0] = x.x; cr[1] = x.y; cr[2] = x.z; cr[3] = x.w;
     }
-    if (!admissible(g, cl))
+    if (!admissible32(cl))
 #pragma unroll
         for (int i = 0; i < 4; i++) cl[i] = f(Ust[ix.u(lr.x) * NC + i]);
-    if (type < 0 && !admissible(g, cr))
+    if (type < 0 && !admissible32(cr))
 #pragma unroll
         for (int i = 0; i < 4; i++) cr[i] = f(Ust[ix.u(lr.y) * NC + i]);
     primitives_guarded(g, cl, pl);

@@ -740,6 +740,8 @@ int mgpu_create(const mgpu_mesh* mesh, const mgpu_config* cfg, mgpu_ctx** out) {
         ctx->gas.gamma_f = (float)ctx->gas.gamma;
         ctx->gas.R_f = (float)ctx->gas.R;
         ctx->gas.cv_f = (float)ctx->gas.cv;
+        ctx->gas.icv_f = (float)(1.0 / ctx->gas.cv);
+        ctx->gas.gm1_f = (float)(ctx->gas.gamma - 1.0);
         ctx->gas.p_min_f = (float)ctx->gas.p_min;
         ctx->gas.p_max_f = (float)ctx->gas.p_max;
         ck(cudaSetDevice(cfg->device), "cudaSetDevice");
