@@ -115,7 +115,7 @@ def parse():
                     help="steps per selector prediction in the learned form (1 = every step; 2 keeps stale "
                          "predictions inside the neighbour check's one-cell margin at CFL <= 0.5)")
     ap.add_argument("--shape", type=int, default=-1,
-                    help="fix the FP32 reconstruction's launch shape (0-6) instead of autotuning it")
+                    help="fix the FP32 reconstruction's launch shape (0-7) instead of autotuning it")
     ap.add_argument("--cpu-sample-n", type=int, default=CPU_SAMPLE_N)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -360,7 +360,8 @@ def autotune(s, args, U0, W0):
     s.set_state(U0, W0)
     return {"chosen_shape": shape, "ms_per_shape": [round(x, 4) for x in tms],
             "shapes": "0: 128 thr/<=128 regs, 1: 128/<=80, 2: 128/<=64, 3: 256/<=64, "
-                      "4-6: staged (bulk copies to shared memory) 1 slot x 4 warps/<=80, 2 x 2/<=128, 1 x 4/<=128"}
+                      "4-7: staged (bulk copies to shared memory) 1 slot x 4 warps/<=80, 2 x 2/<=128, 1 x 4/<=128, "
+                      "1 x 4/<=72"}
 
 
 def time_form(m, args, form, U0, W0, device, selector, barrier=None, clocks=None):
@@ -460,9 +461,9 @@ def run_to_time(s, t_end, chunk=50):
 def run_end_time(args, device, selector):
     """The four-quadrant problem to its end time t = 0.3: the learned form on
     the headline mesh (finite, steps, wall time), and at --end-time-n the
-    plain FP64 path, the FP32 form and the learned form, each stepped at its
-    own CFL time step to exactly t = 0.3, with the FP32 forms' errors against
-    the FP64 state."""
+    plain FP64 path, the FP64-fast form, the FP32 form and the learned form,
+    each stepped at its own CFL time step to exactly t = 0.3, with the
+    others' errors against the FP64 state."""
     out = {"t_end": T_END}
     m = case_mesh(args.n)
     U0, W0 = four_quadrant_state(m.cell_coords)
@@ -483,7 +484,7 @@ def run_end_time(args, device, selector):
         m = case_mesh(n)
         U0, W0 = four_quadrant_state(m.cell_coords)
         finals, rec = {}, {}
-        for form in ("fp64", "fp32", "fp32_learned"):
+        for form in ("fp64", "fp64_fast", "fp32", "fp32_learned"):
             s = make_solver(m, args, form, device, selector)
             s.set_state(U0, W0)
             steps, wall, ok = run_to_time(s, T_END)
@@ -492,7 +493,9 @@ def run_end_time(args, device, selector):
             if form == "fp32_learned":
                 rec[form]["selector"] = selector_summary(selector, s.selector_stats(), args.sel_interval)
             s.close()
-        for form in ("fp32", "fp32_learned"):
+        # fp64_fast (the same scheme with FMA contraction, ~1e-16 per operation)
+        # is the control: how far a perturbation at round-off grows by t_end
+        for form in ("fp64_fast", "fp32", "fp32_learned"):
             rec[form].update(errors_vs(m, finals[form], finals["fp64"]))
         out[f"{n}x{n}_vs_fp64"] = rec
     return out

@@ -417,14 +417,16 @@ int mgpu_enable_kernel_timing(mgpu_ctx* ctx, int enable);
 int mgpu_kernel_times(mgpu_ctx* ctx, double* ms, uint32_t* launches);
 /* Autotuner: times each launch shape of the reconstruction kernel (FP32
  * form at p = 3: 0-2 128-thread blocks with at most 128, 80 or 64 registers
- * per thread, 3 256-thread blocks with 64, 4-6 the staged kernel, whose
+ * per thread, 3 256-thread blocks with 64, 4-7 the staged kernel, whose
  * warps copy their tile's table blocks into shared memory with bulk async
  * copies: one stencil slot per warp and 4 warps per block with at most 80
- * registers, two slots and 2 warps, one slot and 4 warps with 128) on the
- * current state, three launches each after a warm-up, and keeps the fastest
- * for later launches.  ms[7]
- * receives the average time per shape (0 where not applicable), best the
- * chosen shape.  Both may be NULL.  Other forms have a single shape. */
+ * registers, two slots and 2 warps, one slot and 4 warps with 128, one slot
+ * and 4 warps with 72) on the current state, three launches each after a
+ * warm-up, and keeps the fastest for later launches.
+ * ms[MGPU_AUTOTUNE_SHAPES] receives the average time per shape (0 where not
+ * applicable), best the chosen shape.  Both may be NULL.  Other forms have
+ * a single shape. */
+#define MGPU_AUTOTUNE_SHAPES 8
 int mgpu_autotune(mgpu_ctx* ctx, double* ms, int* best);
 /* Fix the reconstruction's launch shape (as mgpu_autotune numbers them);
  * every shape gives the same results. */

@@ -24,6 +24,7 @@ INTEGRATORS = {"SSPRK3": 0, "FE": 1, "RK4": 2}
 BC_TYPES = {"symmetry": 0, "extrapolation": 1, "wall_adiabatic": 2, "upt": 3, "p_out": 4}
 TENO_VARIANTS = {"reference": 0, "corrected": 1, "robust": 2}
 PRECISIONS = {"fp64": 0, "fp64_fast": 1, "fp32": 2}
+AUTOTUNE_SHAPES = 8  # MGPU_AUTOTUNE_SHAPES
 
 TENO_FIELDS = {
     "offsets_stencil_groups": (0, "uint32"),

@@ -197,7 +197,7 @@ namespace f32 {
 // registers, or 256-thread blocks with 64; p = 3 only, other orders use
 // shape 0) or 4..6, the staged form that copies each tile's table blocks
 // into shared memory with cp.async.bulk; chosen by the autotuner
-constexpr int TENO32_SHAPES = 7;
+constexpr int TENO32_SHAPES = MGPU_AUTOTUNE_SHAPES;
 // the batched reconstruction also has shapes 7 and 8: one CTA of 4 or 8
 // warps per mesh tile, its tables resident in shared memory for all cases
 constexpr int TENO32_BATCH_SHAPES = 9;

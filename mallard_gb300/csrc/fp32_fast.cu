@@ -832,8 +832,9 @@ cudaError_t teno_staged1(const TenoArgs& a, const float* U, float* fv, uint8_t* 
 
 // Launch shapes the autotuner chooses from: (block size, minimum resident
 // blocks per SM), i.e. register caps of 128, 80 and 64 per thread; shapes
-// 4-6 are the staged form (p = 3): one stencil slot per warp, 4 warps per
-// block, at most 80 registers; two slots, 2 warps, 128; one slot, 4 warps, 128.
+// 4-7 are the staged form (p = 3): one stencil slot per warp, 4 warps per
+// block, at most 80 registers; two slots, 2 warps, 128; one slot, 4 warps,
+// 128; one slot, 4 warps, at most 72 registers (7 blocks per SM).
 template <int K, int M, int NQ, bool SEL>
 cudaError_t teno_go(const TenoArgs& a, const float* U, float* fv, uint8_t* masks, const uint8_t* pred, int shape,
                     cudaStream_t s) {
@@ -847,6 +848,7 @@ cudaError_t teno_go(const TenoArgs& a, const float* U, float* fv, uint8_t* masks
         if (shape == 4) return teno_staged1<K, M, NQ, SEL, 1, 4, 6>(a, U, fv, masks, pred, s);
         if (shape == 5) return teno_staged1<K, M, NQ, SEL, 2, 2, 7>(a, U, fv, masks, pred, s);
         if (shape == 6) return teno_staged1<K, M, NQ, SEL, 1, 4, 4>(a, U, fv, masks, pred, s);
+        if (shape == 7) return teno_staged1<K, M, NQ, SEL, 1, 4, 7>(a, U, fv, masks, pred, s);
     }
     return cudaErrorInvalidValue;
 }

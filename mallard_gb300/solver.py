@@ -292,7 +292,7 @@ class Solver:
     def autotune(self):
         """Pick the fastest launch shape of the reconstruction kernel on the
         current state; returns (chosen shape, ms per shape)."""
-        ms = np.zeros(7)
+        ms = np.zeros(N.AUTOTUNE_SHAPES)
         best = C.c_int()
         N.check(self._lib.mgpu_autotune(self._h, N.ptr(ms), C.byref(best)))
         return best.value, ms

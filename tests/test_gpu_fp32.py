@@ -108,7 +108,7 @@ def test_launch_shapes_agree(learned):
     sel = Selector()
     sel.load(default_weights_path())
     out = []
-    for shape in range(7):
+    for shape in range(8):
         s, _ = make_pair(m, variant="corrected", precision="fp32")
         if learned:
             s.attach_selector(sel)
