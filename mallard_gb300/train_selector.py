@@ -15,7 +15,10 @@ four problem families:
     angle and Mach number, Rusanov flux), harvested every 100 steps.
 Each harvest keeps every cell where some variable leaves the central
 stencil and a fraction of the all-central cells.  The network is then
-trained with minibatch Adam by the library's own kernels.
+trained with minibatch Adam by the library's own kernels.  --big runs the
+large harvest (about 50M rows): the robust TENO variant, 512 x 512
+four-quadrant and explosion runs of 600 steps, longer shock tubes, more
+ramp channels.
 """
 
 import argparse
@@ -30,15 +33,15 @@ from .selector import Selector, default_weights_path
 GAS = dict(gamma=1.4, p_ref=101325.0, T_ref=298.15, rho_ref=1.225)
 
 
-def _solver(mesh, bc):
+def _solver(mesh, bc, variant="corrected"):
     blist = [{"name": z, "type": bc} for z in mesh.zone_names[1:]]
     return Solver(mesh, face_reconstruction="TENO", basis_type="legendre", basis_order=3, riemann_solver="HLLC",
-                  boundaries=blist, teno_variant="corrected", precision="fp64_fast", **GAS)
+                  boundaries=blist, teno_variant=variant, precision="fp64_fast", **GAS)
 
 
-def _run_and_harvest(sel, mesh, bc, U, W, steps, every, keep, seed):
+def _run_and_harvest(sel, mesh, bc, U, W, steps, every, keep, seed, variant="corrected"):
     rows = 0
-    with _solver(mesh, bc) as s:
+    with _solver(mesh, bc, variant) as s:
         s.set_state(U, W)
         for k in range(steps // every):
             s.run(0.5, every)
@@ -148,10 +151,62 @@ def _run_wedge(sel, r, quick, seed):
     return rows
 
 
-def train(out=None, seed=0, quick=False, epochs=None, log=print):
+def harvest_big(sel, seed=0, log=print):
+    """The large harvest (about 50M rows): the same four families with the
+    robust TENO variant, which keeps the four-quadrant problems finite to
+    their later, more varied states, on larger meshes and longer runs."""
+    r = np.random.default_rng(seed)
+    rows = 0
+    strip = Mesh.generate("cartesian_tri", 1000, 8, 1.0, 0.008)
+    x = strip.cell_coords[:, 0]
+    for i in range(48):
+        left = (r.uniform(0.5, 2.0), r.uniform(-0.5, 0.5), r.uniform(0.5, 2.0))
+        right = (r.uniform(0.05, 0.5), r.uniform(-0.5, 0.5), r.uniform(0.05, 0.5))
+        if r.random() < 0.5:
+            left, right = right, left
+        sel_l = x < r.uniform(0.3, 0.7)
+        rho = np.where(sel_l, left[0], right[0])
+        u = np.where(sel_l, left[1], right[1])
+        p = np.where(sel_l, left[2], right[2])
+        U, W = state_from_primitives(rho, u, 0 * u, p, **GAS)
+        rows += _run_and_harvest(sel, strip, "symmetry", U, W, 800, 40, 0.05, 10 + i, "robust")
+    log(f"  shock tubes: {rows} rows")
+    sq = Mesh.generate("cartesian_tri", 512, 512, 1.0, 1.0)
+    sq.permute_cells(seed + 1)
+    cx, cy = sq.cell_coords[:, 0], sq.cell_coords[:, 1]
+    for i in range(24):
+        sx, sy = r.uniform(0.3, 0.8, 2)
+        q = [(r.uniform(0.1, 2.0), r.uniform(-1.5, 1.5), r.uniform(-1.5, 1.5), r.uniform(0.03, 2.0)) for _ in range(4)]
+        prim = np.zeros((sq.n_cells, 4))
+        for k, m in enumerate(((cx >= sx) & (cy >= sy), (cx < sx) & (cy >= sy), (cx < sx) & (cy < sy),
+                               (cx >= sx) & (cy < sy))):
+            prim[m] = q[k]
+        U, W = state_from_primitives(prim[:, 0], prim[:, 1], prim[:, 2], prim[:, 3], **GAS)
+        rows += _run_and_harvest(sel, sq, "extrapolation", U, W, 600, 20, 0.05, 100 + i, "robust")
+        log(f"  four-quadrant {i + 1}/24: {rows} rows")
+    for i in range(8):
+        c = r.uniform(0.3, 0.7, 2)
+        rad = r.uniform(0.1, 0.3)
+        inn = (cx - c[0]) ** 2 + (cy - c[1]) ** 2 < rad * rad
+        a = (r.uniform(0.5, 2.0), r.uniform(0.5, 2.0))
+        b = (r.uniform(0.1, 0.5), r.uniform(0.05, 0.4))
+        if r.random() < 0.3:
+            a, b = b, a
+        rho = np.where(inn, a[0], b[0])
+        p = np.where(inn, a[1], b[1])
+        U, W = state_from_primitives(rho, 0 * rho, 0 * rho, p, **GAS)
+        rows += _run_and_harvest(sel, sq, "extrapolation", U, W, 600, 30, 0.05, 200 + i, "robust")
+    log(f"  + explosions: {rows} rows")
+    for i in range(8):
+        rows += _run_wedge(sel, r, False, 300 + i)
+    log(f"  + wedges: {rows} rows")
+    return rows
+
+
+def train(out=None, seed=0, quick=False, epochs=None, log=print, big=False):
     t0 = time.time()
     sel = Selector(seed=seed + 1)
-    rows = harvest_all(sel, seed=seed, quick=quick, log=log)
+    rows = harvest_big(sel, seed=seed, log=log) if big else harvest_all(sel, seed=seed, quick=quick, log=log)
     t1 = time.time()
     epochs = epochs or (6 if quick else 12)
     losses = sel.train(epochs=epochs, batch=4096, lr=2e-3, seed=seed + 2)
@@ -170,8 +225,9 @@ def main():
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--quick", action="store_true")
     ap.add_argument("--epochs", type=int, default=None)
+    ap.add_argument("--big", action="store_true", help="the large harvest (about 50M rows, robust TENO runs)")
     a = ap.parse_args()
-    train(a.out, seed=a.seed, quick=a.quick, epochs=a.epochs)
+    train(a.out, seed=a.seed, quick=a.quick, epochs=a.epochs, big=a.big)
 
 
 if __name__ == "__main__":
