@@ -104,6 +104,9 @@ def parse():
                     help="rows of the ramp-channel lattice (3n+1 columns; 816 -> 4.0M triangles); 0 skips it")
     ap.add_argument("--wedge-develop", type=int, default=300,
                     help="untimed steps of the wedge from its uniform start before the timed ones")
+    ap.add_argument("--wedge-total", type=int, default=0,
+                    help="total steps of the wedge (the configuration's 2000); the development steps become "
+                         "total - warmup - steps (0: --wedge-develop)")
     ap.add_argument("--wedge-re", type=float, default=1e5,
                     help="Reynolds number of the wedge on the ramp length (viscous flux, no-slip walls); 0 = inviscid")
     ap.add_argument("--wedge-variant", default="corrected", choices=["corrected", "robust"],
@@ -553,6 +556,7 @@ def run_wedge(args, device, selector):
 
     import mallard_gb300 as mg
     from mallard_gb300.train_selector import wedge_setup
+    develop = max(0, args.wedge_total - args.warmup - args.steps) if args.wedge_total > 0 else args.wedge_develop
     ny = args.wedge_n
     nx = 3 * ny + 1
     t0 = time.perf_counter()
@@ -562,8 +566,9 @@ def run_wedge(args, device, selector):
             else "inviscid (slip walls)")
     out = {"workload": f"ramp channel {nx}x{ny} lattice -> {mesh.n_cells} Delaunay triangles, 15 deg ramp, "
                        f"Mach 2.5, TENO p3 ({args.wedge_variant}) + Rusanov, SSPRK3 CFL {WEDGE_CFL}, {flow}; timed "
-                       f"after {args.wedge_develop} development steps",
-           "cells": mesh.n_cells, "mesh_s": time.perf_counter() - t0, "develop_steps": args.wedge_develop}
+                       f"after {develop} development steps",
+           "cells": mesh.n_cells, "mesh_s": time.perf_counter() - t0, "develop_steps": develop,
+           "total_steps": develop + args.warmup + args.steps}
     finals = {}
     for form, prec in (("fp64", "fp64"), ("fp32_learned", "fp32")):
         t1 = time.perf_counter()
@@ -574,8 +579,8 @@ def run_wedge(args, device, selector):
         stream = torch.cuda.Stream()
         s.set_stream(stream.cuda_stream)
         s.set_state(U0, W0)
-        if args.wedge_develop > 0:
-            s.launch(WEDGE_CFL, args.wedge_develop)
+        if develop > 0:
+            s.launch(WEDGE_CFL, develop)
             s.synchronize()
         if prec == "fp32":
             Ud, Wd = s.get_state()
