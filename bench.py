@@ -27,7 +27,7 @@ timed state that is not finite, or a non-zero status word, prints a
 "status" line without a value and exits 1.
 
 One step = spectral radius + dt + three stages of (reconstruction, face flux,
-residual gather + update), plus one selector inference every second step in
+residual gather + update), plus one selector inference every fourth step in
 the learned form (--sel-interval), all on the GPU, replayed as CUDA graphs.
 Inputs (tables 3.4-7 KB per cell, 7-15 GB) are far larger than L2, so no
 explicit flush is done.
@@ -114,9 +114,10 @@ def parse():
     ap.add_argument("--batch-cases", type=int, default=256,
                     help="cases of the batched section (the four-quadrant ensemble); 0 skips it")
     ap.add_argument("--batch-steps", type=int, default=500, help="total steps of the batched section")
-    ap.add_argument("--sel-interval", type=int, default=2,
-                    help="steps per selector prediction in the learned form (1 = every step; 2 keeps stale "
-                         "predictions inside the neighbour check's one-cell margin at CFL <= 0.5)")
+    ap.add_argument("--sel-interval", type=int, default=4,
+                    help="steps per selector prediction in the learned form (1 = every step; at CFL 0.5 a wave "
+                         "crosses about 0.12 of a cell per step, so 4 steps stay inside the neighbour check's "
+                         "one-cell margin)")
     ap.add_argument("--shape", type=int, default=-1,
                     help="fix the FP32 reconstruction's launch shape (0-7) instead of autotuning it")
     ap.add_argument("--cpu-sample-n", type=int, default=CPU_SAMPLE_N)

@@ -161,7 +161,7 @@ def test_learned_form_error_and_gain():
     assert frac_t < 0.6 and frac_t < frac_u
 
 
-@pytest.mark.parametrize("interval", [1, 2])
+@pytest.mark.parametrize("interval", [1, 2, 4])
 @pytest.mark.parametrize("problem", ["explosion", "four_quadrant"])
 def test_shipped_selector_error_and_work(problem, interval):
     """The trained weights shipped with the package, on problems they were not
