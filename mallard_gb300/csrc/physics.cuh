@@ -165,7 +165,19 @@ __device__ __forceinline__ void riemann(T* F, const T* n, T rl, const T* ul, T p
     } else {
         const T D[4] = {T(0.0), n[0], n[1], Ss};
         const T Plr = T(0.5) * (pl + pr + rl * (Sl - unl) * (Ss - unl) + rr * (Sr - unr) * (Ss - unr));
-        if (Ss >= T(0.0)) {
+        if constexpr (sizeof(T) == 4) {
+            // FP32 form: one correctly rounded reciprocal of the shared
+            // denominator instead of four divisions
+            if (Ss >= T(0.0)) {
+                const T r = __frcp_rn(Sl - Ss);
+#pragma unroll
+                for (int i = 0; i < 4; i++) F[i] = (Ss * (Sl * Ul[i] - Fl[i]) + Sl * Plr * D[i]) * r;
+            } else {
+                const T r = __frcp_rn(Sr - Ss);
+#pragma unroll
+                for (int i = 0; i < 4; i++) F[i] = (Ss * (Sr * Ur[i] - Fr[i]) + Sr * Plr * D[i]) * r;
+            }
+        } else if (Ss >= T(0.0)) {
 #pragma unroll
             for (int i = 0; i < 4; i++) F[i] = (Ss * (Sl * Ul[i] - Fl[i]) + Sl * Plr * D[i]) / (Sl - Ss);
         } else {
