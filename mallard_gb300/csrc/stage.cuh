@@ -184,6 +184,25 @@ __device__ __forceinline__ void update_cell(const UpdateArgs& a, const StageStat
         Wo2[1] = make_double2(w[2], w[3]);
         if (st.u32) store_f32(st.u32 + row * 4, t);
         return;
+    } else if (STAGE == 2 && FOLD) {
+        // 3/4 U + 1/4 (U + dt k1) + dt/4 k2 = U + dt/4 (k1 + k2) = U + 3/2 (W - U) with
+        // the running sum W = U + dt/6 (k1 + k2): no read of the stage state
+        const double2 u0 = U2[0], u1 = U2[1], w0 = W2[0], w1 = W2[1];
+        const double u[4] = {u0.x, u0.y, u1.x, u1.y};
+        double w[4] = {w0.x, w0.y, w1.x, w1.y};
+        const double c1 = dt * (1.0 / 6.0) * iv;
+        double t[4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            w[i] = w[i] + c1 * r[i];
+            t[i] = u[i] + 1.5 * (w[i] - u[i]);
+        }
+        Ut2[0] = make_double2(t[0], t[1]);
+        Ut2[1] = make_double2(t[2], t[3]);
+        Wo2[0] = make_double2(w[0], w[1]);
+        Wo2[1] = make_double2(w[2], w[3]);
+        if (st.u32) store_f32(st.u32 + row * 4, t);
+        return;
     } else if (STAGE == 2) {
         const double2 u0 = U2[0], u1 = U2[1], s0 = Ut2[0], s1 = Ut2[1], w0 = W2[0], w1 = W2[1];
         const double u[4] = {u0.x, u0.y, u1.x, u1.y};
