@@ -109,8 +109,9 @@ def parse():
                          "total - warmup - steps (0: --wedge-develop)")
     ap.add_argument("--wedge-re", type=float, default=1e5,
                     help="Reynolds number of the wedge on the ramp length (viscous flux, no-slip walls); 0 = inviscid")
-    ap.add_argument("--wedge-variant", default="corrected", choices=["corrected", "robust"],
-                    help="TENO variant of the wedge (the corrected one keeps high order in the wall cells)")
+    ap.add_argument("--wedge-variant", default="robust", choices=["corrected", "robust"],
+                    help="TENO variant of the wedge (the corrected one keeps high order in the wall cells but goes "
+                         "non-finite at the ramp wall before the configured 2000 steps)")
     ap.add_argument("--batch-cases", type=int, default=256,
                     help="cases of the batched section (the four-quadrant ensemble); 0 skips it")
     ap.add_argument("--batch-steps", type=int, default=500, help="total steps of the batched section")
