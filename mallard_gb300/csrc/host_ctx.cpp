@@ -830,16 +830,23 @@ int mgpu_set_state(mgpu_ctx* ctx, const double* Uh, const double* primh) {
     return guarded([&] {
         if (!Uh) throw ArgFail("null state");
         ctx->upload_cells(ctx->U.p, Uh, 4);
-        if (primh) {
-            ctx->upload_cells(ctx->prim.p, primh, 5);
+        if (ctx->single() && !primh) {
+            // the FP32 form's step reads neither the FP64 primitives nor the
+            // sound speeds: they are recovered from U when a caller asks
+            ctx->prim_stale = true;
         } else {
-            ck(launch_primitives_batch(ctx->gas, ctx->N, ctx->U.p, ctx->prim.p, ctx->stream), "primitives");
+            if (primh) {
+                ctx->upload_cells(ctx->prim.p, primh, 5);
+            } else {
+                ck(launch_primitives_batch(ctx->gas, ctx->N, ctx->U.p, ctx->prim.p, ctx->stream), "primitives");
+            }
+            ck(launch_sound((int)ctx->N, ctx->gas.gamma, ctx->U.p, ctx->prim.p, ctx->snd.p, ctx->stream),
+               "sound speed");
+            ctx->prim_stale = false;
         }
-        ck(launch_sound((int)ctx->N, ctx->gas.gamma, ctx->U.p, ctx->prim.p, ctx->snd.p, ctx->stream), "sound speed");
         if (ctx->single()) ck(launch_to_f32((size_t)ctx->N * 4, ctx->U.p, ctx->U32.p, ctx->stream), "FP32 copy");
         ck(cudaMemsetAsync(ctx->flags.p, 0, sizeof(unsigned), ctx->stream), "cudaMemsetAsync");
         ck(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
-        ctx->prim_stale = false;
         return MGPU_OK;
     });
 }
