@@ -72,7 +72,7 @@ SEED = 20261203
 CFL = 0.5
 T_END = 0.3
 CPU_SAMPLE_N = 256
-SEL_THRESHOLD = 0.98
+SEL_THRESHOLD = 0.995
 WEDGE_CFL = 0.4
 GAS = dict(gamma=1.4, p_ref=101325.0, T_ref=298.15, rho_ref=1.225)
 # the four-quadrant states (rho, u, v, p) of UR, UL, LL, LR

@@ -260,7 +260,7 @@ class Solver:
         return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(("recon", "flux", "update", "cfl", "selector"))}
 
     # ---- learned stencil selector (FP32 form) --------------------------------
-    def attach_selector(self, selector, threshold=0.98, directional_threshold=2.0, every_stage=False, interval=1):
+    def attach_selector(self, selector, threshold=0.995, directional_threshold=2.0, every_stage=False, interval=1):
         """Drive this FP32-form solver's TENO decisions with a trained
         selector: a variable predicted central with probability >= threshold
         skips the smoothness indicators and the directional stencils; a

@@ -79,7 +79,7 @@ def test_bench_mesh_8_steps_and_learned_error(bench_case):
     with Selector() as sel:
         sel.load(path)
         f32, _ = make_pair(m, variant="robust", precision="fp32", gpu=True)
-        f32.attach_selector(sel, threshold=0.98, interval=2)
+        f32.attach_selector(sel, interval=4)
         f32.set_state(U, W)
         f32.run(0.5, STEPS)
         Ul, _ = f32.get_state()

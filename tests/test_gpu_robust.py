@@ -87,7 +87,9 @@ def test_fast_forms_to_the_end_time(precision):
     """The four-quadrant problem at 64 x 64 to t = 0.3 (the FP64 form's step
     count) in the FMA and FP32 forms against the FP64 form: density L1 within
     the spec bar 1e-3 (a TENO decision within round-off of its
-    threshold can flip at a shock, so neither is bit-close over a whole run)."""
+    threshold can flip at a shock, so neither is bit-close over a whole run),
+    and the same time within 1e-3 (each form takes its own CFL steps, whose
+    sizes follow the largest wave speed of its own state)."""
     m = tri_mesh(64, seed=20261203)
     U, W = four_quadrant(m)
     s, _ = make_pair(m, variant="robust", precision="fp64")
@@ -108,7 +110,7 @@ def test_fast_forms_to_the_end_time(precision):
     l1 = _l1(m, out, ref)
     print(f"robust {precision} vs fp64, t = {t:.4f} ({steps} steps, {precision} t = {t2:.4f}), 64^2: "
           f"density L1 {l1:.2e}")
-    assert np.isfinite(out).all() and abs(t2 - t) <= 1e-4 * t
+    assert np.isfinite(out).all() and abs(t2 - t) <= 1e-3 * t
     assert l1 <= 1e-3, l1
 
 
@@ -132,7 +134,7 @@ def test_learned_form_four_quadrant(interval):
     with Selector() as sel:
         sel.load(path)
         f32, _ = make_pair(m, variant="robust", precision="fp32")
-        f32.attach_selector(sel, threshold=0.98, interval=interval)
+        f32.attach_selector(sel, interval=interval)
         f32.set_state(U, W)
         f32.run(0.5, 300)
         Ug, _ = f32.get_state()

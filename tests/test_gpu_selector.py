@@ -165,7 +165,7 @@ def test_learned_form_error_and_gain():
 @pytest.mark.parametrize("problem", ["explosion", "four_quadrant"])
 def test_shipped_selector_error_and_work(problem, interval):
     """The trained weights shipped with the package, on problems they were not
-    trained on, at the default central threshold 0.98 with one prediction per
+    trained on, at the default central threshold 0.995 with one prediction per
     step: density L1 error against the plain FP64 run and the share of the
     full TENO work, held to the 1e-3 bar.  The explosion runs the corrected
     weighting for 80 steps; the four-quadrant problem runs the robust one
@@ -190,7 +190,7 @@ def test_shipped_selector_error_and_work(problem, interval):
     with Selector() as sel:
         sel.load(path)
         f32, _ = make_pair(m, variant=variant, precision="fp32")
-        f32.attach_selector(sel, threshold=0.98, interval=interval)
+        f32.attach_selector(sel, interval=interval)
         f32.set_state(U, W)
         f32.run(0.5, steps)
         Ug, _ = f32.get_state()
