@@ -1,9 +1,12 @@
-"""mgpu_calc_dt_noalloc: the CFL time step for callers that cannot allocate
-device memory while stepping (graph capture, foreign allocators, fixed
-pools).  It must give the same dt and per-cell spectral radius as
-mgpu_calc_dt, including on consecutive calls that reuse its static scratch.
+"""mgpu_calc_dt_noalloc: the CFL time step for callers that must not allocate
+device memory once they are stepping (an application whose device memory
+all comes from its own pool, a real-time loop that cannot take the
+device-wide synchronisation of cudaMalloc/cudaFree).  It must give the same
+dt and per-cell spectral radius as mgpu_calc_dt, including on consecutive
+calls that reuse its static scratch.
 
-This file is collected last on purpose.
+This file is collected last on purpose: if it fails, a run that stops at the
+first failure has already run every other test.
 """
 
 import ctypes
