@@ -71,7 +71,6 @@ struct GlobalSrc {
     __device__ __forceinline__ const uint4* nb(int s) const {
         return reinterpret_cast<const uint4*>(a.nb4) + (size_t)(tile * B::S + s) * B::GJ * TILE;
     }
-    __device__ __forceinline__ uint4 nb_ld(const uint4* p) const { return __ldg(p); }
     __device__ __forceinline__ const float4* P(int s) const {
         return reinterpret_cast<const float4*>(a.P4) + (size_t)(tile * B::S + s) * B::GP * TILE;
     }
@@ -165,24 +164,19 @@ __device__ __forceinline__ bool teno32_cell(const TenoArgs& a, const float* __re
         for (int k = 0; k < KR; ++k) coef[s][k] = 0.0f;
         x[s] = 0.0f;
         if (!((tile_need >> s) & 1u)) continue;
-        const bool mine = (need >> s) & 1u;
-        // differences to the target cell's average over the stencil: the
-        // neighbour ids and states are loaded before the stencil's table
-        // block is waited for, so the two latencies overlap
-        float d[GJ * 4];
-        if (mine) {
+        ok = src.begin(s) && ok;
+        if (ok && ((need >> s) & 1u)) {
+            // differences to the target cell's average over the stencil
             const uint4* nbp = src.nb(s) + lane;
+            float d[GJ * 4];
 #pragma unroll
             for (int g = 0; g < GJ; ++g) {
-                const uint4 n = src.nb_ld(nbp + g * TILE);
+                const uint4 n = src.ld(nbp + g * TILE);
                 const uint32_t id[4] = {n.x, n.y, n.z, n.w};
 #pragma unroll
                 for (int e = 0; e < 4; ++e)
                     if (g * 4 + e < MR) d[g * 4 + e] = __ldg(U + ix.u(id[e]) * NC + v) - uc;
             }
-        }
-        ok = src.begin(s) && ok;
-        if (ok && mine) {
             if (s == 0 && a.bcell) {
 #pragma unroll
                 for (int j = 0; j < MR; ++j) {
@@ -369,14 +363,10 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned by
                  : "memory");
 }
 
-// IDS: a slot holds the stencil's neighbour ids after its pseudo-inverse
-// (the resident-table batch kernel); without, the ids are read from global
-// memory (the staged kernels, which gather with them before the slot's
-// copy has landed).
-template <int K, int M, int NQ, int NSLOT, bool IDS = true>
+template <int K, int M, int NQ, int NSLOT>
 struct StageLayout {
     using B = TileBlocks<K, M, NQ>;
-    static constexpr unsigned SLOT = B::PB + (IDS ? B::NBB : 0u);  // pseudo-inverse, then neighbour ids
+    static constexpr unsigned SLOT = B::PB + B::NBB;                // pseudo-inverse, then neighbour ids
     static constexpr unsigned PHI = NSLOT * SLOT;                   // face-shape codes of the tile
     static constexpr unsigned BAR = PHI + B::CB;                    // NSLOT + 1 mbarriers
     static constexpr unsigned WARP = (BAR + 8 * (NSLOT + 1) + 127) / 128 * 128;
@@ -387,7 +377,7 @@ struct StageLayout {
 template <int K, int M, int NQ, int NSLOT>
 struct StageSrc {
     using B = TileBlocks<K, M, NQ>;
-    using L = StageLayout<K, M, NQ, NSLOT, false>;
+    using L = StageLayout<K, M, NQ, NSLOT>;
     const TenoArgs& a;
     uint8_t* base;
     int tile, lane32;
@@ -403,6 +393,8 @@ struct StageSrc {
         uint8_t* slot = base + (i % NSLOT) * L::SLOT;
         mbar_expect_tx(bar(i % NSLOT), L::SLOT);
         bulk_g2s(slot, reinterpret_cast<const char*>(a.P4) + (size_t)(tile * B::S + s) * B::PB, B::PB, bar(i % NSLOT));
+        bulk_g2s(slot + B::PB, reinterpret_cast<const char*>(a.nb4) + (size_t)(tile * B::S + s) * B::NBB, B::NBB,
+                 bar(i % NSLOT));
     }
     // all lanes: the union of the cells' stencils, then the first copies
     __device__ __forceinline__ unsigned tile_need(unsigned need) {
@@ -432,11 +424,9 @@ struct StageSrc {
             issued = i + NSLOT + 1;
         }
     }
-    // the neighbour ids come from global memory (gathered with before the slot's copy lands)
     __device__ __forceinline__ const uint4* nb(int s) const {
-        return reinterpret_cast<const uint4*>(a.nb4) + (size_t)(tile * B::S + s) * B::GJ * TILE;
+        return reinterpret_cast<const uint4*>(base + (index(s) % NSLOT) * L::SLOT + B::PB);
     }
-    __device__ __forceinline__ uint4 nb_ld(const uint4* p) const { return __ldg(p); }
     __device__ __forceinline__ const float4* P(int s) const {
         return reinterpret_cast<const float4*>(base + (index(s) % NSLOT) * L::SLOT);
     }
@@ -458,7 +448,7 @@ __global__ void __launch_bounds__(WARPS * 32, MINB) teno32_staged_kernel(const T
                                                                          uint8_t* __restrict__ masks,
                                                                          const uint8_t* __restrict__ pred,
                                                                          unsigned* __restrict__ err) {
-    using L = StageLayout<K, M, NQ, NSLOT, false>;
+    using L = StageLayout<K, M, NQ, NSLOT>;
     using B = TileBlocks<K, M, NQ>;
     extern __shared__ __align__(128) uint8_t stage_smem[];
     const int w = threadIdx.x >> 5, lane32 = threadIdx.x & 31;
@@ -824,7 +814,7 @@ cudaError_t teno_go1(const TenoArgs& a, const float* U, float* fv, uint8_t* mask
 template <int K, int M, int NQ, bool SEL, int NSLOT, int WARPS, int MINB>
 cudaError_t teno_staged1(const TenoArgs& a, const float* U, float* fv, uint8_t* masks, const uint8_t* pred,
                          cudaStream_t s) {
-    constexpr unsigned smem = WARPS * StageLayout<K, M, NQ, NSLOT, false>::WARP;
+    constexpr unsigned smem = WARPS * StageLayout<K, M, NQ, NSLOT>::WARP;
     static bool attr = false;
     if (!attr) {
         const cudaError_t e = cudaFuncSetAttribute(teno32_staged_kernel<K, M, NQ, SEL, NSLOT, WARPS, MINB>,
@@ -946,7 +936,7 @@ __global__ void __launch_bounds__(128) flux32_pair_batch_kernel(const BatchLaunc
 template <int K, int M, int NQ, int NSLOT, int WARPS, int MINB>
 __global__ void __launch_bounds__(WARPS * 32, MINB) teno32_batch_staged_kernel(const BatchLaunch b,
                                                                                const float* __restrict__ U) {
-    using L = StageLayout<K, M, NQ, NSLOT, false>;
+    using L = StageLayout<K, M, NQ, NSLOT>;
     using B = TileBlocks<K, M, NQ>;
     extern __shared__ __align__(128) uint8_t stage_smem[];
     const int w = threadIdx.x >> 5, lane32 = threadIdx.x & 31;
@@ -992,7 +982,6 @@ struct ResidentSrc {
     __device__ __forceinline__ const uint4* nb(int s) const {
         return reinterpret_cast<const uint4*>(base + s * L::SLOT + B::PB);
     }
-    __device__ __forceinline__ uint4 nb_ld(const uint4* p) const { return *p; }
     __device__ __forceinline__ const float4* P(int s) const { return reinterpret_cast<const float4*>(base + s * L::SLOT); }
     __device__ __forceinline__ const uint16_t* codes() { return reinterpret_cast<const uint16_t*>(base + L::PHI); }
     template <class T>
@@ -1078,7 +1067,7 @@ cudaError_t teno_batch_resident(const BatchLaunch& b, const float* U, cudaStream
 
 template <int K, int M, int NQ, int NSLOT, int WARPS, int MINB>
 cudaError_t teno_batch_staged(const BatchLaunch& b, const float* U, cudaStream_t s) {
-    constexpr unsigned smem = WARPS * StageLayout<K, M, NQ, NSLOT, false>::WARP;
+    constexpr unsigned smem = WARPS * StageLayout<K, M, NQ, NSLOT>::WARP;
     static bool attr = false;
     if (!attr) {
         const cudaError_t e = cudaFuncSetAttribute(teno32_batch_staged_kernel<K, M, NQ, NSLOT, WARPS, MINB>,
