@@ -217,9 +217,11 @@ typedef struct mgpu_config {
      * no-slip and adiabatic; other boundaries carry no viscous flux. */
     int viscous;
     double mu_ref, T_mu_ref, sutherland_S, prandtl;
-    /* Where mgpu_finalize computes the TENO least-squares tables
-     * (face_reconstruction.cpp:477-741): MGPU_TABLES_GPU (default; Legendre
-     * basis, else the host) or MGPU_TABLES_HOST.  Both give the same bits. */
+    /* Where mgpu_finalize builds the TENO tables: MGPU_TABLES_GPU (default:
+     * the stencil search, face_reconstruction.cpp:217-475, on the GPU, and
+     * the least squares, :477-741, on the GPU for the Legendre basis, on the
+     * host for the monomial one) or MGPU_TABLES_HOST (both on the host).
+     * Both give the same bits. */
     int table_build;
 } mgpu_config;
 
@@ -450,10 +452,11 @@ enum {
 };
 int mgpu_get_table(mgpu_ctx* ctx, int field, void* dst, uint64_t* bytes);
 /* Wall seconds of mgpu_finalize's phases, seconds[7]: 0 face and cell
- * numbering, 1 geometry and gather lists, 2 TENO stencil search (host), 3
- * table pack (host; includes the host least squares when built there) and
- * upload, 4 least squares on the GPU, 5 other TENO setup, 6 the remaining
- * uploads. */
+ * numbering, 1 geometry and gather lists, 2 TENO stencil search (on the GPU
+ * with MGPU_TABLES_GPU, else on the host; includes the neighbourhood graph
+ * and the stencils' host copy), 3 table pack (host; includes the host least
+ * squares when built there) and upload, 4 least squares on the GPU, 5 other
+ * TENO setup, 6 the remaining uploads. */
 int mgpu_build_times(mgpu_ctx* ctx, double* seconds);
 uint32_t mgpu_n_cells(const mgpu_ctx* ctx);
 

@@ -50,7 +50,10 @@ def _jobs(cuda):
         o = OUT / (s.stem + ".o")
         # *_fast.cu may contract a*b+c into FMA; everything else keeps two roundings
         fmad = "-fmad=true" if s.stem.endswith("_fast") else "-fmad=false"
-        jobs.append((o, [nvcc, ARCH, "-O3", "-lineinfo", fmad, "-std=c++17", "-Xcompiler", "-fPIC",
+        # the stencil search calls std::sort in device code: constexpr (and
+        # so callable there) from C++20 on
+        std = ["-std=c++20", "--expt-relaxed-constexpr"] if s.stem == "stencil_search" else ["-std=c++17"]
+        jobs.append((o, [nvcc, ARCH, "-O3", "-lineinfo", fmad, *std, "-Xcompiler", "-fPIC",
                          "-Xptxas", "-v", "-c", str(s), "-o", str(o)]))
     cxx = os.environ.get("CXX", "g++")
     for s in cpp:

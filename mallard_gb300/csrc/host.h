@@ -69,8 +69,18 @@ struct TenoTables {
 // Throws std::runtime_error with the reference's messages on failure.
 // build_teno_stencils fills everything but mats/areas; teno_stencil_lsq then
 // computes one stencil's pseudo-inverse (K x M_s) and transformed areas,
-// so callers can write them straight into their own layout.
-void build_teno_stencils(const mgpu_mesh& m, int basis, int p, double factor, int q_cell, int q_face, TenoTables& t);
+// so callers can write them straight into their own layout.  gpu_search:
+// the stencils are found on the current CUDA device (gpu_stencil_search),
+// the cells it could not finish again on the host; same result.
+void build_teno_stencils(const mgpu_mesh& m, int basis, int p, double factor, int q_cell, int q_face, TenoTables& t,
+                         bool gpu_search = false);
+// The stencil search on the current CUDA device (stencil_search.cu): the
+// four stencils of every triangle, [cell][4][M], with their sizes, as the
+// host search finds them; status[c] = 1 marks a cell the device did not
+// finish (its sizes are 0).  goff/gnb: each cell's first-order
+// neighbourhood, itself included, sorted.  False, with msg, on a CUDA error.
+bool gpu_stencil_search(const mgpu_mesh& m, const uint32_t* goff, const uint32_t* gnb, int M, uint32_t* flat,
+                        uint8_t* sizes, uint8_t* status, std::string& msg);
 struct LsqWork;
 LsqWork* lsq_work_new();
 void lsq_work_free(LsqWork* w);

@@ -280,7 +280,7 @@ void mgpu_ctx::build() {
     if (cfg.recon == MGPU_RECON_TENO) {
         TenoTables t;
         build_teno_stencils(mv, cfg.basis, cfg.poly_order, cfg.max_stencil_size_factor, cfg.quadrature_order_cell,
-                            cfg.quadrature_order_face, t);
+                            cfg.quadrature_order_face, t, cfg.table_build == MGPU_TABLES_GPU);
         lap(2);
         K = t.K;
         M = t.M;

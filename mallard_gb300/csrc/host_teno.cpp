@@ -22,6 +22,7 @@
 #include <stdexcept>
 #include <string>
 #include <cstring>
+#include <memory>
 #include <utility>
 
 #ifdef _OPENMP
@@ -145,21 +146,38 @@ struct Graph {
 
 Graph neighbourhoods(const mgpu_mesh& m) {
     Graph g;
-    g.off.assign((size_t)m.n_cells + 1, 0);
-    std::vector<uint32_t> tmp;
-    for (uint32_t c = 0; c < m.n_cells; ++c) {
-        tmp.clear();
-        tmp.push_back(c);
-        for (uint32_t k = m.offsets_faces_of_cell[c]; k < m.offsets_faces_of_cell[c + 1]; ++k) {
-            const uint32_t f = m.faces_of_cell[k];
-            const int32_t a = m.cells_of_face[2 * (size_t)f], b = m.cells_of_face[2 * (size_t)f + 1];
-            if (b == -1) continue;
-            tmp.push_back(a == (int32_t)c ? (uint32_t)b : (uint32_t)a);
+    const uint32_t N = m.n_cells;
+    g.off.assign((size_t)N + 1, 0);
+    // per cell at most 1 + its faces entries: fill fixed slots in parallel,
+    // then compact
+    std::vector<uint32_t> cnt(N), slot(N + (size_t)m.offsets_faces_of_cell[N]);
+#pragma omp parallel
+    {
+        std::vector<uint32_t> tmp;
+#pragma omp for schedule(static)
+        for (int64_t ci = 0; ci < (int64_t)N; ++ci) {
+            const uint32_t c = (uint32_t)ci;
+            tmp.clear();
+            tmp.push_back(c);
+            for (uint32_t k = m.offsets_faces_of_cell[c]; k < m.offsets_faces_of_cell[c + 1]; ++k) {
+                const uint32_t f = m.faces_of_cell[k];
+                const int32_t a = m.cells_of_face[2 * (size_t)f], b = m.cells_of_face[2 * (size_t)f + 1];
+                if (b == -1) continue;
+                tmp.push_back(a == (int32_t)c ? (uint32_t)b : (uint32_t)a);
+            }
+            std::sort(tmp.begin(), tmp.end());
+            tmp.erase(std::unique(tmp.begin(), tmp.end()), tmp.end());
+            cnt[c] = (uint32_t)tmp.size();
+            std::copy(tmp.begin(), tmp.end(), &slot[c + (size_t)m.offsets_faces_of_cell[c]]);
         }
-        std::sort(tmp.begin(), tmp.end());
-        tmp.erase(std::unique(tmp.begin(), tmp.end()), tmp.end());
-        g.nb.insert(g.nb.end(), tmp.begin(), tmp.end());
-        g.off[c + 1] = (uint32_t)g.nb.size();
+    }
+    for (uint32_t c = 0; c < N; ++c) g.off[c + 1] = g.off[c] + cnt[c];
+    g.nb.resize(g.off[N]);
+#pragma omp parallel for schedule(static)
+    for (int64_t ci = 0; ci < (int64_t)N; ++ci) {
+        const uint32_t c = (uint32_t)ci;
+        std::copy(&slot[c + (size_t)m.offsets_faces_of_cell[c]], &slot[c + (size_t)m.offsets_faces_of_cell[c]] + cnt[c],
+                  &g.nb[g.off[c]]);
     }
     return g;
 }
@@ -483,7 +501,8 @@ double teno_target_area(const mgpu_mesh& m, const TenoTables& t, uint32_t c, Lsq
     return w.s.at[0];
 }
 
-void build_teno_stencils(const mgpu_mesh& m, int basis, int p, double factor, int q_cell, int q_face, TenoTables& t) {
+void build_teno_stencils(const mgpu_mesh& m, int basis, int p, double factor, int q_cell, int q_face, TenoTables& t,
+                         bool gpu_search) {
     if (p < 1 || p > 4) throw std::runtime_error("TENO basis order must be 1..4");
     t.basis = basis;
     t.p = p;
@@ -511,10 +530,16 @@ void build_teno_stencils(const mgpu_mesh& m, int basis, int p, double factor, in
     const int S = 4;  // 1 central + 3 directional for triangles
     const Graph g = neighbourhoods(m);
 
-    // --- stencils, stored [cell][S][M] with their sizes
-    std::vector<uint32_t> flat((size_t)N * S * M, 0);
+    // --- stencils, stored [cell][S][M] with their sizes (each written up
+    // to its size); on the GPU, then on the host for the cells it marks
+    // (all of them without it)
+    std::unique_ptr<uint32_t[]> flat(new uint32_t[(size_t)N * S * M]);
     std::vector<uint8_t> sizes((size_t)N * S, 0);
+    std::vector<uint8_t> redo(N, 1);
     std::string err;
+    if (gpu_search && M <= 255 && !gpu_stencil_search(m, g.off.data(), g.nb.data(), M, flat.get(), sizes.data(),
+                                                      redo.data(), err))
+        throw std::runtime_error(err);
     int nthreads = 1;
 #ifdef _OPENMP
     nthreads = omp_get_max_threads();
@@ -522,10 +547,15 @@ void build_teno_stencils(const mgpu_mesh& m, int basis, int p, double factor, in
 #pragma omp parallel num_threads(nthreads)
     {
         RingBuilder rb;
-        rb.init(m, g);
         std::vector<std::vector<uint32_t>> st;
+        bool ready = false;
 #pragma omp for schedule(dynamic, 256)
         for (int64_t ci = 0; ci < (int64_t)N; ++ci) {
+            if (!redo[ci]) continue;
+            if (!ready) {
+                rb.init(m, g);
+                ready = true;
+            }
             try {
                 cell_stencils(rb, (uint32_t)ci, M, st);
                 for (int s = 0; s < S; ++s) {
@@ -554,13 +584,13 @@ void build_teno_stencils(const mgpu_mesh& m, int basis, int p, double factor, in
         }
     }
     t.stencils.resize(t.off_stencils.back());
-    for (uint32_t c = 0; c < N; ++c)
+#pragma omp parallel for schedule(static)
+    for (int64_t ci = 0; ci < (int64_t)N; ++ci)
         for (int s = 0; s < S; ++s) {
-            const size_t i = (size_t)c * S + s;
+            const size_t i = (size_t)ci * S + s;
             std::copy(&flat[i * M], &flat[i * M] + sizes[i], &t.stencils[t.off_stencils[i]]);
         }
-    flat.clear();
-    flat.shrink_to_fit();
+    flat.reset();
     // --- basis means from cell 0's central stencil (:598-602)
     t.ipt.assign(K, 0.0);
     {

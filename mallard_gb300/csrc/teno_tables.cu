@@ -1,9 +1,9 @@
 // teno_tables.cu -- the TENO least-squares tables built on the GPU.
 //
-// The host finds the stencils (face_reconstruction.cpp:217-475, a graph
-// search that takes a few percent of the build); this kernel then computes
-// what compute_reconstruction_matrices computes for every stencil
-// (face_reconstruction.cpp:477-741, common_math.h:355-493): the basis
+// The stencils come from the search (face_reconstruction.cpp:217-475;
+// stencil_search.cu on the GPU, host_teno.cpp on the host); this kernel
+// then computes what compute_reconstruction_matrices computes for every
+// stencil (face_reconstruction.cpp:477-741, common_math.h:355-493): the basis
 // moments of each stencil cell in the target cell's reference frame, the
 // mean subtraction, the Householder QR of the reduced (M-1) x (K-1) system
 // and the two triangular solves of the pseudo-inverse.  It writes the

@@ -70,3 +70,37 @@ def test_monomial_basis_builds_on_the_host():
               boundaries=blist, precision="fp64", **GAS)
     with mg.Solver(m, table_build="host", **kw) as sh, mg.Solver(m, table_build="gpu", **kw) as sg:
         np.testing.assert_array_equal(sh.get_table("P"), sg.get_table("P"))
+
+
+def test_gpu_stencil_search_on_a_tied_mesh():
+    """The stencil search on the GPU (stencil_search.cu) against the host's
+    (host_teno.cpp): on a permuted 96x96 cartesian_tri mesh, where almost
+    every ring of more than 16 cells holds equal distances, the neighbour
+    tables -- every stencil's cells in order -- agree, so std::sort's order
+    among ties is the host's."""
+    m = mg.Mesh.generate("cartesian_tri", 96, 96, 1.0, 1.0)
+    m.permute_cells(11)
+    with _solver(m, "fp32", 3, "host") as sh, _solver(m, "fp32", 3, "gpu") as sg:
+        th, tg = sh.get_table("nb32"), sg.get_table("nb32")
+        assert th.shape == tg.shape
+        np.testing.assert_array_equal(th, tg)
+
+
+def test_gpu_stencil_search_errors_as_the_host():
+    """A mesh too small for the stencil: the cells the GPU cannot fill go
+    back to the host search, which raises the reference's error."""
+    m = mg.Mesh.generate("cartesian_tri", 3, 2, 1.0, 1.0)
+    for build in ("host", "gpu"):
+        with pytest.raises(mg.MgpuError, match="Mesh too small for the TENO stencil size"):
+            _solver(m, "fp64", 3, build)
+
+
+def test_gpu_stencil_search_time():
+    """At 1024x1024 (2,097,152 cells) the search on the GPU, with the
+    neighbourhood graph and the stencil layout on the host, takes about
+    0.16 s on a GB300 (the host search takes 1.4 s on its 16 cores)."""
+    m = mg.Mesh.generate("cartesian_tri", 1024, 1024, 1.0, 1.0)
+    with _solver(m, "fp32", 3, "gpu") as s:
+        t = s.build_times()
+    print("build times", t)
+    assert t["stencil_search"] < 0.4, t
