@@ -383,7 +383,7 @@ struct StageSrc {
     int tile, lane32;
     unsigned need_all = 0;  // stencils some cell of the tile evaluates
     int cnt = 0, issued = 0;
-    bool phi_ready = false, ok = true;
+    bool phi_ready = false, ok = true, pre = false;
     __device__ __forceinline__ uint64_t* bar(int i) { return reinterpret_cast<uint64_t*>(base + L::BAR) + i; }
     // the i-th stencil of need_all into slot i % NSLOT (lane 0)
     __device__ __forceinline__ void issue(int i) {
@@ -396,13 +396,22 @@ struct StageSrc {
         bulk_g2s(slot + B::PB, reinterpret_cast<const char*>(a.nb4) + (size_t)(tile * B::S + s) * B::NBB, B::NBB,
                  bar(i % NSLOT));
     }
+    // all lanes, at the warp's start: the central stencil's copy, before
+    // the cells' states and predictions (which decide the rest) arrive.
+    // The central stencil is then staged for every tile, also one whose
+    // cells all skip it (only a confident directional prediction does).
+    __device__ __forceinline__ void prefetch_central() {
+        need_all = 1u;
+        pre = true;
+        if (lane32 == 0) issue(0);
+    }
     // all lanes: the union of the cells' stencils, then the first copies
     __device__ __forceinline__ unsigned tile_need(unsigned need) {
-        need_all = __reduce_or_sync(0xffffffffu, need);
+        need_all = __reduce_or_sync(0xffffffffu, need) | (pre ? 1u : 0u);
         cnt = __popc(need_all);
         issued = cnt < NSLOT ? cnt : NSLOT;
         if (lane32 == 0)
-            for (int i = 0; i < issued; ++i) issue(i);
+            for (int i = pre ? 1 : 0; i < issued; ++i) issue(i);
         return need_all;
     }
     __device__ __forceinline__ int index(int s) const { return __popc(need_all & ((1u << s) - 1u)); }
@@ -464,6 +473,7 @@ __global__ void __launch_bounds__(WARPS * 32, MINB) teno32_staged_kernel(const T
         bulk_g2s(src.base + L::PHI, reinterpret_cast<const char*>(a.fcode) + (size_t)tile * B::CB, B::CB, src.bar(NSLOT));
     }
     __syncwarp();
+    src.prefetch_central();
     const int cell = tile * 8 + (lane32 >> 2), v = lane32 & 3;
     // cells past the mesh take part in the warp's collective steps with
     // nothing to do: smask 0, no prediction, no writes
@@ -956,6 +966,7 @@ __global__ void __launch_bounds__(WARPS * 32, MINB) teno32_batch_staged_kernel(c
         bulk_g2s(src.base + L::PHI, reinterpret_cast<const char*>(a.fcode) + (size_t)tile * B::CB, B::CB, src.bar(NSLOT));
     }
     __syncwarp();
+    src.prefetch_central();
     const int cell = tile * 8 + (lane32 >> 2), v = lane32 & 3;
     teno32_cell<K, M, NQ, false>(a, U, b.fv, nullptr, nullptr, cell, v, 0xffffffffu,
                                  IxB{b.ubase[gi], b.fbase[gi], C, cs}, src, cell < b.n_cells[gi]);
