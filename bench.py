@@ -564,8 +564,8 @@ def run_wedge(args, device, selector):
     t0 = time.perf_counter()
     mesh = mg.Mesh.ramp_channel(nx, ny, 3.0, 1.0, 0.5, 15.0, 0.2, seed=SEED)
     re = args.wedge_re if args.wedge_re > 0 else None
-    flow = (f"viscous Re {re:g} on the ramp length, Pr 0.72, Sutherland, no-slip adiabatic walls" if re
-            else "inviscid (slip walls)")
+    flow = (f"viscous Re {re:g} on the ramp length, Pr 0.72, Sutherland, no-slip adiabatic walls, cell gradients "
+            f"of the reconstructed polynomials" if re else "inviscid (slip walls)")
     out = {"workload": f"ramp channel {nx}x{ny} lattice -> {mesh.n_cells} Delaunay triangles, 15 deg ramp, "
                        f"Mach 2.5, TENO p3 ({args.wedge_variant}) + Rusanov, SSPRK3 CFL {WEDGE_CFL}, {flow}; timed "
                        f"after {develop} development steps",

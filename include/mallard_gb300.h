@@ -69,6 +69,7 @@ enum { MGPU_BASIS_MONOMIAL = 0, MGPU_BASIS_LEGENDRE = 1 };
 enum { MGPU_RIEMANN_RUSANOV = 0, MGPU_RIEMANN_HLL = 1, MGPU_RIEMANN_HLLC = 2 };
 enum { MGPU_INTEGRATOR_SSPRK3 = 0, MGPU_INTEGRATOR_FE = 1, MGPU_INTEGRATOR_RK4 = 2 };
 enum { MGPU_TABLES_GPU = 0, MGPU_TABLES_HOST = 1 };
+enum { MGPU_VISC_GRAD_RECON = 0, MGPU_VISC_GRAD_GREEN_GAUSS = 1 };
 enum {
     MGPU_BC_SYMMETRY = 0,
     MGPU_BC_EXTRAPOLATION = 1,
@@ -211,8 +212,8 @@ typedef struct mgpu_config {
      * mu(T) = mu_ref (T/T_mu_ref)^1.5 (T_mu_ref + S) / (T + S) (Sutherland)
      * for sutherland_S > 0, else the constant mu_ref; conductivity
      * mu cp / prandtl; temperatures in the units of the solver's T = e / cv.
-     * Gradients: Green-Gauss per cell from the cell averages, at a face the
-     * average of its two cells' plus the jump correction along the line
+     * Cell gradients of (u, v, T) as viscous_gradients selects; at a face
+     * the average of its two cells' plus the jump correction along the line
      * joining their centres.  With viscous != 0 wall_adiabatic walls are
      * no-slip and adiabatic; other boundaries carry no viscous flux. */
     int viscous;
@@ -223,6 +224,17 @@ typedef struct mgpu_config {
      * host for the monomial one) or MGPU_TABLES_HOST (both on the host).
      * Both give the same bits. */
     int table_build;
+    /* Cell gradients of the viscous flux: MGPU_VISC_GRAD_RECON (default)
+     * differentiates each cell's reconstructed TENO polynomials at its
+     * centroid -- the conserved variables' gradients, after the variant's
+     * per-cell step (the robust variant's scaling, or zero where a cell falls
+     * back to its average), turned into (u, v, T) gradients with the cell
+     * averages; the reconstruction kernel writes them, so no gradient
+     * kernel runs.  With first-order reconstruction, or
+     * MGPU_VISC_GRAD_GREEN_GAUSS, the Green-Gauss gradients of the cell
+     * averages: (1/V) sum_f phi_f n A, phi_f the mean of the two cells (a
+     * wall: u = v = 0, T of the cell; another boundary: the cell's value). */
+    int viscous_gradients;
 } mgpu_config;
 
 typedef struct mgpu_ctx mgpu_ctx;

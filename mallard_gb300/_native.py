@@ -24,6 +24,7 @@ INTEGRATORS = {"SSPRK3": 0, "FE": 1, "RK4": 2}
 BC_TYPES = {"symmetry": 0, "extrapolation": 1, "wall_adiabatic": 2, "upt": 3, "p_out": 4}
 TENO_VARIANTS = {"reference": 0, "corrected": 1, "robust": 2}
 PRECISIONS = {"fp64": 0, "fp64_fast": 1, "fp32": 2}
+VISC_GRADIENTS = {"recon": 0, "green_gauss": 1}
 AUTOTUNE_SHAPES = 8  # MGPU_AUTOTUNE_SHAPES
 
 TENO_FIELDS = {
@@ -66,7 +67,7 @@ class Config(C.Structure):
         ("rho_ref", C.c_double), ("p_min", C.c_double), ("p_max", C.c_double), ("teno_variant", C.c_int),
         ("precision", C.c_int), ("reorder", C.c_int), ("device", C.c_int),
         ("viscous", C.c_int), ("mu_ref", C.c_double), ("T_mu_ref", C.c_double), ("sutherland_S", C.c_double),
-        ("prandtl", C.c_double), ("table_build", C.c_int),
+        ("prandtl", C.c_double), ("table_build", C.c_int), ("viscous_gradients", C.c_int),
     ]
 
 

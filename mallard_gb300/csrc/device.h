@@ -68,6 +68,20 @@ struct TenoArgs {
     unsigned* err;                // status word: bit 2 when a bounded wait ran out (staged FP32 form)
     // robust TENO variant: per cell 1 if it has a boundary face
     const uint8_t* bcell;         // null unless the variant is MGPU_TENO_ROBUST
+    // Viscous gradients from the reconstruction (MGPU_VISC_GRAD_RECON): the
+    // kernel differentiates each cell's polynomials at its centroid and
+    // writes the cell's (u, v, T) and their gradients.  Null vgrad / vq:
+    // not asked.
+    const double* ji;             // [n_cells][4] inverse Jacobian of the cell's reference frame (FP64 forms)
+    const float4* ji4;            // the same in FP32 (FP32 form)
+    double dphi[2 * KR_MAX];      // [k][2] basis gradient (d/dxi_0, d/dxi_1) at the reference centroid, k >= 1
+    float dphif[2 * KR_MAX];
+    double cv;                    // specific heat at constant volume (T = e / cv)
+    float inv_cv;
+    double* vgrad;                // FP64 forms: [n_cells][6] du/dx, du/dy, dv/dx, dv/dy, dT/dx, dT/dy
+    float4* vq;                   // FP32 form: the Visc32Args records (u, v, T, 0), (du, dv), (dT)
+    float4* vga;
+    float2* vgb;
 };
 
 struct FluxArgs {
@@ -117,6 +131,7 @@ struct ViscArgs {
     double* grad;           // [n_cells][6]: du/dx, du/dy, dv/dx, dv/dy, dT/dx, dT/dy
     double* G;
     double mu_ref, T_ref, S, cp_over_pr;
+    int grad_ready;         // 1: the reconstruction wrote grad (no Green-Gauss kernel)
 };
 
 // FP32 form of the viscous flux: (u, v, T) and their Green-Gauss gradients

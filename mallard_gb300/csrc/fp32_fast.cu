@@ -79,18 +79,28 @@ struct GlobalSrc {
     __device__ __forceinline__ T ld(const T* p) const { return __ldg(p); }
 };
 
+// (u, v, T) of an FP32 state with one correctly rounded reciprocal of the
+// density.
+__device__ __forceinline__ float4 uvT32(const float4 x, float inv_cv) {
+    const float ir = __frcp_rn(x.x);
+    const float u = x.y * ir, v = x.z * ir;
+    const float e = x.w * ir - 0.5f * (u * u + v * v);
+    return make_float4(u, v, e * inv_cv, 0.0f);
+}
+
 // The robust variant's per-cell step in FP32 (teno_flux.cuh's robust_cell):
 // a cell with a boundary face takes its average at every face point;
 // otherwise each variable's deviations are scaled into the central
 // stencil's range [dlo, dhi] (when that stencil was evaluated), and a cell
 // with a face state that is then not admissible takes its average at every
 // face point.  Every lane of live calls it (the cell's four lanes exchange
-// their variables).
+// their variables).  Returns the factor the variable's polynomial was
+// scaled by (1: kept, 0: replaced by the average).
 template <int NF, int NQ>
-__device__ __forceinline__ void robust_cell32(const TenoArgs& a, bool boundary, bool have_range, unsigned live,
-                                              float uc, float dlo, float dhi, float (&out)[NF][NQ]) {
+__device__ __forceinline__ float robust_cell32(const TenoArgs& a, bool boundary, bool have_range, unsigned live,
+                                               float uc, float dlo, float dhi, float (&out)[NF][NQ]) {
+    float th = 1.0f;
     if (!boundary && have_range) {
-        float th = 1.0f;
 #pragma unroll
         for (int fl = 0; fl < NF; ++fl)
 #pragma unroll
@@ -122,6 +132,33 @@ __device__ __forceinline__ void robust_cell32(const TenoArgs& a, bool boundary, 
         for (int fl = 0; fl < NF; ++fl)
 #pragma unroll
             for (int q = 0; q < NQ; ++q) out[fl][q] = uc;
+    return bad ? 0.0f : th;
+}
+
+// Viscous gradients from the reconstruction in FP32 (teno_flux.cuh's
+// write_visc_grad): lane v holds the gradient (gx, gy) of conserved
+// variable v's polynomial at the cell centroid and the cell average uc;
+// lane 0 of the cell writes the Visc32Args records when `write`.  Every lane
+// of live calls it.
+__device__ __forceinline__ void write_visc_grad32(const TenoArgs& a, int cell, int v, unsigned live, float uc,
+                                                  float gx, float gy, bool write) {
+    float r[4], x[4], y[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        r[i] = __shfl_sync(live, uc, i, 4);
+        x[i] = __shfl_sync(live, gx, i, 4);
+        y[i] = __shfl_sync(live, gy, i, 4);
+    }
+    if (v != 0 || !write) return;
+    const float4 q = uvT32(make_float4(r[0], r[1], r[2], r[3]), a.inv_cv);
+    const float ir = __frcp_rn(r[0]), E = r[3] * ir;
+    const float ux = (x[1] - q.x * x[0]) * ir, uy = (y[1] - q.x * y[0]) * ir;
+    const float vx = (x[2] - q.y * x[0]) * ir, vy = (y[2] - q.y * y[0]) * ir;
+    const float ex = (x[3] - E * x[0]) * ir - fmaf(q.x, ux, q.y * vx);
+    const float ey = (y[3] - E * y[0]) * ir - fmaf(q.x, uy, q.y * vy);
+    a.vq[cell] = q;
+    a.vga[cell] = make_float4(ux, uy, vx, vy);
+    a.vgb[cell] = make_float2(ex * a.inv_cv, ey * a.inv_cv);
 }
 
 // Reconstruction of variable v of one cell.  live: lanes of the warp whose
@@ -131,7 +168,7 @@ __device__ __forceinline__ void robust_cell32(const TenoArgs& a, bool boundary, 
 // source makes the same for the whole warp.  Returns false when the source
 // failed (nothing written).  alive false: a lane past the mesh that only
 // takes part in the warp's collective steps (reads and writes nothing).
-template <int K, int M, int NQ, bool SEL, class IX, class SRC>
+template <int K, int M, int NQ, bool SEL, bool VG, class IX, class SRC>
 __device__ __forceinline__ bool teno32_cell(const TenoArgs& a, const float* __restrict__ U, float* __restrict__ fv,
                                             uint8_t* __restrict__ masks, const uint8_t* __restrict__ pred, int cell,
                                             int v, unsigned live, const IX& ix, SRC& src, bool alive = true) {
@@ -277,7 +314,8 @@ __device__ __forceinline__ bool teno32_cell(const TenoArgs& a, const float* __re
     const uint16_t* codes = src.codes();
     const bool fine = codes && ok && alive;
     const bool robust = a.bcell != nullptr;
-    if (!fine && !robust) return false;
+    const bool vgrad = VG && a.vq != nullptr;  // single-case layout (Ix1) only
+    if (!fine && !robust && !vgrad) return false;
     const unsigned code = fine ? src.ld(codes + lane) : 0u;
     float outv[NF][NQ];
     uint32_t slots[NF];
@@ -302,7 +340,31 @@ __device__ __forceinline__ bool teno32_cell(const TenoArgs& a, const float* __re
             outv[fl][q] = out;
         }
     }
-    if (robust) robust_cell32<NF, NQ>(a, fine && a.bcell[cell] != 0, have_range, live, uc, dlo, dhi, outv);
+    // the polynomial's gradient at the centroid (d/dxi, then the frame's
+    // inverse Jacobian)
+    float gx = 0.0f, gy = 0.0f;
+    if (vgrad) {
+        float g0 = 0.0f, g1 = 0.0f;
+#pragma unroll
+        for (int k = 0; k < KR; ++k) {
+            g0 = fmaf(c[k], a.dphif[2 * k], g0);
+            g1 = fmaf(c[k], a.dphif[2 * k + 1], g1);
+        }
+        const float4 J = fine ? __ldg(a.ji4 + cell) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        gx = fmaf(J.x, g0, J.z * g1);
+        gy = fmaf(J.y, g0, J.w * g1);
+    }
+    if (robust) {
+        const float keep = robust_cell32<NF, NQ>(a, fine && a.bcell[cell] != 0, have_range, live, uc, dlo, dhi, outv);
+        if (keep == 0.0f) {
+            gx = 0.0f;
+            gy = 0.0f;
+        } else if (keep < 1.0f) {
+            gx *= keep;
+            gy *= keep;
+        }
+    }
+    if (vgrad) write_visc_grad32(a, cell, v, live, uc, gx, gy, fine);
     if (!fine) return false;
 #pragma unroll
     for (int fl = 0; fl < NF; ++fl) {
@@ -314,7 +376,7 @@ __device__ __forceinline__ bool teno32_cell(const TenoArgs& a, const float* __re
     return true;
 }
 
-template <int K, int M, int NQ, bool SEL, int BS, int MINB>
+template <int K, int M, int NQ, bool SEL, int BS, int MINB, bool VG>
 __global__ void __launch_bounds__(BS, MINB) teno32_kernel(const TenoArgs a, const float* __restrict__ U,
                                                           float* __restrict__ fv, uint8_t* __restrict__ masks,
                                                           const uint8_t* __restrict__ pred) {
@@ -323,7 +385,7 @@ __global__ void __launch_bounds__(BS, MINB) teno32_kernel(const TenoArgs a, cons
     const unsigned live = __ballot_sync(0xffffffffu, cell < a.n_cells);
     if (cell >= a.n_cells) return;
     GlobalSrc<K, M, NQ> src{a, cell >> 3};
-    teno32_cell<K, M, NQ, SEL>(a, U, fv, masks, pred, cell, v, live, Ix1{}, src);
+    teno32_cell<K, M, NQ, SEL, VG>(a, U, fv, masks, pred, cell, v, live, Ix1{}, src);
 }
 
 // Staged form: each warp (one 8-cell tile) copies the table blocks of the
@@ -451,7 +513,7 @@ struct StageSrc {
     __device__ __forceinline__ T ld(const T* p) const { return *p; }
 };
 
-template <int K, int M, int NQ, bool SEL, int NSLOT, int WARPS, int MINB>
+template <int K, int M, int NQ, bool SEL, int NSLOT, int WARPS, int MINB, bool VG>
 __global__ void __launch_bounds__(WARPS * 32, MINB) teno32_staged_kernel(const TenoArgs a, const float* __restrict__ U,
                                                                          float* __restrict__ fv,
                                                                          uint8_t* __restrict__ masks,
@@ -477,7 +539,7 @@ __global__ void __launch_bounds__(WARPS * 32, MINB) teno32_staged_kernel(const T
     const int cell = tile * 8 + (lane32 >> 2), v = lane32 & 3;
     // cells past the mesh take part in the warp's collective steps with
     // nothing to do: smask 0, no prediction, no writes
-    teno32_cell<K, M, NQ, SEL>(a, U, fv, masks, pred, cell, v, 0xffffffffu, Ix1{}, src, cell < a.n_cells);
+    teno32_cell<K, M, NQ, SEL, VG>(a, U, fv, masks, pred, cell, v, 0xffffffffu, Ix1{}, src, cell < a.n_cells);
     if (!src.ok) {
         // a wait ran out: flag it and give every copy still pending on this
         // warp's stage one more bounded wait before the shared memory goes
@@ -518,12 +580,6 @@ __device__ __forceinline__ void primitives_guarded(const GasParams& g, const flo
 // same operations in FP32 here)
 // ---------------------------------------------------------------------------
 
-__device__ __forceinline__ float4 uvT32(const float4 x, float inv_cv) {
-    const float ir = __frcp_rn(x.x);
-    const float u = x.y * ir, v = x.z * ir;
-    const float e = x.w * ir - 0.5f * (u * u + v * v);
-    return make_float4(u, v, e * inv_cv, 0.0f);
-}
 
 __global__ void __launch_bounds__(256) visc_grad32_kernel(const Visc32Args a, const BcTable bct,
                                                           const float* __restrict__ U) {
@@ -811,23 +867,23 @@ cudaError_t flux_nq(const FluxArgs& a, const float* fv, const GasParams& g, cons
     return cudaErrorInvalidValue;
 }
 
-template <int K, int M, int NQ, bool SEL, int BS, int MINB>
+template <int K, int M, int NQ, bool SEL, int BS, int MINB, bool VG>
 cudaError_t teno_go1(const TenoArgs& a, const float* U, float* fv, uint8_t* masks, const uint8_t* pred,
                      cudaStream_t s) {
     const long long threads = (long long)a.n_cells * 4;
     const unsigned blocks = (unsigned)((threads + BS - 1) / BS);
-    if (blocks) teno32_kernel<K, M, NQ, SEL, BS, MINB><<<blocks, BS, 0, s>>>(a, U, fv, masks, pred);
+    if (blocks) teno32_kernel<K, M, NQ, SEL, BS, MINB, VG><<<blocks, BS, 0, s>>>(a, U, fv, masks, pred);
     return cudaGetLastError();
 }
 
 // Staged form (teno32_staged_kernel): one warp per tile, WARPS per block.
-template <int K, int M, int NQ, bool SEL, int NSLOT, int WARPS, int MINB>
+template <int K, int M, int NQ, bool SEL, int NSLOT, int WARPS, int MINB, bool VG>
 cudaError_t teno_staged1(const TenoArgs& a, const float* U, float* fv, uint8_t* masks, const uint8_t* pred,
                          cudaStream_t s) {
     constexpr unsigned smem = WARPS * StageLayout<K, M, NQ, NSLOT>::WARP;
     static bool attr = false;
     if (!attr) {
-        const cudaError_t e = cudaFuncSetAttribute(teno32_staged_kernel<K, M, NQ, SEL, NSLOT, WARPS, MINB>,
+        const cudaError_t e = cudaFuncSetAttribute(teno32_staged_kernel<K, M, NQ, SEL, NSLOT, WARPS, MINB, VG>,
                                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         attr = true;
@@ -835,7 +891,7 @@ cudaError_t teno_staged1(const TenoArgs& a, const float* U, float* fv, uint8_t* 
     const long long tiles = ((long long)a.n_cells + 7) / 8;
     const unsigned blocks = (unsigned)((tiles + WARPS - 1) / WARPS);
     if (blocks)
-        teno32_staged_kernel<K, M, NQ, SEL, NSLOT, WARPS, MINB><<<blocks, WARPS * 32, smem, s>>>(a, U, fv, masks, pred,
+        teno32_staged_kernel<K, M, NQ, SEL, NSLOT, WARPS, MINB, VG><<<blocks, WARPS * 32, smem, s>>>(a, U, fv, masks, pred,
                                                                                                a.err);
     return cudaGetLastError();
 }
@@ -845,20 +901,20 @@ cudaError_t teno_staged1(const TenoArgs& a, const float* U, float* fv, uint8_t* 
 // 4-7 are the staged form (p = 3): one stencil slot per warp, 4 warps per
 // block, at most 80 registers; two slots, 2 warps, 128; one slot, 4 warps,
 // 128; one slot, 4 warps, at most 72 registers (7 blocks per SM).
-template <int K, int M, int NQ, bool SEL>
+template <int K, int M, int NQ, bool SEL, bool VG>
 cudaError_t teno_go(const TenoArgs& a, const float* U, float* fv, uint8_t* masks, const uint8_t* pred, int shape,
                     cudaStream_t s) {
     switch (shape) {
-        case 0: return teno_go1<K, M, NQ, SEL, 128, 4>(a, U, fv, masks, pred, s);
-        case 1: return teno_go1<K, M, NQ, SEL, 128, 6>(a, U, fv, masks, pred, s);
-        case 2: return teno_go1<K, M, NQ, SEL, 128, 8>(a, U, fv, masks, pred, s);
-        case 3: return teno_go1<K, M, NQ, SEL, 256, 4>(a, U, fv, masks, pred, s);
+        case 0: return teno_go1<K, M, NQ, SEL, 128, 4, VG>(a, U, fv, masks, pred, s);
+        case 1: return teno_go1<K, M, NQ, SEL, 128, 6, VG>(a, U, fv, masks, pred, s);
+        case 2: return teno_go1<K, M, NQ, SEL, 128, 8, VG>(a, U, fv, masks, pred, s);
+        case 3: return teno_go1<K, M, NQ, SEL, 256, 4, VG>(a, U, fv, masks, pred, s);
     }
     if constexpr (K == 10 && M == 20 && NQ == 2) {
-        if (shape == 4) return teno_staged1<K, M, NQ, SEL, 1, 4, 6>(a, U, fv, masks, pred, s);
-        if (shape == 5) return teno_staged1<K, M, NQ, SEL, 2, 2, 7>(a, U, fv, masks, pred, s);
-        if (shape == 6) return teno_staged1<K, M, NQ, SEL, 1, 4, 4>(a, U, fv, masks, pred, s);
-        if (shape == 7) return teno_staged1<K, M, NQ, SEL, 1, 4, 7>(a, U, fv, masks, pred, s);
+        if (shape == 4) return teno_staged1<K, M, NQ, SEL, 1, 4, 6, VG>(a, U, fv, masks, pred, s);
+        if (shape == 5) return teno_staged1<K, M, NQ, SEL, 2, 2, 7, VG>(a, U, fv, masks, pred, s);
+        if (shape == 6) return teno_staged1<K, M, NQ, SEL, 1, 4, 4, VG>(a, U, fv, masks, pred, s);
+        if (shape == 7) return teno_staged1<K, M, NQ, SEL, 1, 4, 7, VG>(a, U, fv, masks, pred, s);
     }
     return cudaErrorInvalidValue;
 }
@@ -887,7 +943,7 @@ __global__ void __launch_bounds__(BS, MINB) teno32_batch_kernel(const BatchLaunc
         const unsigned live = __ballot_sync(0xffffffffu, on);
         if (!on) continue;
         GlobalSrc<K, M, NQ> src{b.teno[gi], cell >> 3};
-        teno32_cell<K, M, NQ, false>(b.teno[gi], U, b.fv, nullptr, nullptr, cell, v, live,
+        teno32_cell<K, M, NQ, false, false>(b.teno[gi], U, b.fv, nullptr, nullptr, cell, v, live,
                                      IxB{b.ubase[gi], b.fbase[gi], C, cs}, src);
     }
 }
@@ -968,7 +1024,7 @@ __global__ void __launch_bounds__(WARPS * 32, MINB) teno32_batch_staged_kernel(c
     __syncwarp();
     src.prefetch_central();
     const int cell = tile * 8 + (lane32 >> 2), v = lane32 & 3;
-    teno32_cell<K, M, NQ, false>(a, U, b.fv, nullptr, nullptr, cell, v, 0xffffffffu,
+    teno32_cell<K, M, NQ, false, false>(a, U, b.fv, nullptr, nullptr, cell, v, 0xffffffffu,
                                  IxB{b.ubase[gi], b.fbase[gi], C, cs}, src, cell < b.n_cells[gi]);
     if (!src.ok) {
         if (lane32 == 0) atomicOr(b.flags + gc, 4u);
@@ -1054,7 +1110,7 @@ __global__ void __launch_bounds__(WARPS * 32, MINB) teno32_batch_resident_kernel
     const int cell = tile * 8 + (lane32 >> 2), v = lane32 & 3;
     for (unsigned cs = warp; cs < C; cs += WARPS) {
         if (b.flags[b.case0[gi] + cs] != 0u) continue;
-        teno32_cell<K, M, NQ, false>(a, U, b.fv, nullptr, nullptr, cell, v, 0xffffffffu,
+        teno32_cell<K, M, NQ, false, false>(a, U, b.fv, nullptr, nullptr, cell, v, 0xffffffffu,
                                      IxB{b.ubase[gi], b.fbase[gi], C, cs}, src, cell < n);
     }
 }
@@ -1141,15 +1197,24 @@ cudaError_t launch_flux_batch(const BatchLaunch& b, const GasParams& g, const Bc
 
 cudaError_t launch_teno(const TenoArgs& a, int K, int M, int nq, const float* U, float* fv, uint8_t* masks,
                         int shape, cudaStream_t s) {
-    if (K == 10 && M == 20 && nq == 2) return teno_go<10, 20, 2, false>(a, U, fv, masks, nullptr, shape, s);
-    if (K == 6 && M == 12 && nq == 1) return teno_go1<6, 12, 1, false, 128, 4>(a, U, fv, masks, nullptr, s);
-    if (K == 3 && M == 6 && nq == 1) return teno_go1<3, 6, 1, false, 128, 4>(a, U, fv, masks, nullptr, s);
+    // viscous gradients from the reconstruction in their own instantiations
+    if (a.vq) {
+        if (K == 10 && M == 20 && nq == 2) return teno_go<10, 20, 2, false, true>(a, U, fv, masks, nullptr, shape, s);
+        if (K == 6 && M == 12 && nq == 1) return teno_go1<6, 12, 1, false, 128, 4, true>(a, U, fv, masks, nullptr, s);
+        if (K == 3 && M == 6 && nq == 1) return teno_go1<3, 6, 1, false, 128, 4, true>(a, U, fv, masks, nullptr, s);
+        return cudaErrorInvalidValue;
+    }
+    if (K == 10 && M == 20 && nq == 2) return teno_go<10, 20, 2, false, false>(a, U, fv, masks, nullptr, shape, s);
+    if (K == 6 && M == 12 && nq == 1) return teno_go1<6, 12, 1, false, 128, 4, false>(a, U, fv, masks, nullptr, s);
+    if (K == 3 && M == 6 && nq == 1) return teno_go1<3, 6, 1, false, 128, 4, false>(a, U, fv, masks, nullptr, s);
     return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_teno_selected(const TenoArgs& a, int K, int M, int nq, const float* U, const uint8_t* pred,
                                  float* fv, uint8_t* masks, int shape, cudaStream_t s) {
-    if (K == 10 && M == 20 && nq == 2) return teno_go<10, 20, 2, true>(a, U, fv, masks, pred, shape, s);
+    if (K == 10 && M == 20 && nq == 2)
+        return a.vq ? teno_go<10, 20, 2, true, true>(a, U, fv, masks, pred, shape, s)
+                    : teno_go<10, 20, 2, true, false>(a, U, fv, masks, pred, shape, s);
     return cudaErrorInvalidValue;
 }
 

@@ -459,6 +459,22 @@ void mgpu_ctx::build() {
                 teno.oi2[i * KR + l] = l < i ? 0.0 : (l == i ? 1.0 : 2.0) * t.oi[(size_t)(i + 1) * K + (l + 1)];
                 teno.oi2f[i * KR + l] = (float)teno.oi2[i * KR + l];
             }
+        // basis gradients at the reference centroid (1/3, 1/3), for the
+        // viscous gradients from the reconstruction (the monomial basis with
+        // the plain derivative p x^(p-1), not the (p+1) factor the reference
+        // uses in its oscillation indicator)
+        auto d1 = [&](int p, double x) {
+            if (t.basis == MGPU_BASIS_MONOMIAL) return p == 0 ? 0.0 : (double)p * std::pow(x, (double)(p - 1));
+            return basis_1d_deriv(t.basis, 1, p, x);
+        };
+        for (int k = 1; k < K; ++k) {
+            const int px = t.pidx[2 * k], py = t.pidx[2 * k + 1];
+            const double x = 1.0 / 3.0;
+            teno.dphi[2 * (k - 1)] = d1(px, x) * basis_1d(t.basis, py, x);
+            teno.dphi[2 * (k - 1) + 1] = basis_1d(t.basis, px, x) * d1(py, x);
+            teno.dphif[2 * (k - 1)] = (float)teno.dphi[2 * (k - 1)];
+            teno.dphif[2 * (k - 1) + 1] = (float)teno.dphi[2 * (k - 1) + 1];
+        }
         if (f32) {
             nb4.upload(h_nb4);
             if (gpu_lsq) P4.alloc(tiles * S * GP * TILE * 4);
@@ -624,6 +640,36 @@ void mgpu_ctx::build() {
             visc32.cp_over_pr = (float)visc.cp_over_pr;
             visc32.inv_cv = (float)(1.0 / gas.cv);
         }
+        if (recon_grads()) {
+            // per cell the inverse Jacobian of its TENO reference frame
+            // (nodes 0, 1, 2 at (0,0), (1,0), (0,1)), as the tables use it
+            std::vector<double> h_ji((size_t)N * 4);
+            for (uint32_t c = 0; c < N; ++c) {
+                const uint32_t* nc = mv.nodes_of_cell + mv.offsets_nodes_of_cell[cell_old[c]];
+                double J[4];
+                tri_jacobian(mv.node_coords + 2 * (size_t)nc[0], mv.node_coords + 2 * (size_t)nc[1],
+                             mv.node_coords + 2 * (size_t)nc[2], J);
+                mat2_inverse(J, &h_ji[4 * (size_t)c]);
+            }
+            teno.cv = gas.cv;
+            teno.inv_cv = (float)(1.0 / gas.cv);
+            if (single()) {
+                std::vector<float4> h4(N);
+                for (uint32_t c = 0; c < N; ++c)
+                    h4[c] = make_float4((float)h_ji[4 * (size_t)c], (float)h_ji[4 * (size_t)c + 1],
+                                        (float)h_ji[4 * (size_t)c + 2], (float)h_ji[4 * (size_t)c + 3]);
+                ji4.upload(h4);
+                teno.ji4 = ji4.p;
+                teno.vq = vq.p;
+                teno.vga = vga.p;
+                teno.vgb = vgb.p;
+            } else {
+                ji.upload(h_ji);
+                teno.ji = ji.p;
+                teno.vgrad = grad.p;
+                visc.grad_ready = 1;
+            }
+        }
     }
     // compulsory bytes of one stage: reconstruction + flux (face states in,
     // G out, face geometry) + update (G gathered, state in/out)
@@ -668,6 +714,7 @@ void mgpu_config_defaults(mgpu_config* c) {
     c->sutherland_S = 0.0;
     c->prandtl = 0.72;
     c->table_build = MGPU_TABLES_GPU;
+    c->viscous_gradients = MGPU_VISC_GRAD_RECON;
 }
 
 int mgpu_create(const mgpu_mesh* mesh, const mgpu_config* cfg, mgpu_ctx** out) {
@@ -683,6 +730,8 @@ int mgpu_create(const mgpu_mesh* mesh, const mgpu_config* cfg, mgpu_ctx** out) {
             throw Unsupported("unknown precision mode");
         if (cfg->table_build != MGPU_TABLES_GPU && cfg->table_build != MGPU_TABLES_HOST)
             throw ArgFail("table_build: MGPU_TABLES_GPU or MGPU_TABLES_HOST");
+        if (cfg->viscous_gradients != MGPU_VISC_GRAD_RECON && cfg->viscous_gradients != MGPU_VISC_GRAD_GREEN_GAUSS)
+            throw ArgFail("viscous_gradients: MGPU_VISC_GRAD_RECON or MGPU_VISC_GRAD_GREEN_GAUSS");
         if (cfg->viscous && !(cfg->mu_ref >= 0.0 && cfg->prandtl > 0.0 && (cfg->sutherland_S <= 0.0 || cfg->T_mu_ref > 0.0)))
             throw ArgFail("viscous flux: mu_ref >= 0, prandtl > 0 and, with Sutherland's law, T_mu_ref > 0");
         if (cfg->precision == MGPU_PREC_FP32 &&

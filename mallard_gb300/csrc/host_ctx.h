@@ -110,6 +110,10 @@ struct mgpu_ctx {
     DevArray<float4> vgeo, vq, vga;
     DevArray<float2> vgeo2, vgb;
     Visc32Args visc32{};
+    // viscous gradients from the reconstruction: per cell the inverse
+    // Jacobian of its reference frame
+    DevArray<double> ji;
+    DevArray<float4> ji4;
     DevArray<int8_t> bcidx;
     DevArray<int4> gat, cfaces;
     DevArray<uint32_t> nb, cface;
@@ -176,6 +180,10 @@ struct mgpu_ctx {
     }
 
     bool fast() const { return cfg.precision == MGPU_PREC_FP64_FAST; }
+    // the viscous flux's cell gradients come from the reconstruction
+    bool recon_grads() const {
+        return cfg.viscous && cfg.recon == MGPU_RECON_TENO && cfg.viscous_gradients == MGPU_VISC_GRAD_RECON;
+    }
     bool single() const { return cfg.precision == MGPU_PREC_FP32; }
     // reciprocal-based update and time step (every form but the exact one)
     bool rcp() const { return cfg.precision != MGPU_PREC_FP64; }
@@ -215,7 +223,7 @@ struct mgpu_ctx {
         timed(1, [&] { return launch_visc(Uin); });
     }
     void viscous_gradients32(const float* Uin) {
-        if (!cfg.viscous) return;
+        if (!cfg.viscous || recon_grads()) return;
         timed(1, [&] { return f32::launch_visc_grad(visc32, bct, Uin, stream); });
     }
     cudaError_t launch_visc(const double* Uin) { return launch_viscous(visc, gas, bct, Uin, stream); }

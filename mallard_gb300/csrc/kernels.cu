@@ -337,7 +337,8 @@ cudaError_t launch_sound(int n, double gamma, const double* U, const double* pri
 }
 
 cudaError_t launch_viscous(const ViscArgs& a, const GasParams& g, const BcTable& bct, const double* U, cudaStream_t s) {
-    if (a.n_cells > 0) grad_kernel<<<(a.n_cells + 255) / 256, 256, 0, s>>>(a, g, bct, U);
+    // the reconstruction wrote the gradients when grad_ready
+    if (a.n_cells > 0 && !a.grad_ready) grad_kernel<<<(a.n_cells + 255) / 256, 256, 0, s>>>(a, g, bct, U);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     if (a.n_faces > 0) viscous_kernel<<<(a.n_faces + 255) / 256, 256, 0, s>>>(a, g, bct, U);

@@ -33,12 +33,14 @@ namespace {
 // admissible (density positive and 2 rho E > |rho u|^2) takes its average
 // at every face point.  live: the warp's lanes
 // whose cells exist; the four lanes of a cell exchange their variables.
+// Returns the factor the variable's polynomial was scaled by (1: kept, 0:
+// replaced by the average).
 template <int NF, int NQ>
-__device__ __forceinline__ void robust_cell(const TenoArgs& a, int cell, unsigned live, double uc, double dlo,
-                                            double dhi, double (&out)[NF][NQ]) {
+__device__ __forceinline__ double robust_cell(const TenoArgs& a, int cell, unsigned live, double uc, double dlo,
+                                              double dhi, double (&out)[NF][NQ]) {
     const bool boundary = a.bcell[cell] != 0;
+    double th = 1.0;
     if (!boundary) {
-        double th = 1.0;
 #pragma unroll
         for (int fl = 0; fl < NF; ++fl)
 #pragma unroll
@@ -71,6 +73,46 @@ __device__ __forceinline__ void robust_cell(const TenoArgs& a, int cell, unsigne
         for (int fl = 0; fl < NF; ++fl)
 #pragma unroll
             for (int q = 0; q < NQ; ++q) out[fl][q] = uc;
+    return bad ? 0.0 : th;
+}
+
+// Viscous gradients from the reconstruction: lane v holds the gradient
+// (gx, gy) of conserved variable v's polynomial at the cell centroid and
+// the cell average uc; the cell's lane 0 writes the (u, v, T) gradients
+// (the averages' primitives, as uvT computes them, and the quotient rule).
+__device__ __forceinline__ void write_visc_grad(const TenoArgs& a, int cell, int v, unsigned live, double uc,
+                                                double gx, double gy) {
+    double r[4], x[4], y[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        r[i] = __shfl_sync(live, uc, i, 4);
+        x[i] = __shfl_sync(live, gx, i, 4);
+        y[i] = __shfl_sync(live, gy, i, 4);
+    }
+    if (v != 0) return;
+    const double rho = r[0];
+#if MGPU_FAST
+    const double ir = 1.0 / rho;
+    const double u = r[1] * ir, w = r[2] * ir, E = r[3] * ir;
+    const double ux = (x[1] - u * x[0]) * ir, uy = (y[1] - u * y[0]) * ir;
+    const double vx = (x[2] - w * x[0]) * ir, vy = (y[2] - w * y[0]) * ir;
+    const double ex = (x[3] - E * x[0]) * ir - (u * ux + w * vx), ey = (y[3] - E * y[0]) * ir - (u * uy + w * vy);
+    const double icv = 1.0 / a.cv;
+    const double Tx = ex * icv, Ty = ey * icv;
+#else
+    const double u = r[1] / rho, w = r[2] / rho, E = r[3] / rho;
+    const double ux = (x[1] - u * x[0]) / rho, uy = (y[1] - u * y[0]) / rho;
+    const double vx = (x[2] - w * x[0]) / rho, vy = (y[2] - w * y[0]) / rho;
+    const double ex = (x[3] - E * x[0]) / rho - (u * ux + w * vx), ey = (y[3] - E * y[0]) / rho - (u * uy + w * vy);
+    const double Tx = ex / a.cv, Ty = ey / a.cv;
+#endif
+    double* g = a.vgrad + (size_t)cell * 6;
+    g[0] = ux;
+    g[1] = uy;
+    g[2] = vx;
+    g[3] = vy;
+    g[4] = Tx;
+    g[5] = Ty;
 }
 
 template <int K, int M, int NQ, int VARIANT>
@@ -80,7 +122,8 @@ __global__ void __launch_bounds__(128) teno_kernel(const TenoArgs a, const doubl
     constexpr bool ROBUST = VARIANT == MGPU_TENO_ROBUST;
     const int gt = blockIdx.x * blockDim.x + threadIdx.x;
     const int cell = gt >> 2, v = gt & 3;
-    const unsigned live = ROBUST ? __ballot_sync(0xffffffffu, cell < a.n_cells) : 0u;
+    const bool vgrad = a.vgrad != nullptr;
+    const unsigned live = (ROBUST || vgrad) ? __ballot_sync(0xffffffffu, cell < a.n_cells) : 0u;
     if (cell >= a.n_cells) return;
     const int tile = cell >> 3, lane = cell & 7;
     const double uc = U[(size_t)cell * NC + v];
@@ -200,7 +243,41 @@ __global__ void __launch_bounds__(128) teno_kernel(const TenoArgs a, const doubl
             outv[fl][q] = out;
         }
     }
-    if (ROBUST) robust_cell<NF, NQ>(a, cell, live, uc, dlo, dhi, outv);
+    // the polynomial's gradient at the centroid (d/dxi, then the frame's
+    // inverse Jacobian), summed in the face evaluation's order
+    double gx = 0.0, gy = 0.0;
+    if (vgrad) {
+        double g0 = 0.0, g1 = 0.0;
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+            if (w[s] == 0.0) continue;
+#pragma unroll
+            for (int k = 0; k < KR; ++k) {
+#if MGPU_FAST
+                g0 = g0 + coef[s][k] * a.dphi[2 * k];
+                g1 = g1 + coef[s][k] * a.dphi[2 * k + 1];
+#else
+                const double ck = w[s] * coef[s][k];
+                g0 = g0 + ck * a.dphi[2 * k];
+                g1 = g1 + ck * a.dphi[2 * k + 1];
+#endif
+            }
+        }
+        const double* J = a.ji + (size_t)cell * 4;
+        gx = J[0] * g0 + J[2] * g1;
+        gy = J[1] * g0 + J[3] * g1;
+    }
+    if (ROBUST) {
+        const double keep = robust_cell<NF, NQ>(a, cell, live, uc, dlo, dhi, outv);
+        if (keep == 0.0) {
+            gx = 0.0;
+            gy = 0.0;
+        } else if (keep < 1.0) {
+            gx = keep * gx;
+            gy = keep * gy;
+        }
+    }
+    if (vgrad) write_visc_grad(a, cell, v, live, uc, gx, gy);
 #pragma unroll
     for (int fl = 0; fl < NF; ++fl) {
         const size_t f = slots[fl] >> 1;

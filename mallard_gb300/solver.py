@@ -82,8 +82,10 @@ class Solver:
                  rho_ref=1.225, p_min=-1e20, p_max=1e20, boundaries=(), teno_variant="reference", reorder=True,
                  device=0, precision="fp64", viscous=None, table_build="gpu"):
         """viscous: None for the Euler path, or a dict with mu_ref and
-        optionally T_mu_ref, sutherland_S, prandtl (the viscous face flux,
-        no counterpart in the reference; walls become no-slip).
+        optionally T_mu_ref, sutherland_S, prandtl and gradients ("recon":
+        the reconstructed polynomials' gradients, the default; or
+        "green_gauss") -- the viscous face flux, no counterpart in the
+        reference; walls become no-slip.
         table_build: "gpu" (least-squares tables built by a kernel; Legendre
         basis) or "host"; both give the same bits."""
         self._lib = N.lib()
@@ -124,6 +126,10 @@ class Solver:
             cfg.T_mu_ref = float(viscous.get("T_mu_ref", 1.0))
             cfg.sutherland_S = float(viscous.get("sutherland_S", 0.0))
             cfg.prandtl = float(viscous.get("prandtl", 0.72))
+            grads = viscous.get("gradients", "recon")
+            if grads not in N.VISC_GRADIENTS:
+                raise RuntimeError(f"Unknown viscous gradients: {grads}.")
+            cfg.viscous_gradients = N.VISC_GRADIENTS[grads]
         self.cfg = cfg
         self.nq = 1 if face_reconstruction == "FO" else (
             quadrature_order_face if quadrature_order_face > 0 else (basis_order + 1) // 2)

@@ -118,17 +118,18 @@ def wedge_viscosity(mach=2.5, rho=1.4, p=1.0, reynolds=1e5, length=1.0, prandtl=
 
 
 def wedge_setup(mesh, mach=2.5, rho=1.4, p=1.0, riemann="Rusanov", precision="fp64_fast", reynolds=None,
-                teno_variant="corrected"):
+                teno_variant="corrected", gradients="recon"):
     """Solver and initial state of the supersonic ramp channel: uniform inflow
     state everywhere, "upt" inflow, "p_out" outflow, walls (slip; no-slip
-    and viscous when a Reynolds number is given)."""
+    and viscous when a Reynolds number is given, with the viscous flux's
+    cell gradients from `gradients`: "recon" or "green_gauss")."""
     R = GAS["p_ref"] / (GAS["T_ref"] * GAS["rho_ref"])
     u = mach * float(np.sqrt(GAS["gamma"] * p / rho))
     T = p / (rho * R)
     blist = [{"name": "inflow", "type": "upt", "u": [u, 0.0], "p": p, "T": T},
              {"name": "outflow", "type": "p_out", "p": p},
              {"name": "wall", "type": "wall_adiabatic"}, {"name": "top", "type": "wall_adiabatic"}]
-    visc = wedge_viscosity(mach, rho, p, reynolds) if reynolds else None
+    visc = dict(wedge_viscosity(mach, rho, p, reynolds), gradients=gradients) if reynolds else None
     s = Solver(mesh, face_reconstruction="TENO", basis_type="legendre", basis_order=3, riemann_solver=riemann,
                boundaries=blist, teno_variant=teno_variant, precision=precision, viscous=visc, **GAS)
     n = mesh.n_cells

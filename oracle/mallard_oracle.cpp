@@ -1032,10 +1032,13 @@ struct Case {
     std::vector<Bc> bcs;
     std::vector<double> U, Utmp, prim, face, r1, r2, r3, r4, cfl_local;
     // viscous face flux (no reference counterpart; restated from the GPU
-    // library's definition): Sutherland viscosity, Green-Gauss gradients
+    // library's definition): Sutherland viscosity; cell gradients from the
+    // reconstructed polynomials (visc_grad 0, with TENO) or Green-Gauss
     bool viscous = false;
+    int visc_grad = 0;
     double mu_ref = 0.0, T_mu_ref = 1.0, sutherland_S = 0.0, cp_over_pr = 0.0;
     std::vector<double> grad;       // [n_cells][6]
+    std::vector<double> cgrad;      // [n_cells][4][2]: conserved variables' polynomial gradients
     std::vector<signed char> wall;  // per face: 1 on a wall_adiabatic zone
     // diagnostics: TENO decision per [cell][var]: bit0 central, bit s = stencil s passed CT2
     std::vector<uint8_t> masks;
@@ -1077,7 +1080,10 @@ inline bool robust_admissible(const double* W) {
     return W[0] > 0.0 && 2.0 * W[0] * W[3] > m2;
 }
 
-void robust_cell(Case& cs, uint32_t c, const double* U, double* face, const double* dlo, const double* dhi) {
+// keep[v]: the factor variable v's polynomial was scaled by (1 kept, 0
+// replaced by the average).
+void robust_cell(Case& cs, uint32_t c, const double* U, double* face, const double* dlo, const double* dhi,
+                 double* keep) {
     const OMesh& m = *cs.mesh;
     const int nq = cs.nq;
     const uint32_t fo = m.off_foc[c];
@@ -1090,6 +1096,7 @@ void robust_cell(Case& cs, uint32_t c, const double* U, double* face, const doub
     bool first_order = false;
     for (int fl = 0; fl < nf; fl++)
         if (m.cof[2 * (size_t)m.foc[fo + fl] + 1] < 0) first_order = true;
+    for (int v = 0; v < NC; ++v) keep[v] = 1.0;
     if (!first_order) {
         for (int v = 0; v < NC; ++v) {
             const double u = U[(size_t)c * NC + v];
@@ -1106,6 +1113,7 @@ void robust_cell(Case& cs, uint32_t c, const double* U, double* face, const doub
                         double& w = at(fl, q)[v];
                         w = u + th * (w - u);
                     }
+            keep[v] = th;
         }
         for (int fl = 0; fl < nf && !first_order; fl++)
             for (int q = 0; q < nq; q++)
@@ -1114,10 +1122,20 @@ void robust_cell(Case& cs, uint32_t c, const double* U, double* face, const doub
                     break;
                 }
     }
-    if (first_order)
+    if (first_order) {
         for (int fl = 0; fl < nf; fl++)
             for (int q = 0; q < nq; q++)
                 for (int v = 0; v < NC; ++v) at(fl, q)[v] = U[(size_t)c * NC + v];
+        for (int v = 0; v < NC; ++v) keep[v] = 0.0;
+    }
+}
+
+// Derivative of a 1D basis function for the polynomials' gradients: the
+// Legendre derivatives of basis.h, and p x^(p-1) for the monomial basis
+// (not the (p+1) factor the oscillation indicator's derivative carries).
+inline double grad1(int type, int p, double x) {
+    if (type == BASIS_LEGENDRE) return legendre_d(1, p, x);
+    return p == 0 ? 0.0 : (double)p * std::pow(x, (double)(p - 1));
 }
 
 // TENOFunctor::operator() (face_reconstruction.cpp:866-1039)
@@ -1192,6 +1210,25 @@ void recon_teno_cell(Case& cs, uint32_t c, const double* U, double* face) {
             for (int sl = 1; sl < gs; ++sl) sw[(size_t)sl * NC + v] /= sd;
         }
         if (!cs.masks.empty()) cs.masks[(size_t)c * NC + v] = mask;
+        if (!cs.cgrad.empty()) {
+            // the polynomial's gradient at the centroid (1/3, 1/3) of the
+            // reference frame, then x = Ji^T: summed in the face values' order
+            double g0 = 0.0, g1 = 0.0;
+            const double x = 1.0 / 3.0;
+            for (int sl = 0; sl < gs; sl++) {
+                if (sw[(size_t)sl * NC + v] == 0.0) continue;
+                for (int k = 1; k < K; k++) {
+                    const int px = t.pidx[2 * k], py = t.pidx[2 * k + 1];
+                    const double d0 = grad1(t.basis, px, x) * basis1(t.basis, py, x);
+                    const double d1 = basis1(t.basis, px, x) * grad1(t.basis, py, x);
+                    const double ck = sw[(size_t)sl * NC + v] * dw[(size_t)sl * K * NC + (size_t)k * NC + v];
+                    g0 = g0 + ck * d0;
+                    g1 = g1 + ck * d1;
+                }
+            }
+            cs.cgrad[((size_t)c * NC + v) * 2] = Ji[0] * g0 + Ji[2] * g1;
+            cs.cgrad[((size_t)c * NC + v) * 2 + 1] = Ji[1] * g0 + Ji[3] * g1;
+        }
         for (int fl = 0; fl < nf; fl++) {
             uint32_t f = m.foc[fo + fl];
             int side = m.cof[2 * (size_t)f] == (int32_t)c ? 0 : 1;
@@ -1218,7 +1255,21 @@ void recon_teno_cell(Case& cs, uint32_t c, const double* U, double* face) {
             }
         }
     }
-    if (cs.teno_variant == 2) robust_cell(cs, c, U, face, dlo, dhi);
+    if (cs.teno_variant == 2) {
+        double keep[NC];
+        robust_cell(cs, c, U, face, dlo, dhi, keep);
+        if (!cs.cgrad.empty())
+            for (int v = 0; v < NC; ++v) {
+                double* g = &cs.cgrad[((size_t)c * NC + v) * 2];
+                if (keep[v] == 0.0) {
+                    g[0] = 0.0;
+                    g[1] = 0.0;
+                } else if (keep[v] < 1.0) {
+                    g[0] = keep[v] * g[0];
+                    g[1] = keep[v] * g[1];
+                }
+            }
+    }
 }
 
 void recon(Case& cs, const double* U, double* face) {
@@ -1227,6 +1278,8 @@ void recon(Case& cs, const double* U, double* face) {
         return;
     }
     const OMesh& m = *cs.mesh;
+    if (cs.viscous && cs.visc_grad == 0) cs.cgrad.assign((size_t)m.n_cells * NC * 2, 0.0);
+    else cs.cgrad.clear();
 #pragma omp parallel for schedule(dynamic, 64) if (g_threads > 1) num_threads(g_threads)
     for (int64_t c = 0; c < (int64_t)m.n_cells; ++c) recon_teno_cell(cs, (uint32_t)c, U, face);
 }
@@ -1325,6 +1378,29 @@ inline void uvT(const Gas& g, const double* U, double* q) {
 void viscous_gradients(Case& cs, const double* U) {
     const OMesh& m = *cs.mesh;
     cs.grad.assign((size_t)m.n_cells * 6, 0.0);
+    if (cs.recon == RECON_TENO && cs.visc_grad == 0) {
+        // from the polynomials' gradients of the conserved variables and the
+        // cell averages: u = m0 / rho, v = m1 / rho, e = E - (u^2 + v^2) / 2,
+        // T = e / cv, by the quotient rule
+        for (uint32_t c = 0; c < m.n_cells; ++c) {
+            const double* r = U + (size_t)c * NC;
+            const double* g = &cs.cgrad[(size_t)c * NC * 2];
+            const double rho = r[0];
+            const double u = r[1] / rho, w = r[2] / rho, E = r[3] / rho;
+            const double ux = (g[2] - u * g[0]) / rho, uy = (g[3] - u * g[1]) / rho;
+            const double vx = (g[4] - w * g[0]) / rho, vy = (g[5] - w * g[1]) / rho;
+            const double ex = (g[6] - E * g[0]) / rho - (u * ux + w * vx);
+            const double ey = (g[7] - E * g[1]) / rho - (u * uy + w * vy);
+            double* o = &cs.grad[(size_t)c * 6];
+            o[0] = ux;
+            o[1] = uy;
+            o[2] = vx;
+            o[3] = vy;
+            o[4] = ex / cs.gas.cv;
+            o[5] = ey / cs.gas.cv;
+        }
+        return;
+    }
     for (uint32_t c = 0; c < m.n_cells; ++c) {
         double qc[3], gx[3] = {0, 0, 0}, gy[3] = {0, 0, 0};
         uvT(cs.gas, U + (size_t)c * NC, qc);
@@ -1456,16 +1532,22 @@ void face_flux(Case& cs, uint32_t f, int bc, const Bc* b, const double* U, const
     }
 }
 
+// Faces of the no-slip adiabatic walls, for the viscous flux.
+void mark_walls(Case& cs) {
+    const OMesh& m = *cs.mesh;
+    cs.wall.assign(m.n_faces, 0);
+    for (const Bc& b : cs.bcs)
+        if (b.type == BC_WALL_ADIABATIC)
+            for (uint32_t k = m.zone_off[b.zone]; k < m.zone_off[b.zone + 1]; ++k) cs.wall[m.zone_faces[k]] = 1;
+}
+
 // Solver::calc_rhs (solver_rhs.cpp:44-115)
 void calc_rhs(Case& cs, const double* U, double* face, double* rhs) {
     const OMesh& m = *cs.mesh;
     for (size_t i = 0; i < (size_t)m.n_cells * NC; i++) rhs[i] = 0.0;
     recon(cs, U, face);
     if (cs.viscous) {
-        cs.wall.assign(m.n_faces, 0);
-        for (const Bc& b : cs.bcs)
-            if (b.type == BC_WALL_ADIABATIC)
-                for (uint32_t k = m.zone_off[b.zone]; k < m.zone_off[b.zone + 1]; ++k) cs.wall[m.zone_faces[k]] = 1;
+        mark_walls(cs);
         viscous_gradients(cs, U);
     }
     uint32_t z0 = m.zone_off[0], z1 = m.zone_off[1];
@@ -1855,6 +1937,10 @@ int orc_case_nq(void* h) { return static_cast<Case*>(h)->nq; }
 
 void orc_case_set_teno_variant(void* h, int variant) { static_cast<Case*>(h)->teno_variant = variant; }
 
+// Cell gradients of the viscous flux: 0 from the reconstructed polynomials
+// (with TENO), 1 Green-Gauss.
+void orc_case_set_viscous_gradients(void* h, int kind) { static_cast<Case*>(h)->visc_grad = kind; }
+
 // Viscous face flux on (mu_ref > 0 or Sutherland) / off (viscous = 0).
 void orc_case_set_viscous(void* h, int viscous, double mu_ref, double T_mu_ref, double sutherland_S, double prandtl) {
     Case* cs = static_cast<Case*>(h);
@@ -1877,6 +1963,26 @@ int orc_case_face_values(void* h, const double* U, double* face, uint8_t* masks)
             std::memcpy(masks, cs.masks.data(), cs.masks.size());
             cs.masks.clear();
         }
+    });
+}
+
+// The viscous flux's cell gradients of state U, [n_cells][6]: du/dx, du/dy,
+// dv/dx, dv/dy, dT/dx, dT/dy (reconstructing first when they come from the
+// polynomials).
+int orc_case_viscous_gradients(void* h, const double* U, double* grad) {
+    Case& cs = *static_cast<Case*>(h);
+    return guarded([&] {
+        const OMesh& m = *cs.mesh;
+        const bool was = cs.viscous;
+        cs.viscous = true;
+        if (cs.recon == RECON_TENO && cs.visc_grad == 0) {
+            std::vector<double> face((size_t)m.n_faces * cs.nq * 2 * NC);
+            recon(cs, U, face.data());
+        }
+        mark_walls(cs);
+        viscous_gradients(cs, U);
+        cs.viscous = was;
+        std::copy(cs.grad.begin(), cs.grad.end(), grad);
     });
 }
 

@@ -81,6 +81,8 @@ def load():
         "orc_case_nq": (i32, [vp]),
         "orc_case_set_teno_variant": (None, [vp, i32]),
         "orc_case_set_viscous": (None, [vp, i32, f64, f64, f64, f64]),
+        "orc_case_set_viscous_gradients": (None, [vp, i32]),
+        "orc_case_viscous_gradients": (i32, [vp, vp, vp]),
         "orc_case_set_integrator": (None, [vp, i32]),
         "orc_fe_const_rhs": (None, [vp, vp, u32, f64]),
         "orc_rk4_const_rhs": (None, [vp, vp, u32, f64]),
@@ -203,10 +205,13 @@ class OracleCase:
         """SSPRK3 (default), FE or RK4 (time_integrator.cpp)."""
         self._lib.orc_case_set_integrator(self.h, {"SSPRK3": 0, "FE": 1, "RK4": 2}[name])
 
-    def set_viscous(self, mu_ref, T_mu_ref=1.0, sutherland_S=0.0, prandtl=0.72, viscous=True):
-        """The viscous face flux (no reference counterpart; see the C source)."""
+    def set_viscous(self, mu_ref, T_mu_ref=1.0, sutherland_S=0.0, prandtl=0.72, viscous=True, gradients="recon"):
+        """The viscous face flux (no reference counterpart; see the C source).
+        gradients: "recon" (the reconstructed polynomials', with TENO) or
+        "green_gauss"."""
         self._lib.orc_case_set_viscous(self.h, 1 if viscous else 0, float(mu_ref), float(T_mu_ref),
                                        float(sutherland_S), float(prandtl))
+        self._lib.orc_case_set_viscous_gradients(self.h, {"recon": 0, "green_gauss": 1}[gradients])
 
     def add_boundary(self, zone, bc_type, data=()):
         d = np.asarray(data, dtype=np.float64)
@@ -236,6 +241,14 @@ class OracleCase:
         R = np.empty((self.n_cells, 4))
         self._check(self._lib.orc_case_calc_rhs(self.h, _p(U), _p(R)))
         return R
+
+    def viscous_gradients(self, U):
+        """The viscous flux's cell gradients of U, [n_cells][6]: du/dx,
+        du/dy, dv/dx, dv/dy, dT/dx, dT/dy."""
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        G = np.empty((self.n_cells, 6))
+        self._check(self._lib.orc_case_viscous_gradients(self.h, _p(U), _p(G)))
+        return G
 
     def calc_dt(self, cfl):
         dt = C.c_double()

@@ -341,25 +341,30 @@ def test_ramp_channel_wedge_parity():
     s.close()
 
 
-@pytest.mark.parametrize("precision", ["fp64", "fp32"])
-def test_viscous_ramp_channel_parity(precision):
+@pytest.mark.parametrize("precision,gradients,variant", [
+    ("fp64", "recon", "corrected"), ("fp64", "green_gauss", "corrected"), ("fp64", "recon", "robust"),
+    ("fp32", "recon", "corrected"), ("fp32", "green_gauss", "corrected"), ("fp32", "recon", "robust")])
+def test_viscous_ramp_channel_parity(precision, gradients, variant):
     """The viscous face flux (no reference counterpart; the oracle restates
-    the library's definition): Green-Gauss gradients, Sutherland viscosity,
-    no-slip adiabatic walls, at an exaggerated viscosity (Re = 200) so that it
-    matters.  FP64: one residual at 1e-12 and 20 steps at 1e-10 against the
-    oracle; FP32 form: residual at its own tolerance (median 1e-5, maximum
-    1e-2 relative) and density L1 1e-5 after 20 steps."""
+    the library's definition): cell gradients from the reconstructed
+    polynomials (written by the reconstruction kernel) or Green-Gauss,
+    Sutherland viscosity, no-slip adiabatic walls, at an exaggerated
+    viscosity (Re = 200) so that it matters.  FP64: one residual at 1e-12 and
+    20 steps at 1e-10 against the oracle; FP32 form: residual at its own
+    tolerance (median 1e-5, maximum 1e-2 relative) and density L1 1e-5 after
+    20 steps."""
     from mallard_gb300.train_selector import wedge_setup, wedge_viscosity
     from cases import GAS
     from oracle import OracleCase, OracleMesh
     m = mg.Mesh.ramp_channel(36, 12, 3.0, 1.0, 0.5, 15.0, 0.2, seed=11)
     m.permute_cells(3)
-    s, U, W = wedge_setup(m, mach=2.5, precision=precision, reynolds=200.0)
+    s, U, W = wedge_setup(m, mach=2.5, precision=precision, reynolds=200.0, gradients=gradients,
+                          teno_variant=variant)
     visc = wedge_viscosity(2.5, reynolds=200.0)
     oc = OracleCase(OracleMesh.from_arrays(m), recon="TENO", basis="legendre", poly_order=3, riemann="Rusanov",
                     **GAS)
-    oc.set_teno_variant(1)
-    oc.set_viscous(visc["mu_ref"], visc["T_mu_ref"], visc["sutherland_S"], visc["prandtl"])
+    oc.set_teno_variant({"corrected": 1, "robust": 2}[variant])
+    oc.set_viscous(visc["mu_ref"], visc["T_mu_ref"], visc["sutherland_S"], visc["prandtl"], gradients=gradients)
     R = GAS["p_ref"] / (GAS["T_ref"] * GAS["rho_ref"])
     u = 2.5 * np.sqrt(GAS["gamma"] * 1.0 / 1.4)
     oc.add_boundary(m.zone_index("inflow"), "upt", (u, 0.0, 1.0, 1.0 / (1.4 * R)))
@@ -372,7 +377,7 @@ def test_viscous_ramp_channel_parity(precision):
     # the viscous part is not negligible at this Reynolds number
     oi = OracleCase(OracleMesh.from_arrays(m), recon="TENO", basis="legendre", poly_order=3, riemann="Rusanov",
                     **GAS)
-    oi.set_teno_variant(1)
+    oi.set_teno_variant({"corrected": 1, "robust": 2}[variant])
     for zone, typ, data in (("inflow", "upt", (u, 0.0, 1.0, 1.0 / (1.4 * R))), ("outflow", "p_out", (1.0,)),
                             ("wall", "wall_adiabatic", ()), ("top", "wall_adiabatic", ())):
         oi.add_boundary(m.zone_index(zone), typ, data)
