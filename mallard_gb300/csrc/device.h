@@ -289,6 +289,12 @@ cudaError_t launch_viscous(const ViscArgs& a, const GasParams& g, const BcTable&
 cudaError_t launch_dt(const unsigned long long* rmax_bits, double cfl, double* dt, double* t, unsigned* flags,
                       cudaStream_t s);
 cudaError_t launch_set_scalar(double* dst, double value, cudaStream_t s);
+// caller-order rows of a device-addressable host array <-> internal rows
+// (pos: caller row -> internal row), in one pass; load also writes the FP32
+// copy when dst32 is given
+cudaError_t launch_load_rows(int n, int width, const uint32_t* pos, const double* host, double* dst, float* dst32,
+                             cudaStream_t s);
+cudaError_t launch_store_rows(int n, int width, const uint32_t* pos, const double* src, double* host, cudaStream_t s);
 cudaError_t launch_permute_rows(int n, int width, const uint32_t* idx, const double* src, double* dst, bool scatter,
                                 cudaStream_t s);
 // dst[idx[c]] = src[c * stride] for c < n

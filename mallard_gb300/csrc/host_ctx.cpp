@@ -577,6 +577,11 @@ void mgpu_ctx::build() {
     masks.alloc((size_t)N * 4);
     staging.alloc((size_t)N * 5);
     perm_old.upload(cell_old);
+    {
+        std::vector<uint32_t> cell_new(N);
+        for (uint32_t c = 0; c < N; ++c) cell_new[cell_old[c]] = c;
+        perm_new.upload(cell_new);
+    }
     if (cfg.viscous) {
         std::vector<double2> h_xc(N), h_xf(F_real);
         for (uint32_t c = 0; c < N; ++c)
@@ -878,7 +883,7 @@ int mgpu_set_state(mgpu_ctx* ctx, const double* Uh, const double* primh) {
     if (int rc = need_ready(ctx)) return rc;
     return guarded([&] {
         if (!Uh) throw ArgFail("null state");
-        ctx->upload_cells(ctx->U.p, Uh, 4);
+        ctx->upload_cells(ctx->U.p, Uh, 4, ctx->single() ? ctx->U32.p : nullptr);
         if (ctx->single() && !primh) {
             // the FP32 form's step reads neither the FP64 primitives nor the
             // sound speeds: they are recovered from U when a caller asks
@@ -893,7 +898,6 @@ int mgpu_set_state(mgpu_ctx* ctx, const double* Uh, const double* primh) {
                "sound speed");
             ctx->prim_stale = false;
         }
-        if (ctx->single()) ck(launch_to_f32((size_t)ctx->N * 4, ctx->U.p, ctx->U32.p, ctx->stream), "FP32 copy");
         ck(cudaMemsetAsync(ctx->flags.p, 0, sizeof(unsigned), ctx->stream), "cudaMemsetAsync");
         ck(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
         return MGPU_OK;

@@ -125,6 +125,7 @@ struct mgpu_ctx {
     DevArray<uint8_t> smask, masks, bcell;
     DevArray<double> staging;      // caller-order rows for state transfers
     DevArray<uint32_t> perm_old;   // internal cell -> caller cell
+    DevArray<uint32_t> perm_new;   // caller cell -> internal cell
     TenoArgs teno{};
 
     // CUDA graphs of one CFL step, keyed by cfl: with the selector's
@@ -347,12 +348,34 @@ struct mgpu_ctx {
     // synchronised: stream order protects the staging array, and every
     // caller synchronises before it returns (the host buffer is borrowed
     // until then).
-    void upload_cells(double* dst, const double* src, int width) {
+    // The device's address of pinned host memory (null for other memory):
+    // such rows move in one kernel pass that also permutes them, instead of
+    // a copy into the staging array and a permutation.
+    static const double* pinned_view(const double* h) {
+        cudaPointerAttributes at{};
+        if (cudaPointerGetAttributes(&at, h) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        return at.type == cudaMemoryTypeHost ? static_cast<const double*>(at.devicePointer) : nullptr;
+    }
+    // dst32: the FP32 copy of the rows as well (width 4), or null
+    void upload_cells(double* dst, const double* src, int width, float* dst32 = nullptr) {
+        if (const double* hv = pinned_view(src)) {
+            ck(launch_load_rows((int)N, width, perm_new.p, hv, dst, dst32, stream), "load rows");
+            return;
+        }
         const size_t bytes = (size_t)N * width * sizeof(double);
         ck(cudaMemcpyAsync(staging.p, src, bytes, cudaMemcpyHostToDevice, stream), "H2D");
         ck(launch_permute_rows((int)N, width, perm_old.p, staging.p, dst, false, stream), "permute");
+        if (dst32) ck(launch_to_f32((size_t)N * width, dst, dst32, stream), "FP32 copy");
     }
     void download_cells(const double* src, double* dst, int width) {
+        if (const double* hv = pinned_view(dst)) {
+            ck(launch_store_rows((int)N, width, perm_new.p, src, const_cast<double*>(hv), stream), "store rows");
+            ck(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+            return;
+        }
         const size_t bytes = (size_t)N * width * sizeof(double);
         ck(launch_permute_rows((int)N, width, perm_old.p, src, staging.p, true, stream), "permute");
         ck(cudaMemcpyAsync(dst, staging.p, bytes, cudaMemcpyDeviceToHost, stream), "D2H");

@@ -252,6 +252,29 @@ __global__ void permute_rows_kernel(int n, int width, const uint32_t* __restrict
     else dst[(size_t)c * width + k] = src[o * width + k];
 }
 
+// Rows between a host array the device addresses directly (pinned memory)
+// in the caller's order and a device array in the internal order, in one
+// pass over the host side in its own order (coalesced): caller row i is
+// internal row pos[i].  load: dst[pos[i]] = host[i], and the FP32 copy of
+// each entry into dst32 when given (width 4); store: host[i] = src[pos[i]].
+__global__ void load_rows_kernel(int n, int width, const uint32_t* __restrict__ pos, const double* __restrict__ host,
+                                 double* __restrict__ dst, float* __restrict__ dst32) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)n * width) return;
+    const int i = (int)(t / width), k = (int)(t % width);
+    const size_t o = (size_t)pos[i] * width + k;
+    const double x = host[t];
+    dst[o] = x;
+    if (dst32) dst32[o] = f32_rn(x);
+}
+__global__ void store_rows_kernel(int n, int width, const uint32_t* __restrict__ pos, const double* __restrict__ src,
+                                  double* __restrict__ host) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)n * width) return;
+    const int i = (int)(t / width), k = (int)(t % width);
+    host[t] = src[(size_t)pos[i] * width + k];
+}
+
 // One column of a row-major array, scattered to caller order: dst[idx[c]] =
 // src[c * stride] (the output writer's snapshot).
 __global__ void permute_column_kernel(int n, int stride, const uint32_t* __restrict__ idx,
@@ -386,6 +409,23 @@ cudaError_t launch_permute_rows(int n, int width, const uint32_t* idx, const dou
     const unsigned blocks = (unsigned)((threads + 255) / 256);
     if (blocks == 0) return cudaSuccess;
     permute_rows_kernel<<<blocks, 256, 0, s>>>(n, width, idx, src, dst, scatter ? 1 : 0);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_load_rows(int n, int width, const uint32_t* pos, const double* host, double* dst, float* dst32,
+                             cudaStream_t s) {
+    const long long threads = (long long)n * width;
+    const unsigned blocks = (unsigned)((threads + 255) / 256);
+    if (blocks == 0) return cudaSuccess;
+    load_rows_kernel<<<blocks, 256, 0, s>>>(n, width, pos, host, dst, dst32);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_store_rows(int n, int width, const uint32_t* pos, const double* src, double* host, cudaStream_t s) {
+    const long long threads = (long long)n * width;
+    const unsigned blocks = (unsigned)((threads + 255) / 256);
+    if (blocks == 0) return cudaSuccess;
+    store_rows_kernel<<<blocks, 256, 0, s>>>(n, width, pos, src, host);
     return cudaGetLastError();
 }
 
