@@ -94,8 +94,8 @@ def test_fp32_primitives_and_time_step():
     s64.close()
 
 
-@pytest.mark.parametrize("learned", [False, True])
-def test_launch_shapes_agree(learned):
+@pytest.mark.parametrize("learned,variant", [(False, "corrected"), (True, "corrected"), (True, "robust")])
+def test_launch_shapes_agree(learned, variant):
     """Every launch shape of the FP32 reconstruction (including the staged
     kernel, which reads its tables from shared memory filled by bulk async
     copies) gives the same bits, with and without the learned selector; a
@@ -109,7 +109,7 @@ def test_launch_shapes_agree(learned):
     sel.load(default_weights_path())
     out = []
     for shape in range(8):
-        s, _ = make_pair(m, variant="corrected", precision="fp32")
+        s, _ = make_pair(m, variant=variant, precision="fp32")
         if learned:
             s.attach_selector(sel)
         s.set_launch_shape(shape)
@@ -120,5 +120,5 @@ def test_launch_shapes_agree(learned):
         out.append(s.get_state()[0])
         s.close()
     sel.close()
-    for shape in range(1, 7):
+    for shape in range(1, 8):
         np.testing.assert_array_equal(out[shape], out[0], err_msg=f"shape {shape}")
