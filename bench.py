@@ -365,8 +365,8 @@ def autotune(s, args, U0, W0):
     s.set_state(U0, W0)
     return {"chosen_shape": shape, "ms_per_shape": [round(x, 4) for x in tms],
             "shapes": "0: 128 thr/<=128 regs, 1: 128/<=80, 2: 128/<=64, 3: 256/<=64, "
-                      "4-7: staged (bulk copies to shared memory) 1 slot x 4 warps/<=80, 2 x 2/<=128, 1 x 4/<=128, "
-                      "1 x 4/<=72"}
+                      "4-7: staged (bulk copies to shared memory, 1 stencil slot per warp) 4 warps/<=80, "
+                      "2 warps/<=72, 1 warp/<=72, 4 warps/<=72"}
 
 
 def time_form(m, args, form, U0, W0, device, selector, barrier=None, clocks=None):

@@ -433,10 +433,10 @@ int mgpu_kernel_times(mgpu_ctx* ctx, double* ms, uint32_t* launches);
  * form at p = 3: 0-2 128-thread blocks with at most 128, 80 or 64 registers
  * per thread, 3 256-thread blocks with 64, 4-7 the staged kernel, whose
  * warps copy their tile's table blocks into shared memory with bulk async
- * copies: one stencil slot per warp and 4 warps per block with at most 80
- * registers, two slots and 2 warps, one slot and 4 warps with 128, one slot
- * and 4 warps with 72) on the current state, three launches each after a
- * warm-up, and keeps the fastest for later launches.
+ * copies, one stencil slot per warp: 4 warps per block with at most 80
+ * registers, then 2, 1 and 4 warps per block with at most 72) on the
+ * current state, three launches each after a warm-up, and keeps the
+ * fastest for later launches.
  * ms[MGPU_AUTOTUNE_SHAPES] receives the average time per shape (0 where not
  * applicable), best the chosen shape.  Both may be NULL.  Other forms have
  * a single shape. */

@@ -912,8 +912,8 @@ cudaError_t teno_go(const TenoArgs& a, const float* U, float* fv, uint8_t* masks
     }
     if constexpr (K == 10 && M == 20 && NQ == 2) {
         if (shape == 4) return teno_staged1<K, M, NQ, SEL, 1, 4, 6, VG>(a, U, fv, masks, pred, s);
-        if (shape == 5) return teno_staged1<K, M, NQ, SEL, 2, 2, 7, VG>(a, U, fv, masks, pred, s);
-        if (shape == 6) return teno_staged1<K, M, NQ, SEL, 1, 4, 4, VG>(a, U, fv, masks, pred, s);
+        if (shape == 5) return teno_staged1<K, M, NQ, SEL, 1, 2, 14, VG>(a, U, fv, masks, pred, s);
+        if (shape == 6) return teno_staged1<K, M, NQ, SEL, 1, 1, 28, VG>(a, U, fv, masks, pred, s);
         if (shape == 7) return teno_staged1<K, M, NQ, SEL, 1, 4, 7, VG>(a, U, fv, masks, pred, s);
     }
     return cudaErrorInvalidValue;

@@ -243,10 +243,13 @@ __device__ __forceinline__ void update_cell(const UpdateArgs& a, const StageStat
             for (int i = 0; i < NPR; i++) po[i] = p[i];
             st.snd[row] = sound_speed(g.gamma, u[0], p);
         }
-        bool ok = true;
+        // finite: the exponent field is not all ones (inf, NaN), tested on
+        // the high word's bits with integer instructions, which leaves the
+        // FP64 unit (this kernel's limit on GB300) to the update itself
+        unsigned bad = 0;
 #pragma unroll
-        for (int i = 0; i < 4; i++) ok = ok && isfinite(u[i]);
-        if (!ok) atomicOr(flag, 1u);
+        for (int i = 0; i < 4; i++) bad |= ((unsigned)__double2hiint(u[i]) & 0x7ff00000u) == 0x7ff00000u;
+        if (bad) atomicOr(flag, 1u);
     }
 }
 
