@@ -88,6 +88,7 @@ struct FluxArgs {
     int n_faces;            // faces that carry a flux
     const int2* lr;         // internal cell ids; y = -1 on boundary faces
     const double2* nrm;     // unit normal (reference unit<2> arithmetic, precomputed)
+    const float2* nrm32;    // the same rounded to FP32 once (FP32 form)
     const double* area;
     const int8_t* bc;       // -1 interior, else BcTable index
     const double* fv;
@@ -187,6 +188,7 @@ struct SpecArgs {
     double gamma;
     // FP32 form: the radius comes from the FP32 state rows (spectral32.cuh)
     const float4* u32;      // null in the FP64 forms
+    const float4* geo32;    // FP32 form: per face the unit normal and 1 / dxn rounded once, 0
     double p_min, p_max;
     float gamma_f, p_min_f, p_max_f;
 };

@@ -776,8 +776,8 @@ __device__ __forceinline__ void flux32_face(const FluxArgs& a, const float* __re
                                             const BcTable& bct, int fi, const IX& ix, const double* __restrict__ Ust,
                                             double* __restrict__ Gout, const Visc32Args* va = nullptr) {
     const int2 lr = a.lr[fi];
-    const double2 nn = a.nrm[fi];
-    const float n[2] = {f(nn.x), f(nn.y)};
+    const float2 nn = a.nrm32[fi];
+    const float n[2] = {nn.x, nn.y};
     const int bi = a.bc[fi];
     const int type = bi < 0 ? -1 : bct.bc[bi].type;
     float F[4] = {0.0f, 0.0f, 0.0f, 0.0f};
@@ -819,8 +819,8 @@ __global__ void __launch_bounds__(128) flux32_pair_kernel(const FluxArgs a, cons
     const unsigned live = __ballot_sync(0xffffffffu, fi < a.n_faces);
     if (fi >= a.n_faces) return;
     const int2 lr = a.lr[fi];
-    const double2 nn = a.nrm[fi];
-    const float n[2] = {f(nn.x), f(nn.y)};
+    const float2 nn = a.nrm32[fi];
+    const float n[2] = {nn.x, nn.y};
     const int bi = a.bc[fi];
     const int type = bi < 0 ? -1 : bct.bc[bi].type;
     float Ft[4], F[4];
@@ -978,8 +978,8 @@ __global__ void __launch_bounds__(128) flux32_pair_batch_kernel(const BatchLaunc
         const FluxArgs& a = b.flux[gi];
         const IxB ix{b.ubase[gi], b.fbase[gi], C, cs};
         const int2 lr = a.lr[fi];
-        const double2 nn = a.nrm[fi];
-        const float n[2] = {f(nn.x), f(nn.y)};
+        const float2 nn = a.nrm32[fi];
+        const float n[2] = {nn.x, nn.y};
         const int bi = a.bc[fi];
         const int type = bi < 0 ? -1 : bct.bc[bi].type;
         float Ft[4], F[4];

@@ -182,6 +182,7 @@ int mgpu_batch_finalize(mgpu_batch* b) {
             fa.n_faces = (int)c->F_flux;
             fa.lr = c->lr.p;
             fa.nrm = c->nrm.p;
+            fa.nrm32 = c->nrm32.p;
             fa.area = c->area.p;
             fa.bc = c->bcidx.p;
             fa.guard = c->cfg.teno_variant == MGPU_TENO_ROBUST;

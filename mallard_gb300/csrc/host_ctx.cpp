@@ -543,6 +543,12 @@ void mgpu_ctx::build() {
     // --- upload the rest
     lr.upload(h_lr);
     nrm.upload(h_nrm);
+    if (single()) {
+        // round to nearest once, as the kernels' FP64 -> FP32 conversion does
+        std::vector<float2> h_n32(F_real);
+        for (uint32_t i = 0; i < F_real; ++i) h_n32[i] = make_float2((float)h_nrm[i].x, (float)h_nrm[i].y);
+        nrm32.upload(h_n32);
+    }
     area.upload(h_area);
     dxn.upload(h_dxn);
     if (rcp()) {
@@ -551,6 +557,13 @@ void mgpu_ctx::build() {
         for (uint32_t c = 0; c < N; ++c) h_ivol[c] = 1.0 / h_vol[c];
         idxn.upload(h_idxn);
         ivol.upload(h_ivol);
+        if (single()) {
+            // rounded to nearest once, as the kernels' FP64 -> FP32 conversion does
+            std::vector<float4> h_g(F_real);
+            for (uint32_t i = 0; i < F_real; ++i)
+                h_g[i] = make_float4((float)h_nrm[i].x, (float)h_nrm[i].y, (float)h_idxn[i], 0.0f);
+            geo32.upload(h_g);
+        }
     }
     bcidx.upload(h_bc);
     gat.upload(h_gat);

@@ -101,6 +101,8 @@ struct mgpu_ctx {
     DevArray<unsigned long long> rmax;
     DevArray<int2> lr;
     DevArray<double2> nrm;
+    DevArray<float2> nrm32;  // FP32 form: the unit normals rounded once
+    DevArray<float4> geo32;  // FP32 form: unit normal and 1 / dxn rounded once (time step)
     DevArray<double> area, dxn, idxn, ivol, snd;
     // viscous flux: cell centres, face midpoints, gradients
     DevArray<double2> xc, xf;
@@ -234,6 +236,7 @@ struct mgpu_ctx {
         a.n_faces = (int)F_flux;
         a.lr = lr.p;
         a.nrm = nrm.p;
+        a.nrm32 = nrm32.p;
         a.area = area.p;
         a.bc = bcidx.p;
         a.fv = fv.p;
@@ -324,6 +327,7 @@ struct mgpu_ctx {
         s.p_max_f = gas.p_max_f;
         s.idxn = idxn.p;
         s.u32 = single() ? reinterpret_cast<const float4*>(U32.p) : nullptr;
+        s.geo32 = single() ? geo32.p : nullptr;
     }
 
     // The FP32 form's steps leave the FP64 primitives and sound speeds

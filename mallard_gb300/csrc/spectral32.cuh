@@ -54,8 +54,8 @@ __device__ __forceinline__ float spectral_cell32(const SpecArgs& a, int c, const
         const int f = ent[k];
         const int2 lr = a.lr[f];
         const int L = lr.x, R = lr.y < 0 ? lr.x : lr.y;
-        const double2 n = a.nrm[f];
-        const float nx = f32_rn(n.x), ny = f32_rn(n.y), idx = f32_rn(a.idxn[f]);
+        const float4 gf = a.geo32[f];
+        const float nx = gf.x, ny = gf.y, idx = gf.z;
         const float3 wl = velocity_sound32(a, a.u32[ix.u(L)]);
         const float3 wr = velocity_sound32(a, a.u32[ix.u(R)]);
         const float af = __fmul_rn(0.5f, __fadd_rn(wl.z, wr.z));
