@@ -773,7 +773,15 @@ def run_ours(args):
     for k in kshare:
         kshare[k]["algorithmic_bytes_per_launch"] = kernel_bytes(k, prec, learned, cells, faces, solver, stats)
         kshare[k]["achieved_gbs"] = kshare[k]["algorithmic_bytes_per_launch"] / (kshare[k]["ms_per_launch"] * 1e-3) / 1e9
-    algo = kshare[dom]["algorithmic_bytes_per_launch"]
+    if "selector" in kshare:
+        # a prediction is two launches (mlp_kernel<1>, then trust_kernel);
+        # its bytes are a prediction's
+        sk = kshare["selector"]
+        sk["launches_per_prediction"] = 2
+        sk["ms_per_prediction"] = 2 * sk["ms_per_launch"]
+        sk["algorithmic_bytes_per_prediction"] = sk.pop("algorithmic_bytes_per_launch")
+        sk["achieved_gbs"] = sk["algorithmic_bytes_per_prediction"] / (sk["ms_per_prediction"] * 1e-3) / 1e9
+    algo = kshare[dom].get("algorithmic_bytes_per_launch", kshare[dom].get("algorithmic_bytes_per_prediction"))
     achieved = kshare[dom]["achieved_gbs"]
     traffic = None
     tf = ROOT / "profiles" / "teno_recon_traffic.json"
