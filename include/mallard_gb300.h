@@ -256,7 +256,11 @@ int mgpu_synchronize(mgpu_ctx* ctx);
 /* State in the caller's cell order, [n_cells][4] and [n_cells][5].
  * set_state: primitives NULL recovers them on the device from U with the
  * reference's arithmetic (physics.h:842-867).  get_state: either output may
- * be NULL.  Host buffers (pinned or pageable) are borrowed for the call.
+ * be NULL.  Host buffers (pinned or pageable) are borrowed for the call;
+ * pinned ones (cudaHostAlloc / cudaHostRegister) must hold the whole array,
+ * as for a copy: a kernel reads or writes them in place, permuting the rows
+ * (and writing the FP32 form's copy) in the same pass, where pageable ones
+ * go through a device staging array. */
  * The FP32 form's steps carry no FP64 primitives (its flux and time step
  * read the FP32 state copy): after a step, get_state recovers them from U
  * as set_state does; before any step it returns the ones set_state had. */

@@ -347,14 +347,13 @@ struct mgpu_ctx {
     }
 
     // ---- host <-> device in caller numbering ------------------------------
-    // One copy engine transfer of the caller's buffer (pinned or pageable)
-    // into a staging array, then a permutation kernel on the device.  Not
-    // synchronised: stream order protects the staging array, and every
+    // Pinned host memory: one kernel pass reads (or writes) the caller's
+    // rows in place and permutes them.  Other memory: one copy-engine
+    // transfer into a staging array, then a permutation kernel.  Uploads are
+    // not synchronised: stream order protects the staging array, and every
     // caller synchronises before it returns (the host buffer is borrowed
     // until then).
-    // The device's address of pinned host memory (null for other memory):
-    // such rows move in one kernel pass that also permutes them, instead of
-    // a copy into the staging array and a permutation.
+    // The device's address of pinned host memory (null for other memory).
     static const double* pinned_view(const double* h) {
         cudaPointerAttributes at{};
         if (cudaPointerGetAttributes(&at, h) != cudaSuccess) {
