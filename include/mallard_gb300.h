@@ -260,7 +260,7 @@ int mgpu_synchronize(mgpu_ctx* ctx);
  * pinned ones (cudaHostAlloc / cudaHostRegister) must hold the whole array,
  * as for a copy: a kernel reads or writes them in place, permuting the rows
  * (and writing the FP32 form's copy) in the same pass, where pageable ones
- * go through a device staging array. */
+ * go through a device staging array.
  * The FP32 form's steps carry no FP64 primitives (its flux and time step
  * read the FP32 state copy): after a step, get_state recovers them from U
  * as set_state does; before any step it returns the ones set_state had. */
