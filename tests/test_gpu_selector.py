@@ -47,7 +47,8 @@ def test_inference_matches_bf16_oracle():
         p[mlp.OFF_B1:mlp.OFF_W2] = r.normal(0, 0.2, mlp.HID)
         p[mlp.OFF_B3:] = r.normal(0, 0.5, mlp.OUT)
         s.params = p
-        for n in (1, 127, 128, 1000):
+        # up to 60,000 rows: 469 row blocks, more CTAs than fit at once
+        for n in (1, 127, 128, 1000, 60000):
             X, _ = _rows(n, 10 + n)
             L, P = s.infer(X, threshold=0.6)
             Lo = mlp.infer_bf16(p, X)
@@ -205,12 +206,14 @@ def test_shipped_selector_error_and_work(problem, interval):
     assert frac < 0.8
 
 
-def test_in_solver_predictions_match_harvested_features():
+@pytest.mark.parametrize("n", [20, 160])
+def test_in_solver_predictions_match_harvested_features(n):
     """The FP32 form's in-solver inference (features built from the FP32
     stage state inside the tcgen05 kernel) predicts exactly what the
     stand-alone inference predicts from the harvested features of the same
-    state: same features, same BF16 operands, same logits."""
-    m = mg.Mesh.generate("cartesian_tri", 20, 20, 1.0, 1.0)
+    state: same features, same BF16 operands, same logits, on a small mesh
+    and on one of 51,200 cells (400 row blocks)."""
+    m = mg.Mesh.generate("cartesian_tri", n, n, 1.0, 1.0)
     U, W = explosion(m, radius=0.25)
     with Selector() as sel:
         sel.load(default_weights_path())
